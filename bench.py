@@ -1,0 +1,460 @@
+"""Benchmark of the KPM hot path: KPM nnz*vec*moment/s.
+
+Workload (default): the honeycomb (graphene) DOS workload -- 1000 x 1000
+unit cells (2e6 orbitals), hopping t = 1 with a Peierls phase of 1/1000 flux
+quanta per hexagon, Anderson disorder W = 0.5 (seed 0), R = 64 random-phase
+vectors (rng seed 1, the reference's stream), M = 2000 moments, DOS
+(operator=None), mixed precision (complex64 recursion, FP64 accumulation).
+Synthetic data built by kwant_gb300.lattices; the vector blocks (1 GB each)
+are larger than L2, so no L2 flush is needed between steps.
+
+A "step" is one complete moment computation (R vectors x M moments) of the
+workload.  value = nnz * R * M / (device time per step), with the Hamiltonian
+and vectors resident in HBM.  e2e is the same metric through the C ABI's
+one-shot kpm_dos() with pinned host buffers: Hamiltonian upload, vector
+upload, recursion, device reconstruction and result download every step.
+
+--impl reference times the reference's CPU algorithm (the oracle port of
+kwant.kpm: scipy CSR matvec + vdot, one vector at a time) on the host cores,
+one spawned process per core over disjoint vectors, on a bounded sample.
+"""
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'KPM nnz*vec*moment/s'
+UNIT = 'nnz*vec*moment/s'
+
+
+# ---------------------------------------------------------------- workload
+def make_workload(cells, vectors, seed_dis=0, seed_vec=1):
+    from kwant_gb300 import lattices
+    syst = lattices.honeycomb(cells, t=1.0, flux=1.0 / 1000, W=0.5,
+                              seed=seed_dis)
+    ham = syst.hamiltonian_submatrix(sparse=True).tocsr()
+    n = ham.shape[0]
+    rng = np.random.RandomState(seed_vec)
+    v0 = np.exp(2j * np.pi * rng.random_sample(n))   # the reference's _v0
+    vecs = np.empty((vectors, n), dtype=np.complex128)
+    for r in range(vectors):
+        vecs[r] = np.exp(2j * np.pi * rng.random_sample(n))
+    return ham, v0, vecs
+
+
+def step_bytes(nnz, n, R, precision):
+    """Algorithmic HBM bytes of one Chebyshev step over R vectors:
+    values + column indices + row pointers + read alpha_n, read alpha_{n-1},
+    write alpha_{n+1} (complex64 or complex128)."""
+    sv = 8 if precision == 'mixed' else 16
+    return nnz * sv + 4 * nnz + 4 * (n + 1) + 3 * n * R * sv
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ('clocks.sm,clocks.max.sm,clocks_event_reasons.active,'
+              'clocks_event_reasons.hw_slowdown,'
+              'clocks_event_reasons.hw_thermal_slowdown,'
+              'clocks_event_reasons.sw_thermal_slowdown,'
+              'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.index),
+                 '--query-gpu=' + self.FIELDS, '--format=csv,noheader,nounits',
+                 '-lms', '200'], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=5)
+        sm, mx, reasons = [], None, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown',
+                 'sw_power_cap']
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(',')]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[3:7]):
+                if val.lower() == 'active':
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {'sm_mhz': float(np.median(sm)), 'sm_max_mhz': mx,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+# ------------------------------------------------------------ CPU baseline
+_W = {}
+
+
+def _cpu_init(path, a, b):
+    import scipy.sparse as sp
+    d = np.load(path)
+    _W['ham'] = sp.csr_matrix((d['data'], d['indices'], d['indptr']),
+                              shape=tuple(d['shape']))
+    _W['a'], _W['b'] = a, b
+
+
+def _cpu_task(args):
+    from oracle import kpm_oracle as ko
+    vec, M = args
+    t0 = time.perf_counter()
+    ko.moments_dos(_W['ham'], _W['a'], _W['b'], vec, M)
+    return time.perf_counter() - t0
+
+
+class CpuBaseline:
+    """The oracle port of the reference (one vector at a time, scipy CSR
+    matvec + vdot), one spawned process per core over disjoint vectors."""
+
+    def __init__(self, ham, a, b, vecs, procs):
+        self.tmp = tempfile.NamedTemporaryFile(suffix='.npz', delete=False)
+        self.tmp.close()
+        np.savez(self.tmp.name, data=ham.data, indices=ham.indices,
+                 indptr=ham.indptr, shape=np.array(ham.shape))
+        self.nnz = ham.nnz
+        self.procs = procs
+        self.vecs = vecs
+        ctx = mp.get_context('spawn')
+        self.pool = ctx.Pool(procs, initializer=_cpu_init,
+                             initargs=(self.tmp.name, a, b))
+
+    def run(self, M):
+        t0 = time.perf_counter()
+        jobs = [(self.vecs[r % len(self.vecs)], M) for r in range(self.procs)]
+        self.pool.map(_cpu_task, jobs)
+        dt = time.perf_counter() - t0
+        return self.nnz * self.procs * M / dt, dt
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
+        os.unlink(self.tmp.name)
+
+
+# ---------------------------------------------------------------- main arms
+def dist_setup():
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    return world, rank
+
+
+def run_reference(args):
+    world, rank = dist_setup()
+    if rank != 0:
+        return 0
+    ham, v0, vecs = make_workload(args.cells, min(args.vectors, 64))
+    # Gershgorin bounds on the host: the reference's ARPACK bounds are not
+    # part of the timed moment computation, and this arm runs no GPU code.
+    row_abs = np.asarray(abs(ham).sum(axis=1)).ravel()
+    hi = float(np.max(row_abs))
+    a, b = hi / (1 - 0.05 / 2), 0.0
+    procs = args.cpu_procs or os.cpu_count() or 1
+    base = CpuBaseline(ham, a, b, vecs, procs)
+    try:
+        for _ in range(args.warmup):
+            base.run(args.ref_moments)
+        vals, dts = [], []
+        for _ in range(args.steps):
+            v, dt = base.run(args.ref_moments)
+            vals.append(v)
+            dts.append(dt)
+    finally:
+        base.close()
+    value = float(np.median(vals))
+    sample = ('%d vectors x %d moments of the %s workload per step, one '
+              'spawned process per vector' % (procs, args.ref_moments,
+                                               _workload_name(args)))
+    line = {
+        'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': UNIT,
+        'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': 1e3 * float(np.median(dts)),
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'c128', 'data': 'synthetic',
+        'config': {'workload': _workload_name(args), 'nnz': int(ham.nnz),
+                   'R': procs, 'M': args.ref_moments},
+        'cpu_baseline': {'value': value, 'unit': UNIT, 'cores': procs,
+                         'kind': 'port', 'sample': sample},
+        'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0,
+                'd2h_bytes_per_step': 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def _workload_name(args):
+    return ('honeycomb %dx%d cells (%d orbitals), Peierls flux 1/1000, '
+            'W=0.5, DOS R=%d M=%d' % (args.cells, args.cells,
+                                      2 * args.cells ** 2, args.vectors,
+                                      args.moments))
+
+
+def run_ours(args):
+    import torch
+    from kwant_gb300 import _lib, kpm
+
+    world, rank = dist_setup()
+    if world > 1:
+        import torch.distributed as dist
+        local = int(os.environ.get('LOCAL_RANK', '0'))
+        torch.cuda.set_device(local)
+        dist.init_process_group('nccl')
+    dev = torch.cuda.current_device()
+
+    t_setup = time.perf_counter()
+    ham, v0, vecs = make_workload(args.cells, args.vectors,
+                                  seed_vec=1 + rank)
+    n, nnz = ham.shape[0], ham.nnz
+    R, M = args.vectors, args.moments
+    lo, hi = kpm.spectral_bounds(ham, 0.05, v0, 'lanczos')
+    a, b = kpm._rescale_ab(lo, hi, 0.05)
+    prec = _lib.PREC_MIXED if args.precision == 'mixed' else _lib.PREC_FP64
+    csr = _lib.Csr(ham)
+    handle = _lib.Handle(csr, a, b, prec)
+    block = _lib.Block(handle, vecs, keep_a0=True)
+    stream = torch.cuda.ExternalStream(handle.stream())
+    setup_s = time.perf_counter() - t_setup
+
+    def one_step():
+        block.rewind()
+        return block.dos_moments(0, M)
+
+    for _ in range(args.warmup):
+        one_step()
+
+    # ---- timed region (device resident) ---------------------------------
+    clocks = ClockSampler(dev)
+    clocks.start()
+    handle.profile(True)
+    launches0 = _lib.launch_count()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    mom = None
+    for _ in range(args.steps):
+        mom = one_step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    launches = _lib.launch_count() - launches0
+    n_step, step_ms = handle.profile_read()
+    handle.profile(False)
+    clk = clocks.stop()
+    t_ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([t_ms], device='cuda')
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_ms = float(t.item())
+    ms_per_step = t_ms / args.steps
+    value = world * nnz * R * M / (ms_per_step / 1e3)
+
+    # ---- roofline of the dominant kernel (the fused step) ----------------
+    import json as _json
+    peaks = {}
+    pk = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    if os.path.exists(pk):
+        peaks = _json.load(open(pk))
+    hbm_peak = float(peaks.get('hbm_gbs', 6800.0))
+    peak_src = 'measured' if 'hbm_gbs' in peaks else 'fallback'
+    B = step_bytes(nnz, n, R, args.precision)
+    avg_step_ms = step_ms / max(n_step, 1)
+    achieved = B / (avg_step_ms / 1e3) / 1e9
+    traffic = None
+    tr_path = os.path.join(ROOT, 'profiles', 'step_traffic.json')
+    if os.path.exists(tr_path):
+        tr = _json.load(open(tr_path))
+        traffic = tr.get('%s_R%d' % (args.precision, R))
+
+    # ---- accuracy vs the FP64 path (untimed) -------------------------------
+    accuracy = None
+    if args.accuracy and rank == 0:
+        nodes = kpm._chebyshev_nodes(2 * M)
+        mom64 = None
+        if prec == _lib.PREC_MIXED:
+            h64 = _lib.Handle(csr, a, b, _lib.PREC_FP64)
+            b64 = _lib.Block(h64, vecs, keep_a0=False)
+            mom64 = b64.dos_moments(0, M)
+            b64.close()
+            h64.close()
+            def dens(mm):
+                return _lib.reconstruct(mm[:, :, None], True, False, a,
+                                        _lib.KERNEL_JACKSON, 4.0, nodes)[1][:, 0]
+            d32, d64 = dens(mom), dens(mom64)
+            accuracy = {
+                'dos_linf_per_orbital_vs_fp64': float(
+                    np.max(np.abs(d32 - d64)) / n),
+                'dos_linf_rel_vs_fp64': float(
+                    np.max(np.abs(d32 - d64)) / np.max(np.abs(d64))),
+                'reference': 'FP64 GPU path (parity-tested against the '
+                             'reference fixtures at 1e-12)'}
+
+    # ---- e2e through the C ABI one-shot call (host buffers) ----------------
+    e2e = None
+    if args.e2e and rank == 0:
+        pin_vec = torch.empty((R, n, 2), dtype=torch.float64,
+                              pin_memory=True)
+        pin_vec.numpy()[:] = vecs.view(np.float64).reshape(R, n, 2)
+        pv = pin_vec.numpy().view(np.complex128).reshape(R, n)
+        pins = {}
+        for k, arr in (('indptr', csr.indptr), ('indices', csr.indices),
+                       ('data', csr.data.view(np.float64))):
+            t = torch.empty(arr.shape, dtype={
+                np.dtype(np.int32): torch.int32,
+                np.dtype(np.float64): torch.float64}[arr.dtype],
+                pin_memory=True)
+            t.numpy()[:] = arr
+            pins[k] = t
+        pcsr = _lib.Csr.__new__(_lib.Csr)
+        pcsr.shape = csr.shape
+        pcsr.indptr = pins['indptr'].numpy()
+        pcsr.indices = pins['indices'].numpy()
+        pcsr.data = pins['data'].numpy().view(np.complex128)
+        pcsr.nnz = csr.nnz
+        pcsr.desc = _lib.CsrDesc(n, csr.nnz, _lib.ptr(pcsr.indptr),
+                                 _lib.ptr(pcsr.indices), _lib.ptr(pcsr.data))
+        out_m = torch.empty((R, M, 2), dtype=torch.float64, pin_memory=True)
+        out_g = torch.empty((2 * M, 2), dtype=torch.float64, pin_memory=True)
+        out_d = torch.empty((2 * M, 2), dtype=torch.float64, pin_memory=True)
+        import ctypes as C
+
+        def e2e_step():
+            _lib.check(_lib.lib.kpm_dos(
+                C.byref(pcsr.desc), float(a), float(b), prec, _lib.ptr(pv),
+                R, M, _lib.KERNEL_JACKSON, C.c_void_p(out_m.data_ptr()),
+                C.c_void_p(out_g.data_ptr()), C.c_void_p(out_d.data_ptr())))
+
+        for _ in range(max(1, min(args.warmup, 2))):
+            e2e_step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+        h2d = csr.indptr.nbytes + csr.indices.nbytes + csr.data.nbytes + \
+            vecs.nbytes
+        d2h = out_m.numel() * 8 + out_g.numel() * 8 + out_d.numel() * 8
+        e2e = {'value': nnz * R * M / (e_ms / 1e3), 'unit': UNIT,
+               'h2d_bytes_per_step': int(h2d), 'd2h_bytes_per_step': int(d2h),
+               'ms_per_step': e_ms, 'api': 'kpm_dos (C ABI, pinned host '
+               'buffers, handle create + uploads + recursion + device '
+               'reconstruction + downloads per step)'}
+
+    # ---- CPU baseline (oracle port on the host cores) ----------------------
+    cpu = None
+    if args.cpu and rank == 0 and world == 1:
+        procs = args.cpu_procs or os.cpu_count() or 1
+        base = CpuBaseline(ham, a, b, vecs, procs)
+        try:
+            base.run(8)  # spawn + load
+            v, dt = base.run(args.ref_moments)
+        finally:
+            base.close()
+        cpu = {'value': v, 'unit': UNIT, 'cores': procs, 'kind': 'port',
+               'sample': '%d vectors x %d moments of the same workload, one '
+                         'spawned process per vector (%.1f s)'
+                         % (procs, args.ref_moments, dt)}
+
+    if rank == 0:
+        line = {
+            'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world,
+            'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': ms_per_step, 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None,
+            'dtype': 'c64+f64acc' if args.precision == 'mixed' else 'c128',
+            'data': 'synthetic',
+            'config': {'workload': _workload_name(args),
+                       'precision': args.precision, 'nnz': int(nnz),
+                       'orbitals': int(n), 'R': R, 'M': M,
+                       'matvec_steps_per_step': M // 2,
+                       'l2': 'inputs larger than L2 (vector blocks %.2f GB '
+                             'each), no flush' % (n * R * (8 if args.precision
+                                                          == 'mixed' else 16)
+                                                  / 1e9),
+                       'setup_s': setup_s, 'parallelism':
+                       'replicas' if world > 1 else 'single'},
+            'roofline': {'bound': 'hbm', 'achieved': achieved,
+                         'peak': hbm_peak, 'unit': 'GB/s',
+                         'frac': achieved / hbm_peak, 'traffic': traffic,
+                         'kernel': 'cheb_step_kernel (fused step + moment '
+                                   'dots)',
+                         'algorithmic_bytes_per_launch': B,
+                         'avg_launch_ms': avg_step_ms,
+                         'launches_timed': n_step,
+                         'peak_source': peak_src},
+            'cpu_baseline': cpu, 'e2e': e2e, 'gpu_launches': launches,
+            'clocks': clk, 'accuracy': accuracy,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    block.close()
+    handle.close()
+    return 0
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument('--gpus', type=int, default=1)
+    p.add_argument('--steps', type=int, default=5)
+    p.add_argument('--warmup', type=int, default=3)
+    p.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    p.add_argument('--precision', default='mixed', choices=['mixed', 'fp64'])
+    p.add_argument('--cells', type=int, default=1000)
+    p.add_argument('--vectors', type=int, default=64)
+    p.add_argument('--moments', type=int, default=2000)
+    p.add_argument('--ref-moments', type=int, default=100)
+    p.add_argument('--cpu-procs', type=int, default=0)
+    p.add_argument('--no-e2e', dest='e2e', action='store_false')
+    p.add_argument('--no-cpu', dest='cpu', action='store_false')
+    p.add_argument('--no-accuracy', dest='accuracy', action='store_false')
+    args = p.parse_args()
+    if args.warmup < 3 and args.impl == 'ours':
+        print('warning: fewer than 3 warm-up steps', file=sys.stderr)
+    if args.impl == 'reference':
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == '__main__':
+    sys.exit(main())

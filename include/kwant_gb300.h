@@ -1,0 +1,233 @@
+/*
+ * kwant_gb300 — C ABI of the GB300 (sm_103a) kernel-polynomial-method path.
+ *
+ * This is the drop-in boundary for the KPM hot path of Kwant
+ * (kwant/kpm.py: SpectralDensity, Correlator, conductivity; with
+ * kwant/operator.pyx Density/Current as local operators).  The Python
+ * package kwant_gb300 binds it through ctypes; any other host language
+ * binds the same symbols.
+ *
+ * Conventions
+ *  - Every function returns an int status: KPM_OK (0) or a negative error
+ *    code; kpm_last_error() returns the message of the last failure on the
+ *    calling thread.
+ *  - Complex numbers are interleaved (re, im) doubles, like numpy
+ *    complex128.  Indices are int32 (Kwant's gint, kwant/graph/defs.h:15).
+ *  - Host pointers are owned by the caller and only read/written during the
+ *    call.  Device memory is owned by the handle / block / operator objects.
+ *  - Calls are synchronous with respect to the host (results are in the
+ *    output buffers on return).  Each handle issues its work on one CUDA
+ *    stream.  A handle and the objects created from it must be used from one
+ *    host thread at a time.
+ *  - There is no CPU fallback: without a usable CUDA device every call that
+ *    would compute returns KPM_ECUDA.
+ */
+#ifndef KWANT_GB300_H
+#define KWANT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define KPM_API __attribute__((visibility("default")))
+#else
+#define KPM_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define KPM_OK 0
+#define KPM_EINVAL (-1)      /* invalid argument (reference: ValueError)   */
+#define KPM_ECUDA (-2)       /* CUDA runtime / device error                */
+#define KPM_ENOMEM (-3)      /* device allocation failed                   */
+#define KPM_EDIVERGED (-4)   /* moments left [-mu0, mu0]: bounds too tight */
+#define KPM_ETIMEOUT (-5)    /* a bounded device wait gave up              */
+#define KPM_ESTATE (-6)      /* call out of order (e.g. resume mismatch)   */
+#define KPM_EUNSUPPORTED (-7)
+
+/* ---- enums ------------------------------------------------------------- */
+/* Recursion precision.  FP64: complex128 vectors and matrix, reference
+ * operation order.  MIXED: complex64 vectors and matrix (pre-scaled by
+ * 2/a), FP64 accumulation of every dot product. */
+#define KPM_PREC_FP64 0
+#define KPM_PREC_MIXED 1
+
+#define KPM_KERNEL_NONE 0
+#define KPM_KERNEL_JACKSON 1   /* kwant/kpm.py:1106-1123 */
+#define KPM_KERNEL_LORENTZ 2   /* kwant/kpm.py:1126-1142 */
+
+typedef struct kpm_handle kpm_handle; /* a rescaled Hamiltonian on device  */
+typedef struct kpm_block kpm_block;   /* R vectors + recursion state       */
+typedef struct kpm_op kpm_op;         /* a lowered sesquilinear operator   */
+
+/* CSR matrix on the host: rows x rows, complex128 values (interleaved). */
+typedef struct kpm_csr_desc {
+  int64_t rows;
+  int64_t nnz;
+  const int32_t* indptr;   /* rows + 1 */
+  const int32_t* indices;  /* nnz      */
+  const double* data;      /* 2 * nnz  */
+} kpm_csr_desc;
+
+/* A sesquilinear operator q_w(bra, ket) lowered to "terms" (see
+ * kwant_gb300/operator.py for the lowering of Density, Current and
+ * matrix operators):
+ *   coef_t  = sum_{e in bra_ptr[t]..bra_ptr[t+1]} conj(bra_val[e]) * bra[bra_col[e]]
+ *   q_w     = sum_{t : term_out[t] == w} conj(coef_t) * ket[term_row[t]]
+ * Terms are sorted by output; chunk_ptr splits them into chunks of
+ * consecutive terms of one output (chunk_out[c]); outputs with several
+ * chunks are summed in chunk order.  real0 = 1 takes the real part of the
+ * n = 0 moment (reference kwant/operator.pyx:556-558, bra is ket). */
+typedef struct kpm_op_desc {
+  int64_t num_terms;
+  int64_t num_outputs;
+  int64_t num_chunks;
+  const int32_t* term_row;   /* num_terms     */
+  const int64_t* bra_ptr;    /* num_terms + 1 */
+  const int32_t* bra_col;    /* bra_ptr[num_terms] */
+  const double* bra_val;     /* 2 * bra_ptr[num_terms] */
+  const int64_t* chunk_ptr;  /* num_chunks + 1 (term offsets) */
+  const int32_t* chunk_out;  /* num_chunks */
+  int32_t real0;
+} kpm_op_desc;
+
+/* ---- library ------------------------------------------------------------ */
+KPM_API int kpm_version(void);
+/* Copies the last error message of this thread (NUL-terminated). */
+KPM_API int kpm_last_error(char* buf, size_t len);
+/* Number of CUDA devices visible (0 when none). */
+KPM_API int kpm_device_count(int* count);
+
+/* ---- Hamiltonian handle ---------------------------------------------------
+ * Replaces the rescaled LinearOperator of _rescale (kwant/kpm.py:1145-1187):
+ * the device applies (H v - b v) / a.  a, b as computed by the caller from
+ * the spectral bounds (kwant/kpm.py:1174-1175). */
+KPM_API int kpm_create(const kpm_csr_desc* ham, double a, double b, int precision,
+                       kpm_handle** out);
+/* Use an external CUDA stream (cudaStream_t) for all work of the handle. */
+KPM_API int kpm_set_stream(kpm_handle* h, void* stream);
+KPM_API int kpm_get_stream(kpm_handle* h, void** stream);
+KPM_API int kpm_synchronize(kpm_handle* h);
+KPM_API int kpm_destroy(kpm_handle* h);
+
+/* ---- vector blocks ---------------------------------------------------------
+ * R starting vectors |r> (host, R x N complex128, one vector after another:
+ * the stacked output of the reference's vector factory, kwant/kpm.py:437).
+ * keep_a0 keeps |r> resident (needed for operators and for rewinding). */
+KPM_API int kpm_block_create(kpm_handle* h, const double* vecs, int64_t R,
+                             int keep_a0, kpm_block** out);
+/* Restart the recursion from |r> (requires keep_a0). */
+KPM_API int kpm_block_rewind(kpm_block* blk);
+KPM_API int kpm_block_destroy(kpm_block* blk);
+/* Copy the current recursion state (alpha_{n-1}, alpha_n) to the host, each
+ * R x N complex128 (the reference's _last_two_alphas, kwant/kpm.py:486-488). */
+KPM_API int kpm_block_state(kpm_block* blk, double* alpha_prev, double* alpha_cur);
+
+/* ---- moments -----------------------------------------------------------------
+ * DOS moments (operator=None) of SpectralDensity._update_moments_list,
+ * kwant/kpm.py:436-477: mu_0 = <a0|a0>, mu_1 = <a0|a1>,
+ * mu_2n = 2<a_n|a_n> - mu_0, mu_2n+1 = 2<a_n+1|a_n> - mu_1 (odd tail:
+ * 2<a_last|a_last> - mu_0).  Computes moments [m_start, m_end) of every
+ * vector; m_start is 0 on the first call and the previous m_end when
+ * resuming (add_moments, kwant/kpm.py:318-358).  out: R x (m_end - m_start)
+ * complex128. */
+KPM_API int kpm_block_dos_moments(kpm_block* blk, int64_t m_start, int64_t m_end,
+                                  double* out);
+
+/* Operator moments mu_n = op(a0, T_n(H~) a0), kwant/kpm.py:439-448 and
+ * :478-484 (operator a lowered kwant.operator Density / Current / matrix).
+ * out: R x (m_end - m_start) x num_outputs complex128. */
+KPM_API int kpm_op_create(kpm_handle* h, const kpm_op_desc* desc, kpm_op** out);
+KPM_API int kpm_op_destroy(kpm_op* op);
+KPM_API int kpm_block_op_moments(kpm_block* blk, kpm_op* op, int64_t m_start,
+                                 int64_t m_end, double* out);
+/* op(bra, ket) for single host vectors (reference _LocalOperator.__call__,
+ * kwant/operator.pyx:470-559, MAT_ELS): out num_outputs complex128. */
+KPM_API int kpm_op_apply(kpm_op* op, const double* bra, const double* ket,
+                         double* out);
+
+/* One-shot DOS (the C-ABI form of SpectralDensity with operator=None and
+ * explicit bounds): uploads ham and vecs, runs the recursion, reduces the
+ * moments (mean over vectors, /a, kernel) and reconstructs the density at
+ * the 2M Chebyshev nodes on the device.  moments_out: R x M complex128 (may
+ * be NULL); gammas_out / densities_out: 2M complex128 (may be NULL). */
+KPM_API int kpm_dos(const kpm_csr_desc* ham, double a, double b, int precision,
+                    const double* vecs, int64_t R, int64_t M, int kernel,
+                    double* moments_out, double* gammas_out, double* densities_out);
+
+/* ---- reconstruction (device) -------------------------------------------------
+ * _moments + _calc_fft_moments, kwant/kpm.py:378-388 and :1197-1222:
+ * moments (R x M x W complex128, host) -> mean over R (if mean) -> / a ->
+ * kernel -> zero-pad to 2M -> DCT-III -> reversed ("gammas", 2M x W') ->
+ * divided by pi sqrt(1 - x_k^2) at the nodes x_k ("densities").
+ * W' = W if mean else R x W.  nodes: the 2M ascending Chebyshev nodes.
+ * is_real: the moments passed numpy's real_if_close (kwant/kpm.py:379);
+ * imaginary parts are ignored and divisions are true divisions (numpy's
+ * real arithmetic) instead of reciprocal multiplications (its complex
+ * arithmetic).  Outputs are complex128; gammas_out or densities_out may be
+ * NULL. */
+KPM_API int kpm_reconstruct(int64_t R, int64_t M, int64_t W, const double* moments,
+                            int mean, int is_real, double a, int kernel,
+                            double lorentz_l, const double* nodes, double* gammas_out,
+                            double* densities_out);
+/* Kernel weights g_m (M doubles) as applied by kpm_reconstruct. */
+KPM_API int kpm_kernel_weights(int64_t M, int kernel, double lorentz_l, double* g);
+
+/* ---- spectral bounds -------------------------------------------------------
+ * Extremal eigenvalues of the Hermitian ham by FP64 Lanczos on the device,
+ * started from v0 (N complex128, the reference's _v0, kwant/kpm.py:203),
+ * until the Ritz residual of both extremes is below tol * max|theta|
+ * (replaces the two ARPACK eigsh calls of kwant/kpm.py:1169-1172).
+ * Returns the Ritz values widened by their residual norms. */
+KPM_API int kpm_bounds(const kpm_csr_desc* ham, const double* v0, double tol,
+                       int max_iter, double* lmin, double* lmax, int* iterations);
+
+/* Single-vector FP64 matvec y = ham x on the device (x, y host, N complex128);
+ * the matvec that an ARPACK driver on the host calls (bounds_method
+ * "arpack" of the Python layer). */
+KPM_API int kpm_handle_matvec(kpm_handle* h, const double* x, double* y);
+
+/* ---- correlator / Kubo-Bastin ----------------------------------------------
+ * Correlator moments matrix (kwant/kpm.py:557-606, :685-695):
+ *   Psi_n = v_beta T_n(H~)|r>,  Omega_m = T_m(H~') v_alpha|r>,
+ *   mu_mn = (1/R) sum_r <Omega_m | Psi_n>        (M x M complex128).
+ * H~ uses the handle's (a, b); H~' uses (a2, b2) (the re-derived bounds of
+ * kwant/kpm.py:576-579).  v_alpha, v_beta are CSR (e.g. the velocity of
+ * _velocity, kwant/kpm.py:1042-1085).  gemm selects the contraction:
+ *   0 = FP64 CUDA-core GEMM, 1 = tensor-core split-BF16 (hi+lo) GEMM with
+ *   FP32 accumulation (tcgen05), 2 = automatic (1 for MIXED, 0 for FP64).
+ * mu_out is the mean over vectors (or R x M x M when per_vector). */
+KPM_API int kpm_correlator_moments(kpm_handle* h, double a2, double b2,
+                                   const kpm_csr_desc* v_alpha,
+                                   const kpm_csr_desc* v_beta, const double* vecs,
+                                   int64_t R, int64_t M, int gemm, int per_vector,
+                                   double* mu_out);
+
+/* Integral factor of Correlator._build_integral_factor (kwant/kpm.py:
+ * 720-760) on the device: mu (M x M complex128), kernel weights g (M, with
+ * g[0] already halved), nodes x_k (2M) -> factor (2M complex128). */
+KPM_API int kpm_integral_factor(int64_t M, const double* mu, const double* g,
+                                const double* nodes, double* factor_out);
+
+/* ---- diagnostics -------------------------------------------------------------- */
+/* Device time (ms) of the last recursion call on the handle, measured with
+ * CUDA events on the handle's stream around the kernels only. */
+KPM_API int kpm_last_kernel_ms(kpm_handle* h, double* ms);
+/* Per-launch profiling of the Chebyshev step kernels of a handle: while
+ * enabled, every step-kernel launch is bracketed by CUDA events on the
+ * handle's stream.  kpm_profile_read returns (and resets) the number of
+ * timed launches and their summed device time in ms. */
+KPM_API int kpm_profile(kpm_handle* h, int enable);
+KPM_API int kpm_profile_read(kpm_handle* h, int64_t* launches,
+                             double* total_ms);
+/* Number of kernel launches issued by this library since load. */
+KPM_API int kpm_launch_count(int64_t* count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KWANT_GB300_H */

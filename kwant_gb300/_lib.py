@@ -1,0 +1,375 @@
+"""ctypes binding of ``libkwant_gb300.so`` (the C ABI in include/kwant_gb300.h).
+
+There is no CPU fallback: importing this module without the built library
+raises ``ImportError``, and every compute call without a CUDA device raises
+``KPMCudaError``.
+"""
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, 'libkwant_gb300.so')
+
+KPM_OK = 0
+KPM_EINVAL = -1
+KPM_ECUDA = -2
+KPM_ENOMEM = -3
+KPM_EDIVERGED = -4
+KPM_ETIMEOUT = -5
+KPM_ESTATE = -6
+KPM_EUNSUPPORTED = -7
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+KERNEL_NONE = 0
+KERNEL_JACKSON = 1
+KERNEL_LORENTZ = 2
+
+
+class KPMError(RuntimeError):
+    pass
+
+
+class KPMCudaError(KPMError):
+    pass
+
+
+class KPMStateError(KPMError):
+    pass
+
+
+class KPMUnsupported(KPMError, NotImplementedError):
+    pass
+
+
+class KPMDiverged(KPMError):
+    pass
+
+
+class CsrDesc(C.Structure):
+    _fields_ = [('rows', C.c_int64), ('nnz', C.c_int64),
+                ('indptr', C.c_void_p), ('indices', C.c_void_p),
+                ('data', C.c_void_p)]
+
+
+class OpDesc(C.Structure):
+    _fields_ = [('num_terms', C.c_int64), ('num_outputs', C.c_int64),
+                ('num_chunks', C.c_int64), ('term_row', C.c_void_p),
+                ('bra_ptr', C.c_void_p), ('bra_col', C.c_void_p),
+                ('bra_val', C.c_void_p), ('chunk_ptr', C.c_void_p),
+                ('chunk_out', C.c_void_p), ('real0', C.c_int32)]
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(
+            'kwant_gb300 CUDA library not built (%s missing); run '
+            '"python -m kwant_gb300.build" (needs nvcc, sm_103a)' % LIB_PATH)
+    lib = C.CDLL(LIB_PATH)
+    P = C.c_void_p
+    I64 = C.c_int64
+    D = C.c_double
+    I = C.c_int
+    sigs = {
+        'kpm_version': [],
+        'kpm_last_error': [C.c_char_p, C.c_size_t],
+        'kpm_device_count': [P],
+        'kpm_create': [P, D, D, I, P],
+        'kpm_set_stream': [P, P],
+        'kpm_get_stream': [P, P],
+        'kpm_synchronize': [P],
+        'kpm_destroy': [P],
+        'kpm_block_create': [P, P, I64, I, P],
+        'kpm_block_rewind': [P],
+        'kpm_block_destroy': [P],
+        'kpm_block_state': [P, P, P],
+        'kpm_block_dos_moments': [P, I64, I64, P],
+        'kpm_op_create': [P, P, P],
+        'kpm_op_destroy': [P],
+        'kpm_block_op_moments': [P, P, I64, I64, P],
+        'kpm_op_apply': [P, P, P, P],
+        'kpm_dos': [P, D, D, I, P, I64, I64, I, P, P, P],
+        'kpm_reconstruct': [I64, I64, I64, P, I, I, D, I, D, P, P, P],
+        'kpm_kernel_weights': [I64, I, D, P],
+        'kpm_bounds': [P, P, D, I, P, P, P],
+        'kpm_handle_matvec': [P, P, P],
+        'kpm_correlator_moments': [P, D, D, P, P, P, I64, I64, I, I, P],
+        'kpm_integral_factor': [I64, P, P, P, P],
+        'kpm_last_kernel_ms': [P, P],
+        'kpm_profile': [P, I],
+        'kpm_profile_read': [P, P, P],
+        'kpm_launch_count': [P],
+    }
+    for name, args in sigs.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = C.c_int
+    return lib
+
+
+lib = _load()
+
+
+def last_error():
+    buf = C.create_string_buffer(1024)
+    lib.kpm_last_error(buf, len(buf))
+    return buf.value.decode(errors='replace')
+
+
+def check(status):
+    if status == KPM_OK:
+        return
+    msg = last_error()
+    if status == KPM_EINVAL:
+        raise ValueError(msg)
+    if status == KPM_ECUDA or status == KPM_ENOMEM:
+        raise KPMCudaError(msg)
+    if status == KPM_ESTATE:
+        raise KPMStateError(msg)
+    if status == KPM_EUNSUPPORTED:
+        raise KPMUnsupported(msg)
+    if status == KPM_EDIVERGED:
+        raise KPMDiverged(msg)
+    raise KPMError('status %d: %s' % (status, msg))
+
+
+def ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def device_count():
+    n = C.c_int(0)
+    check(lib.kpm_device_count(C.byref(n)))
+    return n.value
+
+
+def launch_count():
+    n = C.c_int64(0)
+    check(lib.kpm_launch_count(C.byref(n)))
+    return n.value
+
+
+class Csr:
+    """Host CSR arrays kept alive together with their C descriptor."""
+
+    def __init__(self, mat):
+        import scipy.sparse as sp
+        m = sp.csr_matrix(mat)
+        if m.shape[0] != m.shape[1]:
+            raise ValueError('matrix must be square')
+        self.shape = m.shape
+        self.indptr = np.ascontiguousarray(m.indptr, dtype=np.int32)
+        self.indices = np.ascontiguousarray(m.indices, dtype=np.int32)
+        self.data = np.ascontiguousarray(m.data, dtype=np.complex128)
+        self.nnz = int(self.data.shape[0])
+        self.desc = CsrDesc(m.shape[0], self.nnz, ptr(self.indptr),
+                            ptr(self.indices), ptr(self.data))
+
+    def ref(self):
+        return C.byref(self.desc)
+
+
+def c128(a):
+    return np.ascontiguousarray(a, dtype=np.complex128)
+
+
+class Handle:
+    """A Hamiltonian resident on the device with its rescaling (a, b)."""
+
+    def __init__(self, csr, a, b, precision):
+        if not isinstance(csr, Csr):
+            csr = Csr(csr)
+        self.csr = csr
+        self.a, self.b, self.precision = float(a), float(b), precision
+        self.N = csr.shape[0]
+        h = C.c_void_p()
+        check(lib.kpm_create(csr.ref(), self.a, self.b, precision,
+                             C.byref(h)))
+        self._h = h
+
+    @property
+    def ptr(self):
+        return self._h
+
+    def stream(self):
+        s = C.c_void_p()
+        check(lib.kpm_get_stream(self._h, C.byref(s)))
+        return s.value
+
+    def last_kernel_ms(self):
+        ms = C.c_double()
+        check(lib.kpm_last_kernel_ms(self._h, C.byref(ms)))
+        return ms.value
+
+    def profile(self, enable=True):
+        check(lib.kpm_profile(self._h, 1 if enable else 0))
+
+    def profile_read(self):
+        n, ms = C.c_int64(), C.c_double()
+        check(lib.kpm_profile_read(self._h, C.byref(n), C.byref(ms)))
+        return n.value, ms.value
+
+    def matvec(self, x):
+        x = c128(x)
+        y = np.empty_like(x)
+        check(lib.kpm_handle_matvec(self._h, ptr(x), ptr(y)))
+        return y
+
+    def close(self):
+        if getattr(self, '_h', None):
+            lib.kpm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Block:
+    """R vectors and their recursion state on the device."""
+
+    def __init__(self, handle, vecs, keep_a0=True):
+        vecs = c128(np.atleast_2d(vecs))
+        self.handle = handle
+        self.R = vecs.shape[0]
+        if vecs.shape[1] != handle.N:
+            raise ValueError('vector length does not match the Hamiltonian')
+        b = C.c_void_p()
+        check(lib.kpm_block_create(handle.ptr, ptr(vecs), self.R,
+                                   1 if keep_a0 else 0, C.byref(b)))
+        self._b = b
+
+    def dos_moments(self, m_start, m_end):
+        out = np.empty((self.R, m_end - m_start), dtype=np.complex128)
+        check(lib.kpm_block_dos_moments(self._b, m_start, m_end, ptr(out)))
+        return out
+
+    def op_moments(self, op, m_start, m_end):
+        out = np.empty((self.R, m_end - m_start, op.W), dtype=np.complex128)
+        check(lib.kpm_block_op_moments(self._b, op.ptr, m_start, m_end,
+                                       ptr(out)))
+        return out
+
+    def rewind(self):
+        check(lib.kpm_block_rewind(self._b))
+
+    def state(self):
+        prev = np.empty((self.R, self.handle.N), dtype=np.complex128)
+        cur = np.empty_like(prev)
+        check(lib.kpm_block_state(self._b, ptr(prev), ptr(cur)))
+        return prev, cur
+
+    def close(self):
+        if getattr(self, '_b', None):
+            lib.kpm_block_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        self.close()
+
+
+class Op:
+    """A lowered sesquilinear operator on the device."""
+
+    def __init__(self, handle, lowered):
+        self.handle = handle
+        self.low = lowered
+        self.W = int(lowered.num_outputs)
+        d = OpDesc(lowered.num_terms, lowered.num_outputs,
+                   lowered.num_chunks, ptr(lowered.term_row),
+                   ptr(lowered.bra_ptr), ptr(lowered.bra_col),
+                   ptr(lowered.bra_val), ptr(lowered.chunk_ptr),
+                   ptr(lowered.chunk_out), int(lowered.real0))
+        o = C.c_void_p()
+        check(lib.kpm_op_create(handle.ptr, C.byref(d), C.byref(o)))
+        self._o = o
+
+    @property
+    def ptr(self):
+        return self._o
+
+    def apply(self, bra, ket):
+        bra, ket = c128(bra), c128(ket)
+        out = np.empty(self.W, dtype=np.complex128)
+        check(lib.kpm_op_apply(self._o, ptr(bra), ptr(ket), ptr(out)))
+        return out
+
+    def close(self):
+        if getattr(self, '_o', None):
+            lib.kpm_op_destroy(self._o)
+            self._o = None
+
+    def __del__(self):
+        self.close()
+
+
+def reconstruct(moments, mean, is_real, a, kernel, lorentz_l, nodes):
+    """moments: (R, M, W) complex128 -> (gammas, densities), each
+    (2M, W') complex128."""
+    moments = c128(moments)
+    R, M, W = moments.shape
+    Wo = W if mean else R * W
+    gam = np.empty((2 * M, Wo), dtype=np.complex128)
+    rho = np.empty_like(gam)
+    nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+    check(lib.kpm_reconstruct(R, M, W, ptr(moments), 1 if mean else 0,
+                              1 if is_real else 0, float(a), kernel,
+                              float(lorentz_l), ptr(nodes), ptr(gam),
+                              ptr(rho)))
+    return gam, rho
+
+
+def kernel_weights(M, kernel, lorentz_l=4.0):
+    g = np.empty(M, dtype=np.float64)
+    check(lib.kpm_kernel_weights(M, kernel, float(lorentz_l), ptr(g)))
+    return g
+
+
+def bounds(csr, v0, tol, max_iter=1000):
+    if not isinstance(csr, Csr):
+        csr = Csr(csr)
+    v0 = c128(v0)
+    lo, hi, it = C.c_double(), C.c_double(), C.c_int()
+    check(lib.kpm_bounds(csr.ref(), ptr(v0), float(tol), int(max_iter),
+                         C.byref(lo), C.byref(hi), C.byref(it)))
+    return lo.value, hi.value, it.value
+
+
+def correlator_moments(handle, a2, b2, v_alpha, v_beta, vecs, M, gemm=2,
+                       per_vector=False):
+    va = v_alpha if isinstance(v_alpha, Csr) else Csr(v_alpha)
+    vb = v_beta if isinstance(v_beta, Csr) else Csr(v_beta)
+    vecs = c128(np.atleast_2d(vecs))
+    R = vecs.shape[0]
+    shape = (R, M, M) if per_vector else (M, M)
+    out = np.empty(shape, dtype=np.complex128)
+    check(lib.kpm_correlator_moments(handle.ptr, float(a2), float(b2),
+                                     va.ref(), vb.ref(), ptr(vecs), R, M,
+                                     int(gemm), 1 if per_vector else 0,
+                                     ptr(out)))
+    return out
+
+
+def integral_factor(mu, g, nodes):
+    mu = c128(mu)
+    M = mu.shape[0]
+    g = np.ascontiguousarray(g, dtype=np.float64)
+    nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+    out = np.empty(2 * M, dtype=np.complex128)
+    check(lib.kpm_integral_factor(M, ptr(mu), ptr(g), ptr(nodes), ptr(out)))
+    return out
+
+
+def dos(csr, a, b, precision, vecs, M, kernel=KERNEL_JACKSON):
+    if not isinstance(csr, Csr):
+        csr = Csr(csr)
+    vecs = c128(np.atleast_2d(vecs))
+    R = vecs.shape[0]
+    mom = np.empty((R, M), dtype=np.complex128)
+    gam = np.empty(2 * M, dtype=np.complex128)
+    rho = np.empty(2 * M, dtype=np.complex128)
+    check(lib.kpm_dos(csr.ref(), float(a), float(b), precision, ptr(vecs), R,
+                      M, kernel, ptr(mom), ptr(gam), ptr(rho)))
+    return mom, gam, rho

@@ -1,0 +1,124 @@
+// Shared definitions for the KPM CUDA kernels and the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/kwant_gb300.h"
+
+namespace kpm {
+
+// --- error reporting -------------------------------------------------------
+void set_error(const char* fmt, ...);
+const char* last_error();
+
+#define KPM_CUDA(call)                                                      \
+  do {                                                                      \
+    cudaError_t err__ = (call);                                             \
+    if (err__ != cudaSuccess) {                                             \
+      ::kpm::set_error("%s:%d: %s failed: %s", __FILE__, __LINE__, #call,   \
+                       cudaGetErrorString(err__));                          \
+      return KPM_ECUDA;                                                     \
+    }                                                                       \
+  } while (0)
+
+#define KPM_CHECK_LAUNCH() KPM_CUDA(cudaGetLastError())
+
+#define KPM_REQUIRE(cond, ...)                                              \
+  do {                                                                      \
+    if (!(cond)) {                                                          \
+      ::kpm::set_error(__VA_ARGS__);                                        \
+      return KPM_EINVAL;                                                    \
+    }                                                                       \
+  } while (0)
+
+#define KPM_TRY(expr)                                                       \
+  do {                                                                      \
+    int st__ = (expr);                                                      \
+    if (st__ != KPM_OK) return st__;                                        \
+  } while (0)
+
+// --- launch geometry -------------------------------------------------------
+// A "slot" is LANES consecutive threads that together own one matrix row for
+// one group of vectors; each lane holds 16 bytes of vector data
+// (1 complex128 or 2 complex64).
+constexpr int LANES = 16;
+constexpr int STEP_THREADS = 256;
+constexpr int SLOTS = STEP_THREADS / LANES;
+// Vectors per group: 16 (complex128) or 32 (complex64).
+constexpr int GROUP_FP64 = LANES;
+constexpr int GROUP_FP32 = 2 * LANES;
+// Upper bound on the number of row partitions ("x items") of a step: fixed,
+// so the reduction order of every dot product depends only on the number of
+// rows, never on the number of vectors or on the launch shape.
+constexpr int MAX_XITEMS = 2048;
+
+inline int group_size(int precision) {
+  return precision == KPM_PREC_MIXED ? GROUP_FP32 : GROUP_FP64;
+}
+__host__ __device__ inline int64_t round_up(int64_t x, int64_t m) {
+  return (x + m - 1) / m * m;
+}
+__host__ __device__ inline int64_t ceil_div(int64_t x, int64_t m) {
+  return (x + m - 1) / m;
+}
+
+inline int xitems_for_rows(int64_t rows) {
+  int64_t x = ceil_div(rows, (int64_t)SLOTS);
+  if (x > MAX_XITEMS) x = MAX_XITEMS;
+  if (x < 1) x = 1;
+  return (int)x;
+}
+
+// --- handle / block state ---------------------------------------------------
+struct Matrix {
+  int64_t rows = 0, nnz = 0;
+  int32_t* indptr = nullptr;   // rows + 1
+  int32_t* indices = nullptr;  // nnz
+  void* data = nullptr;        // nnz complex (double2 raw H | float2 2H/a)
+};
+
+}  // namespace kpm
+
+struct kpm_handle {
+  int precision = KPM_PREC_FP64;
+  int device = 0;
+  int num_sms = 0;
+  double a = 1.0, b = 0.0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  kpm::Matrix H;
+  // dot-product partials: [groups][xitems][group][3] doubles
+  double* partials = nullptr;
+  size_t partials_cap = 0;
+  int resident_step_blocks = 0;
+  cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+  bool timed = false;
+  // per-launch profiling of step kernels (pairs of events)
+  bool profiling = false;
+  std::vector<cudaEvent_t> prof_events;
+  size_t prof_used = 0;
+};
+
+struct kpm_block {
+  kpm_handle* h = nullptr;
+  int64_t R = 0;        // real vectors
+  int64_t Rpad = 0;     // padded to the group size
+  int groups = 0;
+  int64_t N = 0;
+  bool keep_a0 = false;
+  void* a0 = nullptr;    // [N][Rpad]
+  void* buf[2] = {nullptr, nullptr};
+  void* p_cur = nullptr;   // alpha_n (a0 or one of buf)
+  void* p_prev = nullptr;  // alpha_{n-1}
+  double* mu01 = nullptr;   // [Rpad][2] complex: mu0, mu1 per vector
+  int64_t steps_done = 0;   // number of matvecs applied (n of alpha_n)
+  int mode = -1;            // 0 = DOS, 1 = operator/vectors
+  void* op_coef = nullptr;  // [terms][Rpad] complex128 bra factors
+  const void* op_tag = nullptr;  // operator the factors belong to
+};

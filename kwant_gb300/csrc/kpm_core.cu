@@ -1,0 +1,955 @@
+// Chebyshev recursion of the kernel polynomial method on GB300 (sm_103a).
+//
+// Replaces the per-vector loop of SpectralDensity._update_moments_list
+// (kwant/kpm.py:390-490) and the rescaled matvec of _rescale
+// (kwant/kpm.py:1182-1183) with one fused, batched sparse-matrix x
+// multi-vector pass per Chebyshev step:
+//
+//   alpha_{n+1} = 2 (H alpha_n - b alpha_n) / a - alpha_{n-1}
+//
+// over all R vectors at once.  Vectors are stored interleaved, [row][vector],
+// so a 16-lane slot reads one row of one vector group with 16-byte loads
+// (1 complex128 or 2 complex64 per lane); every neighbour row is a 256-byte
+// coalesced segment.  The per-vector dot products that give the DOS moments
+// (<a_n|a_n>, <a_n+1|a_n>) are accumulated in FP64 in the same pass.
+//
+// Determinism: rows are split into a number of row partitions that depends
+// only on the number of rows; each slot sums its rows in increasing order,
+// slots are summed in order, partitions are summed in order.  A vector's
+// moments therefore do not depend on how many other vectors share the batch
+// or on the launch shape, which keeps add_vectors / add_moments bit-identical
+// to a fresh run (kwant/tests/test_kpm.py:481-535).
+
+#include <cstdarg>
+#include <mutex>
+#include <vector>
+#include <atomic>
+
+#include "kpm_common.cuh"
+#include "kpm_internal.cuh"
+
+namespace kpm {
+
+// ---------------------------------------------------------------- errors
+static thread_local char g_err[1024] = "";
+static std::atomic<int64_t> g_launches{0};
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+const char* last_error() { return g_err; }
+void count_launch(int n) { g_launches += n; }
+
+// ------------------------------------------------------------- allocation
+int dev_alloc(void** p, size_t bytes, cudaStream_t s) {
+  *p = nullptr;
+  if (bytes == 0) return KPM_OK;
+  cudaError_t e = cudaMallocAsync(p, bytes, s);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_error("device allocation of %zu bytes failed: %s", bytes,
+              cudaGetErrorString(e));
+    return KPM_ENOMEM;
+  }
+  return KPM_OK;
+}
+
+void dev_free(void* p, cudaStream_t s) {
+  if (p) cudaFreeAsync(p, s);
+}
+
+int init_device(int* device, int* num_sms) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    set_error("no CUDA device available (%s); kwant_gb300 has no CPU path",
+              e == cudaSuccess ? "0 devices" : cudaGetErrorString(e));
+    return KPM_ECUDA;
+  }
+  KPM_CUDA(cudaGetDevice(device));
+  KPM_CUDA(cudaDeviceGetAttribute(num_sms, cudaDevAttrMultiProcessorCount,
+                                  *device));
+  static std::once_flag once;
+  static int pool_status = KPM_OK;
+  std::call_once(once, [&]() {
+    // Keep freed blocks in the stream-ordered pool so that repeated
+    // create/destroy cycles do not return memory to the driver.
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, *device) == cudaSuccess) {
+      uint64_t thr = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    cudaGetLastError();
+  });
+  return pool_status;
+}
+
+// ---------------------------------------------------------------- matrices
+__global__ void scale_to_c64_kernel(const double2* __restrict__ in,
+                                    float2* __restrict__ out, int64_t n,
+                                    double scale) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n)
+    out[i] = make_float2((float)(in[i].x * scale), (float)(in[i].y * scale));
+}
+
+int upload_matrix(kpm_handle* h, const kpm_csr_desc* m, double scale,
+                  Matrix* out) {
+  KPM_REQUIRE(m->rows > 0 && m->nnz >= 0 && m->indptr && m->indices,
+              "invalid CSR descriptor");
+  // Validate on the host so that no kernel ever indexes out of bounds.
+  KPM_REQUIRE(m->indptr[0] == 0 && m->indptr[m->rows] == m->nnz,
+              "CSR indptr must start at 0 and end at nnz");
+  for (int64_t i = 0; i < m->rows; ++i)
+    KPM_REQUIRE(m->indptr[i] <= m->indptr[i + 1],
+                "CSR indptr not monotone at row %lld", (long long)i);
+  for (int64_t k = 0; k < m->nnz; ++k)
+    KPM_REQUIRE(m->indices[k] >= 0 && m->indices[k] < m->rows,
+                "CSR column index out of range at entry %lld", (long long)k);
+  out->rows = m->rows;
+  out->nnz = m->nnz;
+  KPM_TRY(dev_alloc((void**)&out->indptr, (m->rows + 1) * sizeof(int32_t),
+                    h->stream));
+  KPM_TRY(dev_alloc((void**)&out->indices,
+                    (m->nnz > 0 ? m->nnz : 1) * sizeof(int32_t), h->stream));
+  KPM_CUDA(cudaMemcpyAsync(out->indptr, m->indptr,
+                           (m->rows + 1) * sizeof(int32_t),
+                           cudaMemcpyHostToDevice, h->stream));
+  if (m->nnz > 0)
+    KPM_CUDA(cudaMemcpyAsync(out->indices, m->indices,
+                             m->nnz * sizeof(int32_t), cudaMemcpyHostToDevice,
+                             h->stream));
+  const int64_t nz = m->nnz > 0 ? m->nnz : 1;
+  if (scale == 0.0) {
+    KPM_TRY(dev_alloc(&out->data, nz * sizeof(double2), h->stream));
+    if (m->nnz > 0)
+      KPM_CUDA(cudaMemcpyAsync(out->data, m->data, m->nnz * sizeof(double2),
+                               cudaMemcpyHostToDevice, h->stream));
+  } else {
+    KPM_TRY(dev_alloc(&out->data, nz * sizeof(float2), h->stream));
+    if (m->nnz > 0) {
+      void* staging = nullptr;
+      KPM_TRY(dev_alloc(&staging, m->nnz * sizeof(double2), h->stream));
+      cudaError_t e = cudaMemcpyAsync(staging, m->data,
+                                      m->nnz * sizeof(double2),
+                                      cudaMemcpyHostToDevice, h->stream);
+      if (e == cudaSuccess) {
+        scale_to_c64_kernel<<<(unsigned)ceil_div(m->nnz, 256), 256, 0,
+                              h->stream>>>((const double2*)staging,
+                                           (float2*)out->data, m->nnz, scale);
+        count_launch(1);
+        e = cudaGetLastError();
+      }
+      dev_free(staging, h->stream);
+      KPM_CUDA(e);
+    }
+  }
+  KPM_CUDA(cudaStreamSynchronize(h->stream));
+  return KPM_OK;
+}
+
+void free_matrix(Matrix* m, cudaStream_t s) {
+  dev_free(m->indptr, s);
+  dev_free(m->indices, s);
+  dev_free(m->data, s);
+  m->indptr = nullptr;
+  m->indices = nullptr;
+  m->data = nullptr;
+}
+
+// ----------------------------------------------------------- vector layout
+// [R][N] complex128 (host order)  ->  [N][Rpad] complex (device order)
+template <typename OutT>
+__global__ void to_interleaved_kernel(const double2* __restrict__ in,
+                                      OutT* __restrict__ out, int64_t N,
+                                      int64_t R, int64_t Rpad) {
+  __shared__ double2 tile[32][33];
+  const int64_t n0 = (int64_t)blockIdx.x * 32;
+  const int64_t r0 = (int64_t)blockIdx.y * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    int64_t r = r0 + k, n = n0 + threadIdx.x;
+    double2 v = make_double2(0.0, 0.0);
+    if (r < R && n < N) v = in[r * N + n];
+    tile[k][threadIdx.x] = v;
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    int64_t n = n0 + k, r = r0 + threadIdx.x;
+    if (n < N && r < Rpad) {
+      double2 v = tile[threadIdx.x][k];
+      if constexpr (sizeof(OutT) == 16) {
+        out[n * Rpad + r] = *reinterpret_cast<OutT*>(&v);
+      } else {
+        float2 f = make_float2((float)v.x, (float)v.y);
+        out[n * Rpad + r] = *reinterpret_cast<OutT*>(&f);
+      }
+    }
+  }
+}
+
+// [N][Rpad] complex (device order) -> [R][N] complex128
+template <typename InT>
+__global__ void from_interleaved_kernel(const InT* __restrict__ in,
+                                        double2* __restrict__ out, int64_t N,
+                                        int64_t R, int64_t Rpad) {
+  __shared__ double2 tile[32][33];
+  const int64_t n0 = (int64_t)blockIdx.x * 32;
+  const int64_t r0 = (int64_t)blockIdx.y * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    int64_t n = n0 + k, r = r0 + threadIdx.x;
+    double2 v = make_double2(0.0, 0.0);
+    if (n < N && r < Rpad) {
+      if constexpr (sizeof(InT) == 16) {
+        v = *reinterpret_cast<const double2*>(&in[n * Rpad + r]);
+      } else {
+        float2 f = *reinterpret_cast<const float2*>(&in[n * Rpad + r]);
+        v = make_double2((double)f.x, (double)f.y);
+      }
+    }
+    tile[k][threadIdx.x] = v;
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    int64_t r = r0 + k, n = n0 + threadIdx.x;
+    if (r < R && n < N) out[r * N + n] = tile[threadIdx.x][k];
+  }
+}
+
+int upload_vectors(kpm_handle* h, const double* host, int64_t R, int64_t N,
+                   int64_t Rpad, void* dst) {
+  void* staging = nullptr;
+  size_t bytes = (size_t)R * N * 16;
+  KPM_TRY(dev_alloc(&staging, bytes, h->stream));
+  cudaError_t e = cudaMemcpyAsync(staging, host, bytes,
+                                  cudaMemcpyHostToDevice, h->stream);
+  if (e != cudaSuccess) {
+    dev_free(staging, h->stream);
+    KPM_CUDA(e);
+  }
+  dim3 blk(32, 8), grd((unsigned)ceil_div(N, 32), (unsigned)ceil_div(Rpad, 32));
+  if (h->precision == KPM_PREC_MIXED)
+    to_interleaved_kernel<float2><<<grd, blk, 0, h->stream>>>(
+        (const double2*)staging, (float2*)dst, N, R, Rpad);
+  else
+    to_interleaved_kernel<double2><<<grd, blk, 0, h->stream>>>(
+        (const double2*)staging, (double2*)dst, N, R, Rpad);
+  count_launch(1);
+  e = cudaGetLastError();
+  dev_free(staging, h->stream);
+  KPM_CUDA(e);
+  return KPM_OK;
+}
+
+int download_vectors(kpm_handle* h, const void* src, int64_t R, int64_t N,
+                     int64_t Rpad, double* host) {
+  void* staging = nullptr;
+  size_t bytes = (size_t)R * N * 16;
+  KPM_TRY(dev_alloc(&staging, bytes, h->stream));
+  dim3 blk(32, 8), grd((unsigned)ceil_div(N, 32), (unsigned)ceil_div(Rpad, 32));
+  if (h->precision == KPM_PREC_MIXED)
+    from_interleaved_kernel<float2><<<grd, blk, 0, h->stream>>>(
+        (const float2*)src, (double2*)staging, N, R, Rpad);
+  else
+    from_interleaved_kernel<double2><<<grd, blk, 0, h->stream>>>(
+        (const double2*)src, (double2*)staging, N, R, Rpad);
+  count_launch(1);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(host, staging, bytes, cudaMemcpyDeviceToHost,
+                        h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  dev_free(staging, h->stream);
+  KPM_CUDA(e);
+  return KPM_OK;
+}
+
+// ------------------------------------------------------------ step kernel
+template <bool MIXED> struct Traits;
+template <> struct Traits<false> {
+  using PT = double2;
+  using VT = double2;
+  static constexpr int VPL = 1;
+  static constexpr int G = GROUP_FP64;
+};
+template <> struct Traits<true> {
+  using PT = float4;
+  using VT = float2;
+  static constexpr int VPL = 2;
+  static constexpr int G = GROUP_FP32;
+};
+
+__device__ __forceinline__ void cmul_acc_exact(double& ar, double& ai,
+                                               double2 h, double2 x) {
+  // scipy csr_matvec: sum += Ax[jj] * Xx[Aj[jj]] with
+  // (hr xr - hi xi) + i (hr xi + hi xr), each operation rounded (no FMA).
+  double pr = __dsub_rn(__dmul_rn(h.x, x.x), __dmul_rn(h.y, x.y));
+  double pi = __dadd_rn(__dmul_rn(h.x, x.y), __dmul_rn(h.y, x.x));
+  ar = __dadd_rn(ar, pr);
+  ai = __dadd_rn(ai, pi);
+}
+
+template <bool MIXED, int MODE, bool DOTS>
+__global__ void __launch_bounds__(STEP_THREADS)
+cheb_step_kernel(StepArgs p) {
+  using T = Traits<MIXED>;
+  using PT = typename T::PT;
+  using VT = typename T::VT;
+  constexpr int VPL = T::VPL;
+  constexpr int G = T::G;
+  const int lane = threadIdx.x & (LANES - 1);
+  const int slot = threadIdx.x / LANES;
+  __shared__ double red[DOTS ? SLOTS : 1][DOTS ? G * 3 : 1];
+
+  const PT* __restrict__ x = reinterpret_cast<const PT*>(p.x);
+  const PT* prev = reinterpret_cast<const PT*>(p.prev);
+  PT* out = reinterpret_cast<PT*>(p.out);
+  const VT* __restrict__ vals = reinterpret_cast<const VT*>(p.vals);
+  const int32_t* __restrict__ indptr = p.indptr;
+  const int32_t* __restrict__ indices = p.indices;
+  const int64_t work = (int64_t)p.xitems * p.groups;
+  const int64_t stride = (int64_t)p.xitems * SLOTS;
+
+  for (int64_t w = blockIdx.x; w < work; w += gridDim.x) {
+    const int xi = (int)(w / p.groups);
+    const int g = (int)(w - (int64_t)xi * p.groups);
+    const int64_t col = (int64_t)g * LANES + lane;
+    double nrm[VPL], cre[VPL], cim[VPL];
+#pragma unroll
+    for (int k = 0; k < VPL; ++k) nrm[k] = cre[k] = cim[k] = 0.0;
+
+    for (int64_t i = (int64_t)xi * SLOTS + slot; i < p.rows; i += stride) {
+      const PT xv = x[i * p.rp + col];
+      if constexpr (MODE == STEP_NORM) {
+        if constexpr (MIXED) {
+          nrm[0] = fma((double)xv.x, (double)xv.x,
+                       fma((double)xv.y, (double)xv.y, nrm[0]));
+          nrm[1] = fma((double)xv.z, (double)xv.z,
+                       fma((double)xv.w, (double)xv.w, nrm[1]));
+        } else {
+          nrm[0] = fma(xv.x, xv.x, fma(xv.y, xv.y, nrm[0]));
+        }
+        continue;
+      }
+      const int beg = __ldg(indptr + i), end = __ldg(indptr + i + 1);
+      PT o;
+      if constexpr (!MIXED) {
+        double ar = 0.0, ai = 0.0;
+        int jj = beg;
+        for (; jj + 4 <= end; jj += 4) {
+          int c0 = __ldg(indices + jj), c1 = __ldg(indices + jj + 1);
+          int c2 = __ldg(indices + jj + 2), c3 = __ldg(indices + jj + 3);
+          double2 h0 = vals[jj], h1 = vals[jj + 1];
+          double2 h2 = vals[jj + 2], h3 = vals[jj + 3];
+          double2 x0 = x[(int64_t)c0 * p.rp + col];
+          double2 x1 = x[(int64_t)c1 * p.rp + col];
+          double2 x2 = x[(int64_t)c2 * p.rp + col];
+          double2 x3 = x[(int64_t)c3 * p.rp + col];
+          cmul_acc_exact(ar, ai, h0, x0);
+          cmul_acc_exact(ar, ai, h1, x1);
+          cmul_acc_exact(ar, ai, h2, x2);
+          cmul_acc_exact(ar, ai, h3, x3);
+        }
+        for (; jj < end; ++jj) {
+          int c = __ldg(indices + jj);
+          cmul_acc_exact(ar, ai, vals[jj], x[(int64_t)c * p.rp + col]);
+        }
+        // (H v - b v) * (1/a): numpy's order (kwant/kpm.py:1183; complex
+        // division by a real is a multiplication by the rounded reciprocal).
+        double tr = __dmul_rn(__dsub_rn(ar, __dmul_rn(p.b, xv.x)), p.inv_a);
+        double ti = __dmul_rn(__dsub_rn(ai, __dmul_rn(p.b, xv.y)), p.inv_a);
+        if constexpr (MODE == STEP_FIRST) {
+          o = make_double2(tr, ti);
+        } else {
+          const double2 pv = prev[i * p.rp + col];
+          o = make_double2(__dsub_rn(__dmul_rn(2.0, tr), pv.x),
+                           __dsub_rn(__dmul_rn(2.0, ti), pv.y));
+        }
+      } else {
+        // complex64: values are 2H/a, shift = -2b/a; FMA everywhere.
+        float a0r = p.shift * xv.x, a0i = p.shift * xv.y;
+        float a1r = p.shift * xv.z, a1i = p.shift * xv.w;
+        int jj = beg;
+        for (; jj + 4 <= end; jj += 4) {
+          int c[4];
+          float2 h[4];
+          float4 xx[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            c[u] = __ldg(indices + jj + u);
+            h[u] = vals[jj + u];
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) xx[u] = x[(int64_t)c[u] * p.rp + col];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            a0r = fmaf(h[u].x, xx[u].x, a0r);
+            a0r = fmaf(-h[u].y, xx[u].y, a0r);
+            a0i = fmaf(h[u].x, xx[u].y, a0i);
+            a0i = fmaf(h[u].y, xx[u].x, a0i);
+            a1r = fmaf(h[u].x, xx[u].z, a1r);
+            a1r = fmaf(-h[u].y, xx[u].w, a1r);
+            a1i = fmaf(h[u].x, xx[u].w, a1i);
+            a1i = fmaf(h[u].y, xx[u].z, a1i);
+          }
+        }
+        for (; jj < end; ++jj) {
+          int c = __ldg(indices + jj);
+          float2 h = vals[jj];
+          float4 xx = x[(int64_t)c * p.rp + col];
+          a0r = fmaf(h.x, xx.x, a0r);
+          a0r = fmaf(-h.y, xx.y, a0r);
+          a0i = fmaf(h.x, xx.y, a0i);
+          a0i = fmaf(h.y, xx.x, a0i);
+          a1r = fmaf(h.x, xx.z, a1r);
+          a1r = fmaf(-h.y, xx.w, a1r);
+          a1i = fmaf(h.x, xx.w, a1i);
+          a1i = fmaf(h.y, xx.z, a1i);
+        }
+        if constexpr (MODE == STEP_FIRST) {
+          o = make_float4(0.5f * a0r, 0.5f * a0i, 0.5f * a1r, 0.5f * a1i);
+        } else {
+          const float4 pv = prev[i * p.rp + col];
+          o = make_float4(a0r - pv.x, a0i - pv.y, a1r - pv.z, a1i - pv.w);
+        }
+      }
+      out[i * p.rp + col] = o;
+      if constexpr (DOTS) {
+        // <x|x> and <o|x> = sum conj(o) x
+        if constexpr (MIXED) {
+          double xr0 = xv.x, xi0 = xv.y, xr1 = xv.z, xi1 = xv.w;
+          double or0 = o.x, oi0 = o.y, or1 = o.z, oi1 = o.w;
+          nrm[0] = fma(xr0, xr0, fma(xi0, xi0, nrm[0]));
+          nrm[1] = fma(xr1, xr1, fma(xi1, xi1, nrm[1]));
+          cre[0] = fma(or0, xr0, fma(oi0, xi0, cre[0]));
+          cre[1] = fma(or1, xr1, fma(oi1, xi1, cre[1]));
+          cim[0] = fma(or0, xi0, fma(-oi0, xr0, cim[0]));
+          cim[1] = fma(or1, xi1, fma(-oi1, xr1, cim[1]));
+        } else {
+          nrm[0] = fma(xv.x, xv.x, fma(xv.y, xv.y, nrm[0]));
+          cre[0] = fma(o.x, xv.x, fma(o.y, xv.y, cre[0]));
+          cim[0] = fma(o.x, xv.y, fma(-o.y, xv.x, cim[0]));
+        }
+      }
+    }
+    if constexpr (DOTS || MODE == STEP_NORM) {
+#pragma unroll
+      for (int k = 0; k < VPL; ++k) {
+        red[slot][(lane * VPL + k) * 3 + 0] = nrm[k];
+        red[slot][(lane * VPL + k) * 3 + 1] = cre[k];
+        red[slot][(lane * VPL + k) * 3 + 2] = cim[k];
+      }
+      __syncthreads();
+      double* dst = p.partials + ((int64_t)g * p.xitems + xi) * (G * 3);
+      for (int e = threadIdx.x; e < G * 3; e += blockDim.x) {
+        double s = 0.0;
+#pragma unroll
+        for (int q = 0; q < SLOTS; ++q) s += red[q][e];
+        dst[e] = s;
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// Sum the row-partition partials of every vector in a fixed order and turn
+// them into moments.  One block per vector.
+__global__ void dos_finalize_kernel(const double* __restrict__ partials,
+                                    int G, int xitems, int64_t Rpad,
+                                    int mode, double2* mu01,
+                                    double2* mom, int64_t mom_stride,
+                                    int64_t slot_even, int64_t slot_odd) {
+  const int64_t v = blockIdx.x;
+  const int g = (int)(v / G), e0 = (int)(v % G) * 3;
+  __shared__ double s[3][128];
+  double acc[3] = {0.0, 0.0, 0.0};
+  for (int xi = threadIdx.x; xi < xitems; xi += blockDim.x) {
+    const double* src = partials + ((int64_t)g * xitems + xi) * (G * 3) + e0;
+    acc[0] += src[0];
+    acc[1] += src[1];
+    acc[2] += src[2];
+  }
+  for (int c = 0; c < 3; ++c) s[c][threadIdx.x] = acc[c];
+  __syncthreads();
+  for (int w = 64; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+      for (int c = 0; c < 3; ++c) s[c][threadIdx.x] += s[c][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x != 0) return;
+  const double nrm = s[0][0], cre = s[1][0], cim = s[2][0];
+  if (mode == STEP_FIRST) {
+    double2 m0 = make_double2(nrm, 0.0);
+    double2 m1 = make_double2(cre, -cim);  // <a0|a1> = conj(<a1|a0>)
+    mu01[2 * v] = m0;
+    mu01[2 * v + 1] = m1;
+    if (slot_even >= 0) mom[slot_even * mom_stride + v] = m0;
+    if (slot_odd >= 0) mom[slot_odd * mom_stride + v] = m1;
+  } else if (mode == STEP_RECUR) {
+    const double2 m0 = mu01[2 * v], m1 = mu01[2 * v + 1];
+    if (slot_even >= 0)
+      mom[slot_even * mom_stride + v] =
+          make_double2(2.0 * nrm - m0.x, 0.0 - m0.y);
+    if (slot_odd >= 0)
+      mom[slot_odd * mom_stride + v] =
+          make_double2(2.0 * cre - m1.x, 2.0 * cim - m1.y);
+  } else {  // STEP_NORM: odd tail
+    const double2 m0 = mu01[2 * v];
+    if (slot_even >= 0)
+      mom[slot_even * mom_stride + v] =
+          make_double2(2.0 * nrm - m0.x, 0.0 - m0.y);
+  }
+}
+
+// [count][Rpad] complex -> [R][count] complex
+__global__ void moments_to_host_order_kernel(const double2* __restrict__ in,
+                                             double2* __restrict__ out,
+                                             int64_t count, int64_t R,
+                                             int64_t Rpad, int64_t W) {
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t total = R * count * W;
+  if (idx >= total) return;
+  int64_t w = idx % W;
+  int64_t m = (idx / W) % count;
+  int64_t r = idx / (W * count);
+  out[idx] = in[(m * W + w) * Rpad + r];
+}
+
+// --------------------------------------------------------------- dispatch
+template <bool MIXED, int MODE, bool DOTS>
+static int launch_step_t(kpm_handle* h, const StepArgs& a) {
+  static int occ = -1;
+  if (occ < 0) {
+    int blocks = 0;
+    KPM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &blocks, cheb_step_kernel<MIXED, MODE, DOTS>, STEP_THREADS, 0));
+    occ = blocks > 0 ? blocks : 1;
+  }
+  int64_t work = (int64_t)a.xitems * a.groups;
+  int64_t grid = (int64_t)occ * h->num_sms;
+  if (grid > work) grid = work;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (h->profiling) {
+    while (h->prof_events.size() < h->prof_used + 2) {
+      cudaEvent_t e;
+      KPM_CUDA(cudaEventCreate(&e));
+      h->prof_events.push_back(e);
+    }
+    e0 = h->prof_events[h->prof_used];
+    e1 = h->prof_events[h->prof_used + 1];
+    h->prof_used += 2;
+    KPM_CUDA(cudaEventRecord(e0, h->stream));
+  }
+  cheb_step_kernel<MIXED, MODE, DOTS>
+      <<<(unsigned)grid, STEP_THREADS, 0, h->stream>>>(a);
+  count_launch(1);
+  KPM_CHECK_LAUNCH();
+  if (e1) KPM_CUDA(cudaEventRecord(e1, h->stream));
+  return KPM_OK;
+}
+
+int launch_step(kpm_handle* h, int mode, bool dots, const StepArgs& a) {
+  const bool mixed = h->precision == KPM_PREC_MIXED;
+  if (mixed) {
+    if (mode == STEP_FIRST)
+      return dots ? launch_step_t<true, STEP_FIRST, true>(h, a)
+                  : launch_step_t<true, STEP_FIRST, false>(h, a);
+    if (mode == STEP_RECUR)
+      return dots ? launch_step_t<true, STEP_RECUR, true>(h, a)
+                  : launch_step_t<true, STEP_RECUR, false>(h, a);
+    return launch_step_t<true, STEP_NORM, false>(h, a);
+  }
+  if (mode == STEP_FIRST)
+    return dots ? launch_step_t<false, STEP_FIRST, true>(h, a)
+                : launch_step_t<false, STEP_FIRST, false>(h, a);
+  if (mode == STEP_RECUR)
+    return dots ? launch_step_t<false, STEP_RECUR, true>(h, a)
+                : launch_step_t<false, STEP_RECUR, false>(h, a);
+  return launch_step_t<false, STEP_NORM, false>(h, a);
+}
+
+int ensure_partials(kpm_handle* h, int groups, int xitems) {
+  size_t need = (size_t)groups * xitems * group_size(h->precision) * 3;
+  if (need <= h->partials_cap) return KPM_OK;
+  dev_free(h->partials, h->stream);
+  h->partials = nullptr;
+  h->partials_cap = 0;
+  KPM_TRY(dev_alloc((void**)&h->partials, need * sizeof(double), h->stream));
+  h->partials_cap = need;
+  return KPM_OK;
+}
+
+StepArgs step_args(kpm_block* b, const void* x, const void* prev, void* out) {
+  kpm_handle* h = b->h;
+  StepArgs a{};
+  a.rows = b->N;
+  a.indptr = h->H.indptr;
+  a.indices = h->H.indices;
+  a.vals = h->H.data;
+  a.b = h->b;
+  a.inv_a = 1.0 / h->a;
+  a.shift = (float)(-2.0 * h->b / h->a);
+  a.x = x;
+  a.prev = prev;
+  a.out = out;
+  a.rp = b->Rpad / (h->precision == KPM_PREC_MIXED ? 2 : 1);
+  a.groups = b->groups;
+  a.xitems = xitems_for_rows(b->N);
+  a.partials = h->partials;
+  return a;
+}
+
+// Advance the block's recursion by one matvec.  On the first call alpha_1 =
+// H~ alpha_0; afterwards alpha_{n+1} = 2 H~ alpha_n - alpha_{n-1}.
+int block_advance(kpm_block* b, bool dots) {
+  void* x = b->p_cur;
+  if (b->steps_done == 0) {
+    void* out = b->buf[0];
+    StepArgs a = step_args(b, x, nullptr, out);
+    KPM_TRY(launch_step(b->h, STEP_FIRST, dots, a));
+    b->p_prev = b->p_cur;
+    b->p_cur = out;
+  } else {
+    void* out;
+    if (b->p_prev == b->a0 && b->keep_a0)
+      out = (b->p_cur == b->buf[0]) ? b->buf[1] : b->buf[0];
+    else
+      out = b->p_prev;  // in place: alpha_{n+1} overwrites alpha_{n-1}
+    StepArgs a = step_args(b, x, b->p_prev, out);
+    KPM_TRY(launch_step(b->h, STEP_RECUR, dots, a));
+    b->p_prev = b->p_cur;
+    b->p_cur = out;
+  }
+  b->steps_done += 1;
+  return KPM_OK;
+}
+
+int block_norm(kpm_block* b) {
+  StepArgs a = step_args(b, b->p_cur, nullptr, nullptr);
+  return launch_step(b->h, STEP_NORM, false, a);
+}
+
+int finalize(kpm_block* b, int mode, double2* mom, int64_t slot_even,
+             int64_t slot_odd) {
+  kpm_handle* h = b->h;
+  dos_finalize_kernel<<<(unsigned)b->Rpad, 128, 0, h->stream>>>(
+      h->partials, group_size(h->precision), xitems_for_rows(b->N), b->Rpad,
+      mode, (double2*)b->mu01, mom, b->Rpad, slot_even, slot_odd);
+  count_launch(1);
+  KPM_CHECK_LAUNCH();
+  return KPM_OK;
+}
+
+int moments_to_host(kpm_handle* h, const double2* dev, int64_t count,
+                    int64_t R, int64_t Rpad, int64_t W, double* host) {
+  if (count == 0) return KPM_OK;
+  double2* tmp = nullptr;
+  size_t n = (size_t)R * count * W;
+  KPM_TRY(dev_alloc((void**)&tmp, n * sizeof(double2), h->stream));
+  moments_to_host_order_kernel<<<(unsigned)ceil_div(n, 256), 256, 0,
+                                 h->stream>>>(dev, tmp, count, R, Rpad, W);
+  count_launch(1);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(host, tmp, n * sizeof(double2),
+                        cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  dev_free(tmp, h->stream);
+  KPM_CUDA(e);
+  return KPM_OK;
+}
+
+int timed_begin(kpm_handle* h) {
+  if (!h->ev_start) {
+    KPM_CUDA(cudaEventCreate(&h->ev_start));
+    KPM_CUDA(cudaEventCreate(&h->ev_stop));
+  }
+  KPM_CUDA(cudaEventRecord(h->ev_start, h->stream));
+  return KPM_OK;
+}
+
+int timed_end(kpm_handle* h) {
+  KPM_CUDA(cudaEventRecord(h->ev_stop, h->stream));
+  h->timed = true;
+  return KPM_OK;
+}
+
+}  // namespace kpm
+
+using namespace kpm;
+
+// ======================================================================
+//                                C ABI
+// ======================================================================
+extern "C" {
+
+int kpm_version(void) { return 10000; }
+
+int kpm_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return KPM_EINVAL;
+  strncpy(buf, g_err, len - 1);
+  buf[len - 1] = '\0';
+  return KPM_OK;
+}
+
+int kpm_device_count(int* count) {
+  if (!count) return KPM_EINVAL;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    n = 0;
+  }
+  *count = n;
+  return KPM_OK;
+}
+
+int kpm_launch_count(int64_t* count) {
+  if (!count) return KPM_EINVAL;
+  *count = g_launches.load();
+  return KPM_OK;
+}
+
+int kpm_create(const kpm_csr_desc* ham, double a, double b, int precision,
+               kpm_handle** out) {
+  KPM_REQUIRE(ham && out, "kpm_create: null argument");
+  KPM_REQUIRE(ham->rows > 0 && ham->nnz >= 0 && ham->indptr && ham->indices &&
+                  (ham->nnz == 0 || ham->data),
+              "kpm_create: invalid CSR descriptor");
+  KPM_REQUIRE(ham->rows < INT32_MAX && ham->nnz < INT32_MAX,
+              "kpm_create: CSR exceeds int32 indexing (rows=%lld nnz=%lld)",
+              (long long)ham->rows, (long long)ham->nnz);
+  KPM_REQUIRE(precision == KPM_PREC_FP64 || precision == KPM_PREC_MIXED,
+              "kpm_create: unknown precision %d", precision);
+  KPM_REQUIRE(a > 0 && std::isfinite(a) && std::isfinite(b),
+              "kpm_create: scale a must be positive and finite");
+  *out = nullptr;
+  auto* h = new kpm_handle();
+  h->precision = precision;
+  h->a = a;
+  h->b = b;
+  int st = init_device(&h->device, &h->num_sms);
+  if (st != KPM_OK) {
+    delete h;
+    return st;
+  }
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) !=
+      cudaSuccess) {
+    delete h;
+    set_error("kpm_create: stream creation failed");
+    return KPM_ECUDA;
+  }
+  h->own_stream = true;
+  st = upload_matrix(h, ham, h->precision == KPM_PREC_MIXED ? 2.0 / a : 0.0,
+                     &h->H);
+  if (st != KPM_OK) {
+    kpm_destroy(h);
+    return st;
+  }
+  *out = h;
+  return KPM_OK;
+}
+
+int kpm_set_stream(kpm_handle* h, void* stream) {
+  KPM_REQUIRE(h, "kpm_set_stream: null handle");
+  KPM_CUDA(cudaStreamSynchronize(h->stream));
+  if (h->own_stream) cudaStreamDestroy(h->stream);
+  h->stream = (cudaStream_t)stream;
+  h->own_stream = false;
+  return KPM_OK;
+}
+
+int kpm_get_stream(kpm_handle* h, void** stream) {
+  KPM_REQUIRE(h && stream, "kpm_get_stream: null argument");
+  *stream = (void*)h->stream;
+  return KPM_OK;
+}
+
+int kpm_synchronize(kpm_handle* h) {
+  KPM_REQUIRE(h, "kpm_synchronize: null handle");
+  KPM_CUDA(cudaStreamSynchronize(h->stream));
+  return KPM_OK;
+}
+
+int kpm_destroy(kpm_handle* h) {
+  if (!h) return KPM_OK;
+  free_matrix(&h->H, h->stream);
+  dev_free(h->partials, h->stream);
+  if (h->ev_start) cudaEventDestroy(h->ev_start);
+  if (h->ev_stop) cudaEventDestroy(h->ev_stop);
+  for (cudaEvent_t e : h->prof_events) cudaEventDestroy(e);
+  cudaStreamSynchronize(h->stream);
+  if (h->own_stream) cudaStreamDestroy(h->stream);
+  cudaGetLastError();
+  delete h;
+  return KPM_OK;
+}
+
+int kpm_profile(kpm_handle* h, int enable) {
+  KPM_REQUIRE(h, "kpm_profile: null handle");
+  h->profiling = enable != 0;
+  h->prof_used = 0;
+  return KPM_OK;
+}
+
+int kpm_profile_read(kpm_handle* h, int64_t* launches, double* total_ms) {
+  KPM_REQUIRE(h && launches && total_ms, "kpm_profile_read: null argument");
+  KPM_CUDA(cudaStreamSynchronize(h->stream));
+  double tot = 0.0;
+  for (size_t i = 0; i + 1 < h->prof_used; i += 2) {
+    float f = 0.f;
+    KPM_CUDA(cudaEventElapsedTime(&f, h->prof_events[i],
+                                  h->prof_events[i + 1]));
+    tot += f;
+  }
+  *launches = (int64_t)(h->prof_used / 2);
+  *total_ms = tot;
+  h->prof_used = 0;
+  return KPM_OK;
+}
+
+int kpm_last_kernel_ms(kpm_handle* h, double* ms) {
+  KPM_REQUIRE(h && ms, "kpm_last_kernel_ms: null argument");
+  KPM_REQUIRE(h->timed, "kpm_last_kernel_ms: nothing timed yet");
+  float f = 0.f;
+  KPM_CUDA(cudaEventSynchronize(h->ev_stop));
+  KPM_CUDA(cudaEventElapsedTime(&f, h->ev_start, h->ev_stop));
+  *ms = f;
+  return KPM_OK;
+}
+
+int kpm_block_create(kpm_handle* h, const double* vecs, int64_t R,
+                     int keep_a0, kpm_block** out) {
+  KPM_REQUIRE(h && vecs && out, "kpm_block_create: null argument");
+  KPM_REQUIRE(R > 0, "kpm_block_create: num_vectors must be positive");
+  *out = nullptr;
+  auto* b = new kpm_block();
+  b->h = h;
+  b->R = R;
+  b->N = h->H.rows;
+  const int G = group_size(h->precision);
+  b->Rpad = round_up(R, G);
+  b->groups = (int)(b->Rpad / G);
+  b->keep_a0 = keep_a0 != 0;
+  const size_t csz = h->precision == KPM_PREC_MIXED ? 8 : 16;
+  const size_t vbytes = (size_t)b->N * b->Rpad * csz;
+  int st = KPM_OK;
+  if (st == KPM_OK) st = dev_alloc(&b->buf[0], vbytes, h->stream);
+  if (st == KPM_OK) st = dev_alloc(&b->buf[1], vbytes, h->stream);
+  if (st == KPM_OK && b->keep_a0) st = dev_alloc(&b->a0, vbytes, h->stream);
+  if (st == KPM_OK && !b->keep_a0) b->a0 = b->buf[1];
+  if (st == KPM_OK)
+    st = dev_alloc((void**)&b->mu01, (size_t)b->Rpad * 2 * sizeof(double2),
+                   h->stream);
+  if (st == KPM_OK) st = upload_vectors(h, vecs, R, b->N, b->Rpad, b->a0);
+  if (st == KPM_OK) {
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) {
+      set_error("kpm_block_create: %s", cudaGetErrorString(e));
+      st = KPM_ECUDA;
+    }
+  }
+  if (st != KPM_OK) {
+    kpm_block_destroy(b);
+    return st;
+  }
+  b->p_cur = b->a0;
+  b->p_prev = nullptr;
+  *out = b;
+  return KPM_OK;
+}
+
+int kpm_block_rewind(kpm_block* b) {
+  KPM_REQUIRE(b, "kpm_block_rewind: null block");
+  if (!b->keep_a0) {
+    set_error("kpm_block_rewind: block was created without keep_a0");
+    return KPM_ESTATE;
+  }
+  b->p_cur = b->a0;
+  b->p_prev = nullptr;
+  b->steps_done = 0;
+  b->mode = -1;
+  return KPM_OK;
+}
+
+int kpm_block_destroy(kpm_block* b) {
+  if (!b) return KPM_OK;
+  cudaStream_t s = b->h->stream;
+  dev_free(b->buf[0], s);
+  dev_free(b->buf[1], s);
+  if (b->keep_a0) dev_free(b->a0, s);
+  dev_free(b->mu01, s);
+  dev_free(b->op_coef, s);
+  cudaStreamSynchronize(s);
+  cudaGetLastError();
+  delete b;
+  return KPM_OK;
+}
+
+int kpm_block_state(kpm_block* b, double* alpha_prev, double* alpha_cur) {
+  KPM_REQUIRE(b && alpha_cur, "kpm_block_state: null argument");
+  if (alpha_prev) {
+    if (!b->p_prev) {
+      set_error("kpm_block_state: no previous vector before the first step");
+      return KPM_ESTATE;
+    }
+    KPM_TRY(download_vectors(b->h, b->p_prev, b->R, b->N, b->Rpad,
+                             alpha_prev));
+  }
+  return download_vectors(b->h, b->p_cur, b->R, b->N, b->Rpad, alpha_cur);
+}
+
+int kpm_block_dos_moments(kpm_block* b, int64_t m_start, int64_t m_end,
+                          double* out) {
+  KPM_REQUIRE(b && out, "kpm_block_dos_moments: null argument");
+  KPM_REQUIRE(m_end >= 2 && m_start >= 0 && m_start < m_end,
+              "kpm_block_dos_moments: need 0 <= m_start < m_end, m_end >= 2 "
+              "(got %lld, %lld)", (long long)m_start, (long long)m_end);
+  kpm_handle* h = b->h;
+  if (m_start == 0) {
+    if (b->steps_done != 0) {
+      set_error("kpm_block_dos_moments: block already advanced; rewind it");
+      return KPM_ESTATE;
+    }
+  } else if (b->mode != 0 || m_start / 2 != b->steps_done) {
+    set_error("kpm_block_dos_moments: cannot resume at moment %lld "
+              "(state after %lld matvecs, mode %d)", (long long)m_start,
+              (long long)b->steps_done, b->mode);
+    return KPM_ESTATE;
+  }
+  b->mode = 0;
+  const int64_t count = m_end - m_start;
+  const int G = group_size(h->precision);
+  KPM_TRY(ensure_partials(h, b->groups, xitems_for_rows(b->N)));
+  double2* mom = nullptr;
+  KPM_TRY(dev_alloc((void**)&mom, (size_t)count * b->Rpad * sizeof(double2),
+                    h->stream));
+  (void)G;
+  int st = timed_begin(h);
+  auto slot = [&](int64_t m) -> int64_t {
+    return (m >= m_start && m < m_end) ? m - m_start : -1;
+  };
+  if (st == KPM_OK && m_start == 0) {
+    st = block_advance(b, true);
+    if (st == KPM_OK) st = finalize(b, STEP_FIRST, mom, slot(0), slot(1));
+  }
+  int64_t n0 = m_start / 2 > 1 ? m_start / 2 : 1;
+  for (int64_t n = n0; st == KPM_OK && n < m_end / 2; ++n) {
+    st = block_advance(b, true);
+    if (st == KPM_OK)
+      st = finalize(b, STEP_RECUR, mom, slot(2 * n), slot(2 * n + 1));
+  }
+  if (st == KPM_OK && (m_end % 2)) {
+    st = block_norm(b);
+    if (st == KPM_OK)
+      st = finalize(b, STEP_NORM, mom, slot(m_end - 1), -1);
+  }
+  if (st == KPM_OK) st = timed_end(h);
+  if (st == KPM_OK) st = moments_to_host(h, mom, count, b->R, b->Rpad, 1, out);
+  dev_free(mom, h->stream);
+  return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,277 @@
+// Kubo-Bastin correlator moments on the device.
+//
+// Correlator.__init__ (kwant/kpm.py:557-606) runs two Chebyshev recursions
+// and contracts their stored vectors:
+//   Psi_n   = v_beta T_n(H~) |r>            (kwant/kpm.py:708-718)
+//   Omega_m = T_m(H~') v_alpha |r>          (kwant/kpm.py:697-706, :603)
+//   mu_mn   = mean_r <Omega_m | Psi_n>      (kwant/kpm.py:685-695)
+// Here both recursions run batched over all R vectors; every step writes its
+// vectors straight into a K-major store (row n = one Chebyshev order,
+// K = orbital * R + vector), so the contraction is one "NT" GEMM over
+// K = N R:  mu = Omega^* Psi^T / R.
+//
+// Stores and contractions:
+//   FP64  : complex128 rows, FP64 CUDA-core GEMM (split-K, fixed-order
+//           reduction).
+//   BF16x3: each real component x stored as hi = bf16(x), lo = bf16(x - hi)
+//           in four planes (re_hi, re_lo, im_hi, im_lo); the tensor-core GEMM
+//           (kpm_gemm_tc.cu) forms hi*hi + hi*lo + lo*hi with FP32
+//           accumulation.
+
+#include <cuda_bf16.h>
+
+#include "kpm_common.cuh"
+#include "kpm_internal.cuh"
+#include "kpm_gemm.cuh"
+
+namespace kpm {
+
+// y[i][r] = sum_j V_ij x[j][r], written to the K-major store row
+// (K index i * R + r).  One thread per (row, vector); vectors fastest.
+template <bool MIXED, int STORE>
+__global__ void spmm_to_store_kernel(int64_t rows, int64_t R, int64_t Rpad,
+                                     const int32_t* __restrict__ ip,
+                                     const int32_t* __restrict__ ix,
+                                     const double2* __restrict__ v,
+                                     const void* __restrict__ x,
+                                     StoreRow dst) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= rows * R) return;
+  const int64_t i = idx / R, r = idx % R;
+  double yr = 0.0, yi = 0.0;
+  if (v == nullptr) {
+    if constexpr (MIXED) {
+      const float2 a = reinterpret_cast<const float2*>(x)[i * Rpad + r];
+      yr = a.x;
+      yi = a.y;
+    } else {
+      const double2 a = reinterpret_cast<const double2*>(x)[i * Rpad + r];
+      yr = a.x;
+      yi = a.y;
+    }
+  } else {
+    for (int jj = ip[i]; jj < ip[i + 1]; ++jj) {
+      const double2 h = v[jj];
+      double xr, xi;
+      if constexpr (MIXED) {
+        const float2 a =
+            reinterpret_cast<const float2*>(x)[(int64_t)ix[jj] * Rpad + r];
+        xr = a.x;
+        xi = a.y;
+      } else {
+        const double2 a =
+            reinterpret_cast<const double2*>(x)[(int64_t)ix[jj] * Rpad + r];
+        xr = a.x;
+        xi = a.y;
+      }
+      yr = fma(h.x, xr, fma(-h.y, xi, yr));
+      yi = fma(h.x, xi, fma(h.y, xr, yi));
+    }
+  }
+  store_put<STORE>(dst, idx, yr, yi);
+}
+
+// y[i][r] = sum_j V_ij x[j][r] in block layout (used for v_alpha |r>).
+template <bool MIXED>
+__global__ void spmm_block_kernel(int64_t rows, int64_t Rpad,
+                                  const int32_t* __restrict__ ip,
+                                  const int32_t* __restrict__ ix,
+                                  const double2* __restrict__ v,
+                                  const void* __restrict__ x, void* y) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= rows * Rpad) return;
+  const int64_t i = idx / Rpad, r = idx % Rpad;
+  double yr = 0.0, yi = 0.0;
+  for (int jj = ip[i]; jj < ip[i + 1]; ++jj) {
+    const double2 h = v[jj];
+    double xr, xi;
+    if constexpr (MIXED) {
+      const float2 a =
+          reinterpret_cast<const float2*>(x)[(int64_t)ix[jj] * Rpad + r];
+      xr = a.x;
+      xi = a.y;
+    } else {
+      const double2 a =
+          reinterpret_cast<const double2*>(x)[(int64_t)ix[jj] * Rpad + r];
+      xr = a.x;
+      xi = a.y;
+    }
+    yr = fma(h.x, xr, fma(-h.y, xi, yr));
+    yi = fma(h.x, xi, fma(h.y, xr, yi));
+  }
+  if constexpr (MIXED)
+    reinterpret_cast<float2*>(y)[idx] = make_float2((float)yr, (float)yi);
+  else
+    reinterpret_cast<double2*>(y)[idx] = make_double2(yr, yi);
+}
+
+template <int STORE>
+static int put_row(kpm_handle* h, const Matrix* V, const void* x, int64_t N,
+                   int64_t R, int64_t Rpad, StoreRow dst) {
+  const int64_t n = N * R;
+  const unsigned grid = (unsigned)ceil_div(n, 256);
+  const bool mixed = h->precision == KPM_PREC_MIXED;
+  const int32_t* ip = V ? V->indptr : nullptr;
+  const int32_t* ix = V ? V->indices : nullptr;
+  const double2* vv = V ? (const double2*)V->data : nullptr;
+  if (mixed)
+    spmm_to_store_kernel<true, STORE><<<grid, 256, 0, h->stream>>>(
+        N, R, Rpad, ip, ix, vv, x, dst);
+  else
+    spmm_to_store_kernel<false, STORE><<<grid, 256, 0, h->stream>>>(
+        N, R, Rpad, ip, ix, vv, x, dst);
+  count_launch(1);
+  KPM_CHECK_LAUNCH();
+  return KPM_OK;
+}
+
+// Build a block whose starting vectors are already on the device.
+static int block_from_device(kpm_handle* h, int64_t R, void* a0_owned,
+                             kpm_block** out) {
+  auto* b = new kpm_block();
+  b->h = h;
+  b->R = R;
+  b->N = h->H.rows;
+  const int G = group_size(h->precision);
+  b->Rpad = round_up(R, G);
+  b->groups = (int)(b->Rpad / G);
+  b->keep_a0 = true;
+  b->a0 = a0_owned;
+  const size_t csz = h->precision == KPM_PREC_MIXED ? 8 : 16;
+  const size_t vbytes = (size_t)b->N * b->Rpad * csz;
+  int st = dev_alloc(&b->buf[0], vbytes, h->stream);
+  if (st == KPM_OK) st = dev_alloc(&b->buf[1], vbytes, h->stream);
+  if (st == KPM_OK)
+    st = dev_alloc((void**)&b->mu01, (size_t)b->Rpad * 2 * 16, h->stream);
+  if (st != KPM_OK) {
+    kpm_block_destroy(b);
+    return st;
+  }
+  b->p_cur = b->a0;
+  *out = b;
+  return KPM_OK;
+}
+
+template <int STORE>
+static int run_recursion(kpm_block* b, const Matrix* V, int64_t M,
+                         Store* store, double a, double bshift) {
+  kpm_handle* h = b->h;
+  // per-call scale (the correlator's second recursion uses (a2, b2))
+  const double a_save = h->a, b_save = h->b;
+  h->a = a;
+  h->b = bshift;
+  int st = KPM_OK;
+  for (int64_t n = 0; st == KPM_OK && n < M; ++n) {
+    if (n > 0) st = block_advance(b, false);
+    if (st == KPM_OK)
+      st = put_row<STORE>(h, V, b->p_cur, b->N, b->R, b->Rpad,
+                          store->row(n));
+  }
+  h->a = a_save;
+  h->b = b_save;
+  return st;
+}
+
+}  // namespace kpm
+
+using namespace kpm;
+
+extern "C" {
+
+int kpm_correlator_moments(kpm_handle* h, double a2, double b2,
+                           const kpm_csr_desc* v_alpha,
+                           const kpm_csr_desc* v_beta, const double* vecs,
+                           int64_t R, int64_t M, int gemm, int per_vector,
+                           double* mu_out) {
+  KPM_REQUIRE(h && v_alpha && v_beta && vecs && mu_out,
+              "kpm_correlator_moments: null argument");
+  KPM_REQUIRE(R > 0 && M >= 2, "kpm_correlator_moments: need R > 0, M >= 2");
+  KPM_REQUIRE(v_alpha->rows == h->H.rows && v_beta->rows == h->H.rows,
+              "kpm_correlator_moments: operator shape mismatch");
+  KPM_REQUIRE(a2 > 0, "kpm_correlator_moments: a2 must be positive");
+  if (gemm == 2) gemm = h->precision == KPM_PREC_MIXED ? 1 : 0;
+  KPM_REQUIRE(gemm == 0 || gemm == 1, "kpm_correlator_moments: bad gemm");
+  if (gemm == 1 && per_vector) {
+    set_error("kpm_correlator_moments: per-vector moments need gemm=0");
+    return KPM_EUNSUPPORTED;
+  }
+  const int64_t N = h->H.rows;
+  const int64_t K = N * R;
+  cudaStream_t s = h->stream;
+  Matrix Va, Vb;
+  kpm_block *bR = nullptr, *bL = nullptr;
+  Store psi, omega;
+  int st = upload_matrix(h, v_alpha, 0.0, &Va);
+  if (st == KPM_OK) st = upload_matrix(h, v_beta, 0.0, &Vb);
+  const int kind = gemm == 1 ? STORE_BF16X3 : STORE_C128;
+  if (st == KPM_OK) st = store_alloc(&psi, kind, M, K, s);
+  if (st == KPM_OK) st = store_alloc(&omega, kind, M, K, s);
+  if (st == KPM_OK) st = kpm_block_create(h, vecs, R, 1, &bR);
+  if (st == KPM_OK) st = timed_begin(h);
+  // Psi_n = v_beta T_n(H~)|r>
+  if (st == KPM_OK)
+    st = kind == STORE_C128
+             ? run_recursion<STORE_C128>(bR, &Vb, M, &psi, h->a, h->b)
+             : run_recursion<STORE_BF16X3>(bR, &Vb, M, &psi, h->a, h->b);
+  // Omega_m = T_m(H~') v_alpha|r>
+  if (st == KPM_OK) {
+    const size_t csz = h->precision == KPM_PREC_MIXED ? 8 : 16;
+    void* a0L = nullptr;
+    st = dev_alloc(&a0L, (size_t)N * bR->Rpad * csz, s);
+    if (st == KPM_OK) {
+      const int64_t n = N * bR->Rpad;
+      if (h->precision == KPM_PREC_MIXED)
+        spmm_block_kernel<true><<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(
+            N, bR->Rpad, Va.indptr, Va.indices, (const double2*)Va.data,
+            bR->a0, a0L);
+      else
+        spmm_block_kernel<false><<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(
+            N, bR->Rpad, Va.indptr, Va.indices, (const double2*)Va.data,
+            bR->a0, a0L);
+      count_launch(1);
+      if (cudaGetLastError() != cudaSuccess) {
+        set_error("kpm_correlator_moments: spmm launch failed");
+        st = KPM_ECUDA;
+      }
+    }
+    if (st == KPM_OK) st = block_from_device(h, R, a0L, &bL);
+    else dev_free(a0L, s);
+  }
+  if (st == KPM_OK) {
+    // release the first recursion's vectors before the second one
+    kpm_block_destroy(bR);
+    bR = nullptr;
+    if (h->precision == KPM_PREC_MIXED) {
+      // complex64 values are pre-scaled by 2/a; a2 equals a up to rounding
+      // (kwant/kpm.py:576-579), so only the diagonal shift is re-derived.
+      st = kind == STORE_C128
+               ? run_recursion<STORE_C128>(bL, nullptr, M, &omega, h->a, b2)
+               : run_recursion<STORE_BF16X3>(bL, nullptr, M, &omega, h->a,
+                                             b2);
+    } else {
+      st = kind == STORE_C128
+               ? run_recursion<STORE_C128>(bL, nullptr, M, &omega, a2, b2)
+               : run_recursion<STORE_BF16X3>(bL, nullptr, M, &omega, a2, b2);
+    }
+  }
+  if (bL) {
+    kpm_block_destroy(bL);
+    bL = nullptr;
+  }
+  if (st == KPM_OK) {
+    if (gemm == 0)
+      st = gemm_fp64(h, &omega, &psi, M, K, R, per_vector, mu_out);
+    else
+      st = gemm_bf16x3(h, &omega, &psi, M, K, R, mu_out);
+  }
+  if (st == KPM_OK) st = timed_end(h);
+  if (bR) kpm_block_destroy(bR);
+  store_free(&psi, s);
+  store_free(&omega, s);
+  free_matrix(&Va, s);
+  free_matrix(&Vb, s);
+  cudaStreamSynchronize(s);
+  return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,73 @@
+// K-major vector stores and the moments-matrix contraction of the correlator.
+#pragma once
+
+#include <cuda_bf16.h>
+
+#include "kpm_common.cuh"
+
+namespace kpm {
+
+enum { STORE_C128 = 0, STORE_BF16X3 = 1 };
+
+// K padding of the BF16x3 planes: a multiple of the tensor-core K tile.
+constexpr int64_t STORE_KPAD = 128;
+
+struct StoreRow {
+  double2* c128;            // STORE_C128 row
+  __nv_bfloat16* p[4];      // STORE_BF16X3 row: re_hi, re_lo, im_hi, im_lo
+};
+
+struct Store {
+  int kind = STORE_C128;
+  int64_t M = 0, K = 0, Kp = 0;  // rows, logical K, padded K (row stride)
+  double2* c128 = nullptr;
+  __nv_bfloat16* planes = nullptr;  // 4 planes of M x Kp
+  StoreRow row(int64_t n) const {
+    StoreRow r{};
+    if (kind == STORE_C128) {
+      r.c128 = c128 + n * K;
+    } else {
+      for (int q = 0; q < 4; ++q) r.p[q] = planes + (q * M + n) * Kp;
+    }
+    return r;
+  }
+};
+
+__device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& hi,
+                                           __nv_bfloat16& lo) {
+  hi = __float2bfloat16_rn(x);
+  lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+}
+
+template <int STORE>
+__device__ __forceinline__ void store_put(const StoreRow& r, int64_t k,
+                                          double re, double im) {
+  if constexpr (STORE == STORE_C128) {
+    r.c128[k] = make_double2(re, im);
+  } else {
+    __nv_bfloat16 h, l;
+    split_bf16((float)re, h, l);
+    r.p[0][k] = h;
+    r.p[1][k] = l;
+    split_bf16((float)im, h, l);
+    r.p[2][k] = h;
+    r.p[3][k] = l;
+  }
+}
+
+int store_alloc(Store* s, int kind, int64_t M, int64_t K, cudaStream_t st);
+void store_free(Store* s, cudaStream_t st);
+
+// mu = Omega^* Psi^T / R  (M x M complex128 to the host); FP64 CUDA cores.
+int gemm_fp64(kpm_handle* h, const Store* omega, const Store* psi, int64_t M,
+              int64_t K, int64_t R, int per_vector, double* mu_host);
+// Same contraction on BF16x3 stores: tensor cores (tcgen05) when available,
+// FP32 accumulation.
+int gemm_bf16x3(kpm_handle* h, const Store* omega, const Store* psi,
+                int64_t M, int64_t K, int64_t R, double* mu_host);
+// CUDA-core evaluation of exactly the BF16x3 products (hi*hi + hi*lo +
+// lo*hi, FP32 per-tile accumulation): the check for the tensor-core kernel.
+int gemm_bf16x3_simt(kpm_handle* h, const Store* omega, const Store* psi,
+                     int64_t M, int64_t K, int64_t R, double* mu_host);
+
+}  // namespace kpm

@@ -1,0 +1,60 @@
+// Internal interfaces shared by the KPM translation units.
+#pragma once
+
+#include "kpm_common.cuh"
+
+namespace kpm {
+
+enum { STEP_FIRST = 0, STEP_RECUR = 1, STEP_NORM = 2 };
+
+struct StepArgs {
+  int64_t rows;
+  const int32_t* indptr;
+  const int32_t* indices;
+  const void* vals;
+  double b, inv_a;  // complex128: (H v - b v) * inv_a
+  float shift;      // complex64: values are 2H/a, diagonal shift -2b/a
+  const void* x;    // alpha_n        [rows][Rpad]
+  const void* prev; // alpha_{n-1}    (may alias out)
+  void* out;        // alpha_{n+1}
+  int64_t rp;       // 16-byte payloads per row
+  int groups;
+  int xitems;
+  double* partials; // [groups][xitems][group][3]
+};
+
+void count_launch(int n);
+int dev_alloc(void** p, size_t bytes, cudaStream_t s);
+void dev_free(void* p, cudaStream_t s);
+int init_device(int* device, int* num_sms);
+
+// CSR upload.  scale == 0 keeps complex128 values; otherwise values are
+// stored as complex64 multiplied by scale.
+int upload_matrix(kpm_handle* h, const kpm_csr_desc* m, double scale,
+                  Matrix* out);
+void free_matrix(Matrix* m, cudaStream_t s);
+
+int upload_vectors(kpm_handle* h, const double* host, int64_t R, int64_t N,
+                   int64_t Rpad, void* dst);
+int download_vectors(kpm_handle* h, const void* src, int64_t R, int64_t N,
+                     int64_t Rpad, double* host);
+
+int launch_step(kpm_handle* h, int mode, bool dots, const StepArgs& a);
+StepArgs step_args(kpm_block* b, const void* x, const void* prev, void* out);
+int block_advance(kpm_block* b, bool dots);
+int block_norm(kpm_block* b);
+int ensure_partials(kpm_handle* h, int groups, int xitems);
+int moments_to_host(kpm_handle* h, const double2* dev, int64_t count,
+                    int64_t R, int64_t Rpad, int64_t W, double* host);
+int timed_begin(kpm_handle* h);
+int timed_end(kpm_handle* h);
+
+// Device reconstruction of kpm_reconstruct from device moments laid out as
+// [R][M][W] complex128.
+int reconstruct_on_device(cudaStream_t s, int64_t R, int64_t M, int64_t W,
+                          const double2* moments, int mean, int is_real,
+                          double a, int kernel, double lorentz_l,
+                          const double* nodes,
+                          double* gammas_out, double* densities_out);
+
+}  // namespace kpm

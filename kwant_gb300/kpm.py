@@ -1,0 +1,849 @@
+"""Kernel polynomial method on a GB300: drop-in for ``kwant.kpm``.
+
+Same public API as kwant/kpm.py (``SpectralDensity``, ``Correlator``,
+``conductivity``, ``RandomVectors``, ``LocalVectors``, ``jackson_kernel``,
+``lorentz_kernel``, ``fermi_distribution``; kwant/kpm.py:32-34) with the hot
+path on the device:
+
+* the Chebyshev recursion of all vectors of a call runs as one batched,
+  fused sparse x multi-vector pass per step (``csrc/kpm_core.cu``), with the
+  moment dot products (DOS) or the operator (Density / Current / matrix,
+  ``csrc/kpm_ops.cu``) evaluated in the same step sequence;
+* the mean over vectors, the 1/a scale, the Jackson / Lorentz kernel and the
+  DCT-III reconstruction run on the device (``csrc/kpm_recon.cu``);
+* spectral bounds come from a device Lanczos (``csrc/kpm_lanczos.cu``), or
+  from ARPACK driving device matvecs (``bounds_method='arpack'``, which
+  reproduces the reference's bounds);
+* the correlator's two recursions and its moments-matrix contraction run on
+  the device (``csrc/kpm_correlator.cu``, ``csrc/kpm_gemm*.cu``).
+
+Extra keyword-only arguments: ``precision`` ('fp64': complex128 recursion in
+the reference's operation order; 'mixed': complex64 recursion with FP64
+accumulation of every dot product) and ``bounds_method``.
+
+Host code keeps the reference's semantics for everything that is not
+arithmetic on the vectors: argument checks and error messages, the random
+vector stream (``_v0`` first, then one block per vector from the same
+MT19937 stream), ``real_if_close``, resume bookkeeping and the cheap
+post-processing (``__call__`` at arbitrary energies, ``integrate``,
+``Correlator.__call__``).
+"""
+
+import math
+from collections.abc import Iterable
+
+import numpy as np
+from numpy.polynomial.chebyshev import chebval
+from scipy.integrate import simpson
+from scipy.sparse import coo_matrix, csr_matrix
+from scipy.sparse.linalg import LinearOperator, eigsh
+
+from . import _lib
+from . import operator as _operator
+
+__all__ = ['SpectralDensity', 'Correlator', 'conductivity',
+           'RandomVectors', 'LocalVectors', 'jackson_kernel', 'lorentz_kernel',
+           'fermi_distribution']
+
+SAMPLING = 2  # kwant/kpm.py:36
+
+_PRECISIONS = {'fp64': _lib.PREC_FP64, 'double': _lib.PREC_FP64,
+               'mixed': _lib.PREC_MIXED}
+
+
+# --------------------------------------------------------------------------
+# helpers mirroring the reference
+# --------------------------------------------------------------------------
+
+def ensure_rng(rng=None):
+    """kwant/_common.py:115-135."""
+    if rng is None:
+        return np.random.mtrand._rand
+    if isinstance(rng, (int, np.integer)):
+        return np.random.RandomState(rng)
+    if all(hasattr(rng, attr) for attr in ('random_sample', 'randn',
+                                           'randint', 'choice')):
+        return rng
+    raise ValueError("Expecting a seed or an object that offers the "
+                     "numpy.random.RandomState interface.")
+
+
+def _is_system(obj):
+    """A Kwant-like finite system (kwant.system.System or LatticeSystem)."""
+    return hasattr(obj, 'hamiltonian_submatrix') and hasattr(obj, 'graph')
+
+
+def _is_local_operator(obj):
+    return type(obj).__name__ in ('Density', 'Current') and \
+        hasattr(obj, 'where') and hasattr(obj, 'bind')
+
+
+def _kernel_id(kernel):
+    """Device id of a known kernel callable, else None."""
+    name = getattr(kernel, '__name__', None)
+    mod = getattr(kernel, '__module__', '') or ''
+    if name == 'jackson_kernel' and ('kpm' in mod):
+        return _lib.KERNEL_JACKSON
+    if name == 'lorentz_kernel' and ('kpm' in mod):
+        return _lib.KERNEL_LORENTZ
+    return None
+
+
+def _precision(precision):
+    try:
+        return _PRECISIONS[precision]
+    except KeyError:
+        raise ValueError("precision must be one of %s"
+                         % sorted(_PRECISIONS)) from None
+
+
+def _chebyshev_nodes(n_sampling):
+    """kwant/kpm.py:1190-1194."""
+    raw, step = np.linspace(np.pi, 0, n_sampling, endpoint=False,
+                            retstep=True)
+    return np.cos(raw + step / 2)
+
+
+def jackson_kernel(moments):
+    """Convolutes ``moments`` with the Jackson kernel (kwant/kpm.py:1106-1123,
+    Rev. Mod. Phys. 78, 275, Eq. 71).  Host version for user code; the
+    density reconstruction applies the same weights on the device."""
+    n_moments = len(moments)
+    m = np.arange(n_moments)
+    kernel_array = ((n_moments - m + 1) *
+                    np.cos(np.pi * m / (n_moments + 1)) +
+                    np.sin(np.pi * m / (n_moments + 1)) /
+                    np.tan(np.pi / (n_moments + 1)))
+    kernel_array /= n_moments + 1
+    return np.transpose(np.transpose(moments) * kernel_array)
+
+
+def lorentz_kernel(moments, l=4):
+    """Convolutes ``moments`` with the Lorentz kernel
+    (kwant/kpm.py:1126-1142)."""
+    n_moments = len(moments)
+    m = np.arange(n_moments)
+    kernel_array = np.sinh(l * (1 - m / n_moments)) / np.sinh(l)
+    return np.transpose(np.transpose(moments) * kernel_array)
+
+
+def fermi_distribution(energy, mu, temperature):
+    """kwant/kpm.py:990-1009."""
+    if temperature < 0:
+        raise ValueError("temperature must be non-negative")
+    elif temperature == 0:
+        return np.array(np.less(energy - mu, 0), dtype=float)
+    else:
+        return 1 / (1 + np.exp((energy - mu) / temperature))
+
+
+def _rescale_ab(lmin, lmax, eps):
+    """kwant/kpm.py:1174-1180."""
+    tol = eps / 2
+    a = np.abs(lmax - lmin) / (2. - eps)
+    b = (lmax + lmin) / 2.
+    if lmax - lmin <= abs(lmax + lmin) * tol / 2:
+        raise ValueError(
+            'The Hamiltonian has a single eigenvalue, it is not possible to '
+            'obtain a spectral density.')
+    return a, b
+
+
+def spectral_bounds(hamiltonian, eps=0.05, v0=None, method='lanczos'):
+    """Lowest and highest eigenvalue of ``hamiltonian`` (the two eigsh calls
+    of kwant/kpm.py:1169-1172).  'lanczos': FP64 Lanczos on the device with
+    Ritz-residual widening; 'arpack': scipy's ARPACK (tol = eps/2) with every
+    matvec on the device, which reproduces the reference's bounds."""
+    ham = csr_matrix(hamiltonian)
+    n = ham.shape[0]
+    if v0 is None:
+        v0 = np.exp(2j * np.pi * np.random.RandomState(0).random_sample(n))
+    tol = eps / 2
+    if method == 'lanczos':
+        lo, hi, _ = _lib.bounds(ham, v0, tol, max_iter=max(50, min(n, 3000)))
+        return lo, hi
+    if method == 'arpack':
+        h = _lib.Handle(ham, 1.0, 0.0, _lib.PREC_FP64)
+        op = LinearOperator(shape=ham.shape, matvec=h.matvec, dtype=complex)
+        try:
+            lmax = eigsh(op, k=1, which='LA', return_eigenvectors=False,
+                         tol=tol, v0=v0)[0]
+            lmin = eigsh(op, k=1, which='SA', return_eigenvectors=False,
+                         tol=tol, v0=v0)[0]
+        finally:
+            h.close()
+        return lmin, lmax
+    raise ValueError("bounds_method must be 'lanczos' or 'arpack'")
+
+
+class _RescaledHamiltonian(LinearOperator):
+    """The reference's ``SpectralDensity.hamiltonian`` (kwant/kpm.py:1182-1185)
+    with the matvec on the device."""
+
+    def __init__(self, ham, a, b):
+        self._ham = ham
+        self._a, self._b = a, b
+        self._dev = None
+        super().__init__(dtype=complex, shape=ham.shape)
+
+    def _matvec(self, v):
+        if self._dev is None:
+            self._dev = _lib.Handle(self._ham, 1.0, 0.0, _lib.PREC_FP64)
+        v = np.asarray(v, complex).ravel()
+        return (self._dev.matvec(v) - self._b * v) / self._a
+
+
+# --------------------------------------------------------------------------
+# vector factories (kwant/kpm.py:850-985)
+# --------------------------------------------------------------------------
+
+class _VectorFactory:
+    """kwant/kpm.py:850-929."""
+
+    def __init__(self, vectors=None, num_vectors=None, accumulate=True):
+        assert isinstance(vectors, Iterable)
+        try:
+            _len = len(vectors)
+            if num_vectors is None:
+                num_vectors = _len
+        except TypeError:
+            _len = np.inf
+            if num_vectors is None:
+                raise ValueError("'num_vectors' must be specified when "
+                                 "'vectors' has no len() method.")
+        self._max_vectors = _len
+        self._iterator = iter(vectors)
+        self.accumulate = accumulate
+        self.saved_vectors = []
+        self.num_vectors = 0
+        self.add_vectors(num_vectors=num_vectors)
+        self._last_idx = -np.inf
+        self._last_vector = None
+
+    def _fill_in_saved_vectors(self, index):
+        if index < self._last_idx and not self.accumulate:
+            raise ValueError("Cannot get previous values if 'accumulate' "
+                             "is False")
+        if index >= self.num_vectors:
+            raise IndexError('Requested more vectors than available')
+        self._last_idx = index
+        if self.accumulate:
+            if self.saved_vectors[index] is None:
+                self.saved_vectors[index] = next(self._iterator)
+        else:
+            self._last_vector = next(self._iterator)
+
+    def __getitem__(self, index):
+        self._fill_in_saved_vectors(index)
+        if self.accumulate:
+            return self.saved_vectors[index]
+        return self._last_vector
+
+    def add_vectors(self, num_vectors=None):
+        if num_vectors is None:
+            raise ValueError("'num_vectors' must be specified.")
+        else:
+            if num_vectors <= 0 or num_vectors != int(num_vectors):
+                raise ValueError("'num_vectors' must be a positive integer")
+            elif self.num_vectors + num_vectors > self._max_vectors:
+                raise ValueError("'num_vectors' is larger than available "
+                                 "vectors")
+        self.num_vectors += num_vectors
+        if self.accumulate:
+            self.saved_vectors.extend([None] * num_vectors)
+
+
+def _normalize_orbs_where(syst, where):
+    """kwant/kpm.py:1025-1039 (and _from_where_to_orbs, :1012-1022)."""
+    if _is_system(syst):
+        sr = np.asarray(syst.site_ranges, dtype=np.int64)
+        tot_norbs = int(sr[-1, 2])
+        where = _operator._normalize_site_where(syst, where)
+        start, norbs = _operator._site_orbitals(sr, where.reshape(-1))
+        orbs = []
+        for s, n in zip(start, norbs):
+            orbs.extend(range(s, s + n))
+    else:
+        try:
+            tot_norbs = csr_matrix(syst).shape[0]
+        except TypeError:
+            raise TypeError("'syst' is neither a matrix "
+                            "nor a Kwant system.")
+        orbs = (range(tot_norbs) if where is None
+                else np.asarray(where, int))
+    return tot_norbs, orbs
+
+
+def RandomVectors(syst, where=None, rng=None):
+    """Random-phase vectors exp(2 pi i u) on the orbitals of ``where``
+    (kwant/kpm.py:932-951)."""
+    rng = ensure_rng(rng)
+    tot_norbs, orbs = _normalize_orbs_where(syst, where)
+    while True:
+        vector = np.zeros(tot_norbs, dtype=complex)
+        vector[orbs] = np.exp(2j * np.pi * rng.random_sample(len(orbs)))
+        yield vector
+
+
+class LocalVectors:
+    """Unit vectors on the orbitals of ``where`` (kwant/kpm.py:954-985)."""
+
+    def __init__(self, syst, where=None, *args):
+        self.tot_norbs, self.orbs = _normalize_orbs_where(syst, where)
+        self._idx = 0
+
+    def __len__(self):
+        return len(self.orbs)
+
+    def __iter__(self):
+        return self
+
+    def __next__(self):
+        if self._idx < len(self):
+            vector = np.zeros(self.tot_norbs)
+            vector[self.orbs[self._idx]] = 1
+            self._idx = self._idx + 1
+            return vector
+        raise StopIteration('Too many vectors requested from this generator')
+
+
+# --------------------------------------------------------------------------
+# SpectralDensity
+# --------------------------------------------------------------------------
+
+class _Batch:
+    """Vectors [r0, r0 + R) of a SpectralDensity with their device state."""
+
+    def __init__(self, r0, block):
+        self.r0 = r0
+        self.block = block
+
+
+class SpectralDensity:
+    r"""Spectral density of an operator by the kernel polynomial method.
+
+    Drop-in for ``kwant.kpm.SpectralDensity`` (kwant/kpm.py:39-490); see the
+    module docstring for what runs on the device.  ``energies``,
+    ``densities``, ``num_moments``, ``num_vectors``, ``bounds``, ``eps``,
+    ``kernel``, ``mean``, ``__call__``, ``integrate``, ``add_moments`` and
+    ``add_vectors`` behave as in the reference.
+
+    Extra keyword-only parameters
+    -----------------------------
+    precision : 'fp64' (default) or 'mixed'
+    bounds_method : 'lanczos' (default) or 'arpack'
+    """
+
+    def __init__(self, hamiltonian, params=None, operator=None,
+                 num_vectors=10, num_moments=None, energy_resolution=None,
+                 vector_factory=None, bounds=None, eps=0.05, rng=None,
+                 kernel=None, mean=True, accumulate_vectors=True, *,
+                 precision='fp64', bounds_method='lanczos'):
+
+        if num_moments and energy_resolution:
+            raise TypeError("either 'num_moments' or 'energy_resolution' "
+                            "must be provided.")
+        self.eps = eps
+        self._precision = _precision(precision)
+
+        if _is_system(hamiltonian):
+            hamiltonian = hamiltonian.hamiltonian_submatrix(params=params,
+                                                            sparse=True)
+        try:
+            hamiltonian = csr_matrix(hamiltonian)
+        except Exception:
+            raise ValueError("'hamiltonian' is neither a matrix "
+                             "nor a Kwant system.")
+        if hamiltonian.ndim != 2 or hamiltonian.shape[0] != \
+                hamiltonian.shape[1]:
+            raise ValueError("'hamiltonian' is neither a matrix "
+                             "nor a Kwant system.")
+
+        # operator: lowered to the device term form (kwant/kpm.py:187-198)
+        if operator is None:
+            self.operator = None
+            self._lowered = None
+        elif _is_local_operator(operator):
+            self.operator = operator.bind(params=params)
+            self._lowered = _operator.lower(self.operator, params=params)
+        elif callable(operator):
+            raise NotImplementedError(
+                'an arbitrary Python callable operator cannot run on the '
+                'device; pass a kwant Density/Current operator or a matrix')
+        elif hasattr(operator, 'dot'):
+            operator = csr_matrix(operator)
+            self.operator = operator
+            self._lowered = _operator.lower_matrix(operator)
+        else:
+            raise ValueError("Parameter 'operator' has no '.dot' "
+                             "attribute and is not callable.")
+
+        self.mean = mean
+        rng = ensure_rng(rng)
+        self._v0 = np.exp(2j * np.pi * rng.random_sample(hamiltonian.shape[0]))
+
+        if eps <= 0:
+            raise ValueError("'eps' must be positive")
+
+        if bounds:
+            lmin, lmax = bounds
+        else:
+            lmin, lmax = spectral_bounds(hamiltonian, eps, self._v0,
+                                         bounds_method)
+        self._a, self._b = _rescale_ab(lmin, lmax, eps)
+        self._ham_csr = hamiltonian
+        self.hamiltonian = _RescaledHamiltonian(hamiltonian, self._a, self._b)
+        self.bounds = (self._b - self._a, self._b + self._a)
+
+        if energy_resolution:
+            num_moments = math.ceil((1.6 * self._a) / energy_resolution)
+        elif num_moments is None:
+            num_moments = 100
+        if num_moments <= 0 or num_moments != int(num_moments):
+            raise ValueError("'num_moments' must be a positive integer")
+        num_moments = int(num_moments)
+        if num_moments < 2:
+            raise ValueError("'num_moments' must be at least 2")
+
+        if vector_factory is None:
+            self._vector_factory = _VectorFactory(
+                RandomVectors(hamiltonian, rng=rng),
+                num_vectors=num_vectors, accumulate=accumulate_vectors)
+        else:
+            if not isinstance(vector_factory, Iterable):
+                raise TypeError('vector_factory must be iterable')
+            try:
+                len(vector_factory)
+            except TypeError:
+                if num_vectors is None:
+                    raise ValueError('num_vectors must be provided if'
+                                     'vector_factory has no length.')
+            self._vector_factory = _VectorFactory(
+                vector_factory, num_vectors=num_vectors,
+                accumulate=accumulate_vectors)
+        num_vectors = self._vector_factory.num_vectors
+
+        self._handle = _lib.Handle(_lib.Csr(hamiltonian), self._a, self._b,
+                                   self._precision)
+        self._op = None if self._lowered is None else \
+            _lib.Op(self._handle, self._lowered)
+        self._batches = []
+        self._moments_arr = None   # (R, M) or (R, M, W) complex128
+
+        self.num_moments = 0
+        self._update_moments_list(num_moments, num_vectors)
+        self.num_moments = num_moments
+
+        self.kernel = kernel if kernel is not None else jackson_kernel
+        self._reconstruct()
+
+    # -- public properties -------------------------------------------------
+    @property
+    def energies(self):
+        return (self._a * _chebyshev_nodes(SAMPLING * self.num_moments)
+                + self._b)
+
+    @property
+    def num_vectors(self):
+        return 0 if self._moments_arr is None else self._moments_arr.shape[0]
+
+    @property
+    def _moments_list(self):
+        """Per-vector moments, as the reference stores them
+        (kwant/kpm.py:486-490)."""
+        if self._moments_arr is None:
+            return []
+        arr = self._moments_arr
+        if self._lowered is None or self._lowered.scalar:
+            arr = arr[..., 0]
+        return list(arr)
+
+    @property
+    def _last_two_alphas(self):
+        """(alpha_{n-1}, alpha_n) of every vector, read from the device."""
+        out = []
+        for batch in self._batches:
+            prev, cur = batch.block.state()
+            out.extend(zip(prev, cur))
+        return out
+
+    # -- moments -------------------------------------------------------------
+    def _block_moments(self, block, m_start, m_end):
+        if self._op is None:
+            return block.dos_moments(m_start, m_end)
+        return block.op_moments(self._op, m_start, m_end)
+
+    def _update_moments_list(self, n_moments, num_vectors):
+        """kwant/kpm.py:390-490 on the device."""
+        have = self.num_vectors
+        if have == num_vectors:
+            new_vectors = 0
+        elif have < num_vectors:
+            new_vectors = num_vectors - have
+        else:
+            raise ValueError('Cannot decrease number of vectors')
+
+        if n_moments == self.num_moments:
+            new_moments = 0
+            if new_vectors == 0:
+                return
+        else:
+            if not self._vector_factory.accumulate and self.num_moments:
+                raise ValueError("Cannot increase the number of moments if "
+                                 "'accumulate_vectors' is 'False'.")
+            new_moments = n_moments - self.num_moments
+            if new_moments < 0:
+                raise ValueError('Cannot decrease number of moments')
+            if new_vectors != 0 and self.num_moments:
+                raise ValueError("Only 'num_moments' *or* 'num_vectors' "
+                                 "may be updated at a time.")
+
+        if new_vectors:
+            vecs = np.array([np.asarray(self._vector_factory[r], complex)
+                             for r in range(have, num_vectors)])
+            if vecs.ndim != 2 or vecs.shape[1] != self._ham_csr.shape[0]:
+                raise ValueError('vectors must have the length of the '
+                                 'Hamiltonian')
+            keep = self._vector_factory.accumulate or self._op is not None
+            block = _lib.Block(self._handle, vecs, keep_a0=keep)
+            mom = self._block_moments(block, 0, n_moments)
+            if self._op is None:
+                mom = mom[:, :, None]
+            self._moments_arr = mom if self._moments_arr is None else \
+                np.concatenate([self._moments_arr, mom], axis=0)
+            if self._vector_factory.accumulate:
+                self._batches.append(_Batch(have, block))
+            else:
+                block.close()
+        elif new_moments:
+            parts = []
+            for batch in self._batches:
+                mom = self._block_moments(batch.block, self.num_moments,
+                                          n_moments)
+                if self._op is None:
+                    mom = mom[:, :, None]
+                parts.append(mom)
+            self._moments_arr = np.concatenate(
+                [self._moments_arr, np.concatenate(parts, axis=0)], axis=1)
+
+    def _moments(self):
+        """kwant/kpm.py:378-388 (host copy of the reduced moments)."""
+        moments = np.real_if_close(self._moments_list)
+        moments = np.swapaxes(moments, 0, 1)
+        if self.mean:
+            moments = np.mean(moments, axis=1)
+        moments /= self._a
+        return self.kernel(moments)
+
+    def _reconstruct(self):
+        """Mean, 1/a, kernel and DCT on the device (kwant/kpm.py:251-252)."""
+        arr = self._moments_arr                      # (R, M, W)
+        R, M, W = arr.shape
+        is_real = bool(np.all(np.abs(arr.imag) <
+                              100 * np.finfo(np.float64).eps))
+        nodes = _chebyshev_nodes(SAMPLING * M)
+        kid = _kernel_id(self.kernel)
+        if kid is not None:
+            gam, rho = _lib.reconstruct(arr, self.mean, is_real, self._a, kid,
+                                        4.0, nodes)
+        else:
+            # user kernel: runs on the host (user code); DCT on the device
+            mom = self._moments()
+            mom = np.asarray(mom)
+            flat = mom.reshape(M, -1)
+            gam, rho = _lib.reconstruct(
+                np.ascontiguousarray(flat[None, :, :]), True,
+                not np.iscomplexobj(flat), 1.0, _lib.KERNEL_NONE, 4.0, nodes)
+        scalar = self._lowered is None or self._lowered.scalar
+        if self.mean:
+            shape = (2 * M,) if scalar else (2 * M, W)
+        else:
+            shape = (2 * M, R) if scalar else (2 * M, R, W)
+        if is_real:
+            gam, rho = gam.real, rho.real
+        self._gammas = gam.reshape(shape)
+        self.densities = rho.reshape(shape)
+
+    # -- public methods ------------------------------------------------------
+    def __call__(self, energy=None):
+        """kwant/kpm.py:263-295."""
+        if energy is None:
+            return self.energies, self.densities
+        energy = np.asarray(energy)
+        e = (energy - self._b) / self._a
+        g_e = (np.pi * np.sqrt(1 - e) * np.sqrt(1 + e))
+        moments = self._moments()
+        moments[1:] = 2 * moments[1:]
+        return np.transpose(chebval(e, moments) / g_e)
+
+    def integrate(self, distribution_function=None):
+        """kwant/kpm.py:297-316."""
+        factor = self._a / (2 * self.num_moments)
+        if distribution_function is None:
+            rho = self._gammas
+        else:
+            distribution_array = distribution_function(self.energies)
+            rho = np.transpose(self._gammas.transpose() * distribution_array)
+        return factor * np.sum(rho, axis=0)
+
+    def add_moments(self, num_moments=None, *, energy_resolution=None):
+        """kwant/kpm.py:318-358."""
+        if not ((num_moments is None) ^ (energy_resolution is None)):
+            raise TypeError("either 'num_moments' or 'energy_resolution' "
+                            "must be provided.")
+        if energy_resolution:
+            if energy_resolution <= 0:
+                raise ValueError("'energy_resolution' must be positive")
+            present_resolution = self._a * 1.6 / self.num_moments
+            if present_resolution < energy_resolution:
+                raise ValueError('Energy resolution is already smaller '
+                                 'than the requested resolution')
+            num_moments = math.ceil((1.6 * self._a) / energy_resolution)
+        if (num_moments is None or num_moments <= 0
+                or num_moments != int(num_moments)):
+            raise ValueError("'num_moments' must be a positive integer")
+        self._update_moments_list(self.num_moments + int(num_moments),
+                                  self.num_vectors)
+        self.num_moments += int(num_moments)
+        self._reconstruct()
+
+    def add_vectors(self, num_vectors=None):
+        """kwant/kpm.py:360-376."""
+        self._vector_factory.add_vectors(num_vectors)
+        num_vectors = self._vector_factory.num_vectors - self.num_vectors
+        self._update_moments_list(self.num_moments,
+                                  self.num_vectors + num_vectors)
+        self._reconstruct()
+
+
+# --------------------------------------------------------------------------
+# Correlator / conductivity
+# --------------------------------------------------------------------------
+
+def _operator_matrix(op, params, n):
+    """CSR matrix of an operator acting to the right (kwant/kpm.py:1088-1103):
+    None -> identity, Density/Current -> its ACT map, matrix -> itself."""
+    if op is None:
+        from scipy.sparse import identity
+        return identity(n, dtype=complex, format='csr')
+    if _is_local_operator(op):
+        if isinstance(op, _operator._LocalOperator):
+            op = op.bind(params=params) if not op._bound else op
+        return _operator.act_matrix(op, n, params)
+    if callable(op) and not hasattr(op, 'dot'):
+        raise NotImplementedError(
+            'an arbitrary Python callable operator cannot run on the '
+            'device; pass a kwant operator or a matrix')
+    if hasattr(op, 'dot'):
+        return csr_matrix(op)
+    raise TypeError("The operators must have a '.dot' "
+                    "attribute or must be callable.")
+
+
+class Correlator:
+    """Response of the correlation between two operators
+    (kwant/kpm.py:493-760), with both Chebyshev recursions and the
+    moments-matrix contraction on the device.
+
+    Extra keyword-only arguments: ``precision`` ('fp64' | 'mixed'),
+    ``bounds_method``, ``gemm`` ('auto' | 'fp64' | 'bf16x3').
+    """
+
+    def __init__(self, hamiltonian, operator1=None, operator2=None,
+                 **kwargs):
+        params = kwargs.get('params')
+        self.mean = kwargs.get('mean', True)
+        self._accumulate = kwargs.get('accumulate_vectors', False)
+        precision = kwargs.pop('precision', 'fp64')
+        bounds_method = kwargs.pop('bounds_method', 'lanczos')
+        gemm = kwargs.pop('gemm', 'auto')
+        self._gemm = {'auto': 2, 'fp64': 0, 'bf16x3': 1,
+                      'bf16x3-simt': 3}[gemm]
+        self._precision = _precision(precision)
+        kwargs.pop('operator', None)
+        if _is_system(hamiltonian):
+            hamiltonian = hamiltonian.hamiltonian_submatrix(params=params,
+                                                            sparse=True)
+        try:
+            hamiltonian = csr_matrix(hamiltonian)
+        except Exception:
+            raise ValueError("'hamiltonian' is neither a matrix "
+                             "nor a Kwant system.")
+        n = hamiltonian.shape[0]
+        self._ham_csr = hamiltonian
+        self._op1 = _operator_matrix(operator1, params, n)
+        self._op2 = _operator_matrix(operator2, params, n)
+
+        # the state of the first SpectralDensity of the reference
+        # (kwant/kpm.py:570-575): rng stream, _v0, bounds, num_moments
+        num_moments = kwargs.get('num_moments')
+        energy_resolution = kwargs.get('energy_resolution')
+        if num_moments and energy_resolution:
+            raise TypeError("either 'num_moments' or 'energy_resolution' "
+                            "must be provided.")
+        eps = kwargs.get('eps', 0.05)
+        self.eps = eps
+        rng_arg = kwargs.get('rng')
+        rng = ensure_rng(rng_arg)
+        self._v0 = np.exp(2j * np.pi * rng.random_sample(n))
+        if eps <= 0:
+            raise ValueError("'eps' must be positive")
+        bounds = kwargs.get('bounds')
+        if bounds:
+            lmin, lmax = bounds
+        else:
+            lmin, lmax = spectral_bounds(hamiltonian, eps, self._v0,
+                                         bounds_method)
+        self._a, self._b = _rescale_ab(lmin, lmax, eps)
+        # second recursion: bounds that reproduce (a, b) (kwant/kpm.py:576-579)
+        _a = self._a * (1 - eps / 2)
+        self._a2, self._b2 = _rescale_ab(self._b - _a, self._b + _a, eps)
+        if energy_resolution:
+            num_moments = math.ceil((1.6 * self._a) / energy_resolution)
+        elif num_moments is None:
+            num_moments = 100
+        if num_moments <= 0 or num_moments != int(num_moments):
+            raise ValueError("'num_moments' must be a positive integer")
+        self.num_moments = int(num_moments)
+
+        vector_factory = kwargs.get('vector_factory')
+        num_vectors = kwargs.get('num_vectors', 10)
+        if vector_factory is None:
+            self._vector_factory = _VectorFactory(
+                RandomVectors(hamiltonian, rng=rng), num_vectors=num_vectors,
+                accumulate=True)
+        else:
+            if not isinstance(vector_factory, Iterable):
+                raise TypeError('vector_factory must be iterable')
+            try:
+                len(vector_factory)
+            except TypeError:
+                if num_vectors is None:
+                    raise ValueError('num_vectors must be provided if'
+                                     'vector_factory has no length.')
+            self._vector_factory = _VectorFactory(
+                vector_factory, num_vectors=num_vectors, accumulate=True)
+        # the reference's second SpectralDensity draws its own _v0 from the
+        # same rng argument (kwant/kpm.py:598-599, :201-203)
+        ensure_rng(rng_arg).random_sample(n)
+
+        kernel = kwargs.get('kernel')
+        self.kernel = kernel if kernel is not None else jackson_kernel
+        self._handle = _lib.Handle(_lib.Csr(hamiltonian), self._a, self._b,
+                                   self._precision)
+        self._compute()
+
+    @property
+    def num_vectors(self):
+        return self._vector_factory.num_vectors
+
+    @property
+    def energies(self):
+        return (self._a * _chebyshev_nodes(SAMPLING * self.num_moments)
+                + self._b)
+
+    def _vectors(self):
+        return np.array([np.asarray(self._vector_factory[r], complex)
+                         for r in range(self._vector_factory.num_vectors)])
+
+    def _compute(self):
+        vecs = self._vectors()
+        mu = _lib.correlator_moments(
+            self._handle, self._a2, self._b2, self._op1, self._op2, vecs,
+            self.num_moments, gemm=self._gemm, per_vector=not self.mean)
+        self.moments_matrix = mu
+        self._build_integral_factor()
+
+    def _build_integral_factor(self):
+        """kwant/kpm.py:720-760 on the device."""
+        n_moments = self.num_moments
+        g_kernel = self.kernel(np.ones(n_moments))
+        g_kernel = np.asarray(g_kernel, dtype=float)
+        g_kernel[0] /= 2
+        nodes = (self.energies - self._b) / self._a
+        if self.mean:
+            self._integral_factor = _lib.integral_factor(
+                self.moments_matrix, g_kernel, nodes)
+        else:
+            self._integral_factor = np.array(
+                [_lib.integral_factor(m, g_kernel, nodes)
+                 for m in self.moments_matrix]).T
+
+    def __call__(self, mu=0, temperature=0):
+        """kwant/kpm.py:608-630."""
+        e = self.energies
+        e_rescaled = (e - self._b) / self._a
+        distribution_array = fermi_distribution(e, mu, temperature)
+        integrand = np.divide(distribution_array, (1 - e_rescaled ** 2) ** 2)
+        integrand = np.multiply(integrand, self._integral_factor)
+        integral = simpson(integrand, x=e_rescaled)
+        prefactor = 2 * 4**2 / ((2 * self._a) ** 2)
+        return prefactor * integral
+
+    def add_moments(self, num_moments=None, *, energy_resolution=None):
+        """kwant/kpm.py:637-664 (recomputed on the device with the larger
+        expansion; equal to a direct run with the final num_moments)."""
+        if not ((num_moments is None) ^ (energy_resolution is None)):
+            raise TypeError("either 'num_moments' or 'energy_resolution' "
+                            "must be provided.")
+        if energy_resolution:
+            if energy_resolution <= 0:
+                raise ValueError("'energy_resolution' must be positive")
+            present_resolution = self._a * 1.6 / self.num_moments
+            if present_resolution < energy_resolution:
+                raise ValueError('Energy resolution is already smaller '
+                                 'than the requested resolution')
+            num_moments = math.ceil((1.6 * self._a) / energy_resolution)
+        if (num_moments is None or num_moments <= 0
+                or num_moments != int(num_moments)):
+            raise ValueError("'num_moments' must be a positive integer")
+        self.num_moments += int(num_moments)
+        self._compute()
+
+    def add_vectors(self, num_vectors=None):
+        """kwant/kpm.py:666-683."""
+        self._vector_factory.add_vectors(num_vectors)
+        self._compute()
+
+
+def _velocity(hamiltonian, params, op_type, positions):
+    """kwant/kpm.py:1042-1085: v = H o i (x_col - x_row) for a direction,
+    or the given operator / matrix."""
+    directions = dict(x=0, y=1, z=2)
+    if _is_local_operator(op_type):
+        return op_type
+    if isinstance(op_type, str):
+        direction = directions[op_type]
+        if _is_system(hamiltonian):
+            operator, norbs, norbs = hamiltonian.hamiltonian_submatrix(
+                params=params, sparse=True, return_norb=True)
+            if hasattr(hamiltonian, 'orbital_positions'):
+                positions = hamiltonian.orbital_positions()
+            else:
+                positions = np.vstack([[hamiltonian.pos(i)] * norb
+                                       for i, norb in enumerate(norbs)])
+        elif positions is not None:
+            operator = coo_matrix(hamiltonian, copy=True)
+        positions = np.asarray(positions, dtype=float)
+        operator = coo_matrix(operator)
+        displacements = positions[operator.col] - positions[operator.row]
+        if direction > displacements.shape[1]:
+            raise ValueError("{} is not an allowed direction.".format(op_type))
+        operator.data = operator.data * (1j * displacements[:, direction])
+        return operator.tocsr()
+    try:
+        return csr_matrix(op_type)
+    except Exception:
+        raise ValueError("Velocity operator must be provided as a matrix, "
+                         "a kwant operator, or a direction.")
+
+
+def conductivity(hamiltonian, alpha='x', beta='x', positions=None, **kwargs):
+    """Kubo-Bastin conductivity tensor element (kwant/kpm.py:763-847)."""
+    if positions is None and not _is_system(hamiltonian):
+        raise ValueError("If 'hamiltonian' is a matrix, positions "
+                         "must be provided")
+    params = kwargs.get('params')
+    alpha = _velocity(hamiltonian, params, alpha, positions)
+    beta = _velocity(hamiltonian, params, beta, positions)
+    return Correlator(hamiltonian, operator1=alpha, operator2=beta, **kwargs)

@@ -12,3 +12,8 @@ def pytest_configure(config):
     config.addinivalue_line(
         'markers', 'gpu: needs a CUDA GPU (GB300, sm_103a) and the built '
         'extension library')
+
+
+# the scratch build of the reference (fixture generation) is not part of the
+# suite
+collect_ignore_glob = ['golden/*']

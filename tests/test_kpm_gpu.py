@@ -1,0 +1,306 @@
+"""GPU parity of the KPM path against the reference's golden outputs.
+
+Every case reproduces a reference run (tests/golden/make_golden.py) with the
+same Hamiltonian, the same random-vector stream (rng seed) and the same raw
+spectral bounds, and compares per-vector moments, densities and energies.
+
+Tolerances (relative to the largest magnitude of the reference quantity):
+  precision='fp64'  : 1e-12 (the reference's own TOL, kwant/tests/test_kpm.py:38)
+  precision='mixed' : densities / N within 1e-5 (DOS L-infinity target)
+"""
+
+import numpy as np
+import pytest
+
+from golden_io import load, csr, ref_vectors
+from oracle import kpm_oracle as ko
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+def _rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    assert a.shape == b.shape, (a.shape, b.shape)
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+@pytest.fixture(scope='module')
+def kpm():
+    from kwant_gb300 import _lib, kpm
+    if _lib.device_count() == 0:
+        pytest.fail('no CUDA device: the GPU tests need a GB300')
+    return kpm
+
+
+def _sd(kpm, ham, g, **kw):
+    kw.setdefault('rng', int(g['seed']))
+    return kpm.SpectralDensity(ham, bounds=(g['lmin'], g['lmax']), **kw)
+
+
+# --------------------------------------------------------------- DOS, fp64
+def test_rmt_dos_fp64(kpm):
+    g = load('rmt20')
+    sd = _sd(kpm, g['ham'], g, num_moments=200, num_vectors=5)
+    assert sd._a == g['a'] and sd._b == g['b']
+    assert np.array_equal(sd.energies, g['energies'])
+    assert _rel(np.array(sd._moments_list), g['moments_list']) < TOL
+    assert _rel(sd.densities, g['densities']) < TOL
+    assert _rel(sd._gammas, g['gammas']) < TOL
+
+
+def test_rmt_add_moments_bit_identical(kpm):
+    """kwant/tests/test_kpm.py:481-505: add_moments == fresh run, bit for
+    bit, including odd counts."""
+    g = load('rmt20')
+    sd = _sd(kpm, g['ham'], g, num_moments=200, num_vectors=5)
+    sd.add_moments(200)
+    fresh = _sd(kpm, g['ham'], g, num_moments=400, num_vectors=5)
+    assert np.array_equal(np.array(sd._moments_list),
+                          np.array(fresh._moments_list))
+    assert _rel(np.array(sd._moments_list), g['add_moments_list']) < TOL
+    odd = _sd(kpm, g['ham'], g, num_moments=201, num_vectors=5)
+    assert _rel(np.array(odd._moments_list), g['odd_moments_list']) < TOL
+    even = _sd(kpm, g['ham'], g, num_moments=200, num_vectors=5)
+    even.add_moments(1)
+    assert np.array_equal(np.array(even._moments_list),
+                          np.array(odd._moments_list))
+
+
+def test_rmt_add_vectors_bit_identical(kpm):
+    """kwant/tests/test_kpm.py:526-535."""
+    g = load('rmt20')
+    sd = _sd(kpm, g['ham'], g, num_moments=200, num_vectors=5)
+    sd.add_vectors(3)
+    fresh = _sd(kpm, g['ham'], g, num_moments=200, num_vectors=8)
+    assert np.array_equal(sd.densities, fresh.densities)
+    assert _rel(np.array(sd._moments_list), g['vec_moments_list']) < TOL
+
+
+def test_rmt_operator_identity_matrix(kpm):
+    g = load('rmt20')
+    sd = _sd(kpm, g['ham'], g, num_moments=200, num_vectors=5,
+             operator=np.identity(20))
+    assert _rel(np.array(sd._moments_list), g['op_moments_list']) < TOL
+    assert _rel(sd.densities, g['op_densities']) < TOL
+
+
+def test_rmt_lorentz_mean_false(kpm):
+    g = load('rmt20')
+    sd = _sd(kpm, g['ham'], g, num_moments=64, num_vectors=3,
+             kernel=kpm.lorentz_kernel, mean=False)
+    assert _rel(sd.densities, g['lor_densities']) < TOL
+
+
+def test_rmt_call_and_integrate(kpm):
+    g = load('rmt20')
+    sd = _sd(kpm, g['ham'], g, num_moments=200, num_vectors=5)
+    assert _rel(sd(g['call_energies']), g['call_values']) < TOL
+    assert abs(sd.integrate() - g['integrate']) < 1e-10
+    f = sd.integrate(lambda e: kpm.fermi_distribution(e, 0.1, 0.05))
+    assert abs(f - g['integrate_fermi']) < 1e-10
+
+
+def test_custom_kernel_runs_on_host_values(kpm):
+    g = load('rmt20')
+    sd = _sd(kpm, g['ham'], g, num_moments=200, num_vectors=5,
+             kernel=lambda m: kpm.jackson_kernel(m))
+    assert _rel(sd.densities, g['densities']) < TOL
+
+
+# ------------------------------------------------------ plain-KPM workload
+def test_square100_fp64(kpm):
+    g = load('square100')
+    sd = _sd(kpm, csr(g), g, num_moments=100, num_vectors=10)
+    assert _rel(np.array(sd._moments_list), g['moments_list']) < TOL
+    assert _rel(sd.densities, g['densities']) < TOL
+
+
+def test_square100_mixed_dos_error(kpm):
+    g = load('square100')
+    ham = csr(g)
+    n = ham.shape[0]
+    sd = _sd(kpm, ham, g, num_moments=100, num_vectors=10, precision='mixed')
+    err = np.max(np.abs(sd.densities - g['densities'])) / n
+    assert err < 1e-5, err
+
+
+# --------------------------------------------------------------- operators
+def test_ldos_density_where(kpm):
+    from kwant_gb300.system import LatticeSystem
+    from kwant_gb300.operator import Density
+    g = load('honeycomb_ldos')
+    ham = csr(g)
+    n = ham.shape[0]
+    syst = LatticeSystem(ham, [(0, 1, 0), (n, 0, n)], np.zeros((n, 2)))
+    dens = Density(syst, where=list(g['where']))
+    sd = _sd(kpm, ham, g, operator=dens, num_moments=60, num_vectors=4)
+    assert _rel(np.array(sd._moments_list), g['moments_list']) < TOL
+    assert _rel(sd.densities, g['densities']) < TOL
+    dsum = Density(syst, where=list(g['where']), sum=True)
+    sd = _sd(kpm, ham, g, operator=dsum, num_moments=60, num_vectors=4)
+    assert _rel(sd.densities, g['sum_densities']) < TOL
+    dos = _sd(kpm, ham, g, num_moments=60, num_vectors=4)
+    assert _rel(dos.densities, g['dos_densities']) < TOL
+
+
+def test_current_chain(kpm):
+    from kwant_gb300.system import LatticeSystem
+    from kwant_gb300.operator import Current
+    g = load('chain_current')
+    ham = csr(g)
+    n = ham.shape[0]
+    syst = LatticeSystem(ham, [(0, 1, 0), (n, 0, n)],
+                         np.arange(n, dtype=float)[:, None])
+    cur = Current(syst, where=[tuple(w) for w in g['where']])
+    sd = _sd(kpm, ham, g, operator=cur, num_moments=200, num_vectors=5)
+    assert _rel(np.array(sd._moments_list), g['moments_list']) < TOL
+    assert _rel(sd.densities, g['densities']) < TOL
+
+
+def test_two_orbital_operators(kpm):
+    from kwant_gb300.system import LatticeSystem
+    from kwant_gb300.operator import Density, Current
+    g = load('rashba_ops')
+    ham = csr(g)
+    n = ham.shape[0]
+    syst = LatticeSystem(ham, [(0, 2, 0), (n // 2, 0, n)], g['positions'])
+    sz = np.diag([1.0, -1.0])
+    d_sum = Density(syst, onsite=sz, sum=True)
+    d_loc = Density(syst, onsite=sz, where=list(g['where_sites']))
+    cur = Current(syst, onsite=sz, where=[tuple(w) for w in g['hop_where']])
+    kw = dict(num_moments=40, num_vectors=3)
+    for op, pre in ((d_sum, 'sz_'), (d_loc, 'loc_'), (cur, 'cur_')):
+        sd = _sd(kpm, ham, g, operator=op, **kw)
+        assert _rel(np.array(sd._moments_list), g[pre + 'moments_list']) \
+            < TOL, pre
+        assert _rel(sd.densities, g[pre + 'densities']) < TOL, pre
+    # MAT_ELS and ACT on the device
+    assert _rel(d_loc(g['bra'], g['ket']), g['dens_loc_call']) < TOL
+    assert abs(d_sum(g['bra'], g['ket']) - g['dens_sz_call']) < 1e-10
+    assert abs(d_sum(g['bra']) - g['dens_sz_self']) < 1e-10
+    assert _rel(cur(g['bra'], g['ket']), g['cur_call']) < TOL
+    assert _rel(d_loc.act(g['ket']), g['dens_loc_act']) < TOL
+    assert _rel(cur.act(g['ket']), g['cur_act']) < TOL
+
+
+def test_mixed_operator_moments(kpm):
+    from kwant_gb300.system import LatticeSystem
+    from kwant_gb300.operator import Density
+    g = load('honeycomb_ldos')
+    ham = csr(g)
+    n = ham.shape[0]
+    syst = LatticeSystem(ham, [(0, 1, 0), (n, 0, n)], np.zeros((n, 2)))
+    dens = Density(syst, where=list(g['where']))
+    sd = _sd(kpm, ham, g, operator=dens, num_moments=60, num_vectors=4,
+             precision='mixed')
+    err = np.max(np.abs(sd.densities - g['densities']))
+    assert err < 1e-5 * max(1.0, np.max(np.abs(g['densities']))), err
+
+
+# ------------------------------------------------------------------ bounds
+def test_lanczos_bounds_enclose_spectrum(kpm):
+    g = load('rmt20')
+    ev = np.linalg.eigvalsh(g['ham'])
+    lo, hi = kpm.spectral_bounds(g['ham'], 0.05, method='lanczos')
+    assert lo <= ev[0] + 1e-9 and hi >= ev[-1] - 1e-9
+    assert abs(lo - ev[0]) < 0.025 * abs(ev[0]) + 1e-6
+    g = load('square100')
+    ham = csr(g)
+    lo, hi = kpm.spectral_bounds(ham, 0.05, method='lanczos')
+    # reference ARPACK bounds (tol = eps/2) agree to that tolerance
+    assert abs(lo - g['lmin']) < 0.025 * abs(g['lmin'])
+    assert abs(hi - g['lmax']) < 0.025 * abs(g['lmax'])
+
+
+def test_default_bounds_path(kpm):
+    """bounds=None: device bounds; densities match the reference within
+    the effect of the bound tolerance."""
+    g = load('square100')
+    ham = csr(g)
+    sd = kpm.SpectralDensity(ham, rng=1, num_moments=100, num_vectors=10)
+    assert abs(sd._a - g['a']) < 0.03 * g['a']
+    ev_max = np.max(np.abs(sd.densities))
+    assert ev_max > 0
+
+
+def test_arpack_bounds_reproduce_reference(kpm):
+    g = load('square100')
+    ham = csr(g)
+    sd = kpm.SpectralDensity(ham, rng=1, num_moments=100, num_vectors=10,
+                             bounds_method='arpack')
+    # ARPACK itself runs on the host CPU of the test machine; its floating
+    # point may differ from the machine that made the fixture.
+    assert abs(sd._a - g['a']) < 1e-8 * g['a']
+    assert abs(sd._b - g['b']) < 1e-8
+    assert _rel(sd.densities, g['densities']) < 1e-6
+
+
+# ----------------------------------------------------------- reconstruction
+def test_device_dct_matches_scipy(kpm):
+    from kwant_gb300 import _lib
+    rs = np.random.RandomState(0)
+    for M, W in ((7, 1), (64, 3), (500, 2)):
+        mom = rs.randn(1, M, W) + 1j * rs.randn(1, M, W)
+        nodes = ko.chebyshev_nodes(2 * M)
+        gam, rho = _lib.reconstruct(mom, True, False, 1.0, _lib.KERNEL_NONE,
+                                    4.0, nodes)
+        ref_rho, ref_gam = ko.calc_fft_moments(mom[0])
+        assert _rel(gam, ref_gam) < 1e-12
+        assert _rel(rho, ref_rho) < 1e-12
+
+
+def test_kernel_weights_on_device(kpm):
+    from kwant_gb300 import _lib
+    for M in (2, 10, 1000):
+        g = _lib.kernel_weights(M, _lib.KERNEL_JACKSON)
+        assert _rel(g, ko.jackson_kernel(np.ones(M))) < 1e-13
+        g = _lib.kernel_weights(M, _lib.KERNEL_LORENTZ, 4.0)
+        assert _rel(g, ko.lorentz_kernel(np.ones(M))) < 1e-13
+
+
+# ------------------------------------------------------------ conductivity
+def test_conductivity_fp64(kpm):
+    g = load('conductivity')
+    ham = csr(g)
+    pos = g['orb_positions']
+    kw = dict(rng=0, num_moments=48, num_vectors=4,
+              bounds=(g['lmin'], g['lmax']))
+    cond = kpm.conductivity(ham, alpha='x', beta='y', positions=pos, **kw)
+    assert cond._a == g['a'] and cond._b == g['b']
+    assert _rel(cond.moments_matrix, g['mu_xy']) < 1e-11
+    assert _rel(cond._integral_factor, g['factor_xy']) < 1e-10
+    vals = np.array([[cond(mu=m, temperature=T) for m in g['mus']]
+                     for T in g['temps']])
+    assert _rel(vals, g['values_xy']) < 1e-9
+    cxx = kpm.conductivity(ham, alpha='x', beta='x', positions=pos, **kw)
+    vals = np.array([[cxx(mu=m, temperature=T) for m in g['mus']]
+                     for T in g['temps']])
+    assert _rel(vals, g['values_xx']) < 1e-9
+    cond.add_moments(16)
+    vals = np.array([cond(mu=m, temperature=0.1) for m in g['mus']])
+    assert _rel(vals, g['values_add']) < 1e-9
+
+
+def test_conductivity_mixed_bf16x3(kpm):
+    g = load('conductivity')
+    ham = csr(g)
+    pos = g['orb_positions']
+    kw = dict(rng=0, num_moments=48, num_vectors=4,
+              bounds=(g['lmin'], g['lmax']))
+    cond = kpm.conductivity(ham, alpha='x', beta='y', positions=pos,
+                            precision='mixed', gemm='bf16x3', **kw)
+    assert _rel(cond.moments_matrix, g['mu_xy']) < 1e-4
+    vals = np.array([[cond(mu=m, temperature=T) for m in g['mus']]
+                     for T in g['temps']])
+    err = np.max(np.abs(vals - g['values_xy']))
+    assert err < 1e-3 * max(1.0, np.max(np.abs(g['values_xy']))), err
+
+
+# ------------------------------------------------------------- determinism
+def test_repeatable(kpm):
+    g = load('square100')
+    a = _sd(kpm, csr(g), g, num_moments=50, num_vectors=10, precision='mixed')
+    b = _sd(kpm, csr(g), g, num_moments=50, num_vectors=10, precision='mixed')
+    assert np.array_equal(a.densities, b.densities)
