@@ -248,7 +248,8 @@ def run_ours(args):
     a, b = kpm._rescale_ab(lo, hi, 0.05)
     prec = _lib.PREC_MIXED if args.precision == 'mixed' else _lib.PREC_FP64
     csr = _lib.Csr(ham)
-    handle = _lib.Handle(csr, a, b, prec)
+    handle = _lib.Handle(csr, a, b, prec,
+                         reorder=args.reorder and args.precision == 'mixed')
     block = _lib.Block(handle, vecs, keep_a0=True)
     stream = torch.cuda.ExternalStream(handle.stream())
     setup_s = time.perf_counter() - t_setup
@@ -312,21 +313,40 @@ def run_ours(args):
         mom64 = None
         if prec == _lib.PREC_MIXED:
             h64 = _lib.Handle(csr, a, b, _lib.PREC_FP64)
-            b64 = _lib.Block(h64, vecs, keep_a0=False)
+            b64 = _lib.Block(h64, vecs, keep_a0=True)
+            s64 = torch.cuda.ExternalStream(h64.stream())
+            f0 = torch.cuda.Event(enable_timing=True)
+            f1 = torch.cuda.Event(enable_timing=True)
+            f0.record(s64)
             mom64 = b64.dos_moments(0, M)
+            f1.record(s64)
+            torch.cuda.synchronize()
+            fp64_ms = f0.elapsed_time(f1)
             b64.close()
             h64.close()
+
             def dens(mm):
                 return _lib.reconstruct(mm[:, :, None], True, False, a,
-                                        _lib.KERNEL_JACKSON, 4.0, nodes)[1][:, 0]
+                                        _lib.KERNEL_JACKSON, 4.0,
+                                        nodes)[1][:, 0]
             d32, d64 = dens(mom), dens(mom64)
+            diff = np.abs(d32 - d64) / n
+            # nodes inside the spectral bounds (the eps margin excluded):
+            # there the DOS is nonzero; outside it the 1/sqrt(1 - x^2)
+            # weight of the reconstruction amplifies rounding near zero DOS
+            inside = np.abs(nodes) <= 1 - 0.05 / 2
             accuracy = {
-                'dos_linf_per_orbital_vs_fp64': float(
-                    np.max(np.abs(d32 - d64)) / n),
+                'dos_linf_per_orbital_vs_fp64': float(np.max(diff)),
+                'dos_linf_per_orbital_vs_fp64_inside_bounds':
+                    float(np.max(diff[inside])),
                 'dos_linf_rel_vs_fp64': float(
                     np.max(np.abs(d32 - d64)) / np.max(np.abs(d64))),
+                'argmax_node_x': float(nodes[int(np.argmax(diff))]),
                 'reference': 'FP64 GPU path (parity-tested against the '
-                             'reference fixtures at 1e-12)'}
+                             'reference fixtures at 1e-12)',
+                'fp64_gpu_value': nnz * R * M / (fp64_ms / 1e3),
+                'fp64_gpu_ms_per_step': fp64_ms,
+                'mixed_over_fp64_moment_steps': fp64_ms / ms_per_step}
 
     # ---- e2e through the C ABI one-shot call (host buffers) ----------------
     e2e = None
@@ -448,6 +468,7 @@ def main():
     p.add_argument('--no-e2e', dest='e2e', action='store_false')
     p.add_argument('--no-cpu', dest='cpu', action='store_false')
     p.add_argument('--no-accuracy', dest='accuracy', action='store_false')
+    p.add_argument('--no-reorder', dest='reorder', action='store_false')
     args = p.parse_args()
     if args.warmup < 3 and args.impl == 'ours':
         print('warning: fewer than 3 warm-up steps', file=sys.stderr)

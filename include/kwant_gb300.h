@@ -107,6 +107,15 @@ KPM_API int kpm_device_count(int* count);
  * the spectral bounds (kwant/kpm.py:1174-1175). */
 KPM_API int kpm_create(const kpm_csr_desc* ham, double a, double b, int precision,
                        kpm_handle** out);
+/* kpm_create with flags.  KPM_FLAG_REORDER: store the Hamiltonian in a
+ * reverse Cuthill-McKee order of its sparsity pattern (computed on the
+ * host), so that the neighbours of a row are close in memory and stay in L2
+ * during a step.  Vectors, operators and results are permuted on the device
+ * transparently; moments are invariant under the reordering.  No reference
+ * counterpart (the reference multiplies in the given order). */
+#define KPM_FLAG_REORDER 1
+KPM_API int kpm_create_ex(const kpm_csr_desc* ham, double a, double b,
+                          int precision, int flags, kpm_handle** out);
 /* Use an external CUDA stream (cudaStream_t) for all work of the handle. */
 KPM_API int kpm_set_stream(kpm_handle* h, void* stream);
 KPM_API int kpm_get_stream(kpm_handle* h, void** stream);
@@ -152,7 +161,8 @@ KPM_API int kpm_op_apply(kpm_op* op, const double* bra, const double* ket,
 /* One-shot DOS (the C-ABI form of SpectralDensity with operator=None and
  * explicit bounds): uploads ham and vecs, runs the recursion, reduces the
  * moments (mean over vectors, /a, kernel) and reconstructs the density at
- * the 2M Chebyshev nodes on the device.  moments_out: R x M complex128 (may
+ * the 2M Chebyshev nodes on the device.  KPM_PREC_MIXED uses
+ * KPM_FLAG_REORDER.  moments_out: R x M complex128 (may
  * be NULL); gammas_out / densities_out: 2M complex128 (may be NULL). */
 KPM_API int kpm_dos(const kpm_csr_desc* ham, double a, double b, int precision,
                     const double* vecs, int64_t R, int64_t M, int kernel,

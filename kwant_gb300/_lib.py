@@ -27,6 +27,7 @@ PREC_MIXED = 1
 KERNEL_NONE = 0
 KERNEL_JACKSON = 1
 KERNEL_LORENTZ = 2
+FLAG_REORDER = 1
 
 
 class KPMError(RuntimeError):
@@ -78,6 +79,7 @@ def _load():
         'kpm_last_error': [C.c_char_p, C.c_size_t],
         'kpm_device_count': [P],
         'kpm_create': [P, D, D, I, P],
+        'kpm_create_ex': [P, D, D, I, I, P],
         'kpm_set_stream': [P, P],
         'kpm_get_stream': [P, P],
         'kpm_synchronize': [P],
@@ -179,15 +181,16 @@ def c128(a):
 class Handle:
     """A Hamiltonian resident on the device with its rescaling (a, b)."""
 
-    def __init__(self, csr, a, b, precision):
+    def __init__(self, csr, a, b, precision, reorder=False):
         if not isinstance(csr, Csr):
             csr = Csr(csr)
         self.csr = csr
         self.a, self.b, self.precision = float(a), float(b), precision
         self.N = csr.shape[0]
+        self.reorder = bool(reorder)
         h = C.c_void_p()
-        check(lib.kpm_create(csr.ref(), self.a, self.b, precision,
-                             C.byref(h)))
+        check(lib.kpm_create_ex(csr.ref(), self.a, self.b, precision,
+                                FLAG_REORDER if reorder else 0, C.byref(h)))
         self._h = h
 
     @property

@@ -99,6 +99,9 @@ struct kpm_handle {
   int resident_step_blocks = 0;
   cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
   bool timed = false;
+  // optional locality reordering: device row p holds original row perm[p]
+  int32_t* perm = nullptr;            // device, new -> old (null: identity)
+  std::vector<int32_t> h_iperm;       // host, old -> new
   // per-launch profiling of step kernels (pairs of events)
   bool profiling = false;
   std::vector<cudaEvent_t> prof_events;

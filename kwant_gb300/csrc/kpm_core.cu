@@ -97,11 +97,10 @@ __global__ void scale_to_c64_kernel(const double2* __restrict__ in,
     out[i] = make_float2((float)(in[i].x * scale), (float)(in[i].y * scale));
 }
 
-int upload_matrix(kpm_handle* h, const kpm_csr_desc* m, double scale,
-                  Matrix* out) {
+// Validate a CSR on the host so that no kernel ever indexes out of bounds.
+int validate_csr(const kpm_csr_desc* m) {
   KPM_REQUIRE(m->rows > 0 && m->nnz >= 0 && m->indptr && m->indices,
               "invalid CSR descriptor");
-  // Validate on the host so that no kernel ever indexes out of bounds.
   KPM_REQUIRE(m->indptr[0] == 0 && m->indptr[m->rows] == m->nnz,
               "CSR indptr must start at 0 and end at nnz");
   for (int64_t i = 0; i < m->rows; ++i)
@@ -110,6 +109,12 @@ int upload_matrix(kpm_handle* h, const kpm_csr_desc* m, double scale,
   for (int64_t k = 0; k < m->nnz; ++k)
     KPM_REQUIRE(m->indices[k] >= 0 && m->indices[k] < m->rows,
                 "CSR column index out of range at entry %lld", (long long)k);
+  return KPM_OK;
+}
+
+int upload_matrix(kpm_handle* h, const kpm_csr_desc* m, double scale,
+                  Matrix* out) {
+  KPM_TRY(validate_csr(m));
   out->rows = m->rows;
   out->nnz = m->nnz;
   KPM_TRY(dev_alloc((void**)&out->indptr, (m->rows + 1) * sizeof(int32_t),
@@ -166,14 +171,15 @@ void free_matrix(Matrix* m, cudaStream_t s) {
 template <typename OutT>
 __global__ void to_interleaved_kernel(const double2* __restrict__ in,
                                       OutT* __restrict__ out, int64_t N,
-                                      int64_t R, int64_t Rpad) {
+                                      int64_t R, int64_t Rpad,
+                                      const int32_t* __restrict__ perm) {
   __shared__ double2 tile[32][33];
   const int64_t n0 = (int64_t)blockIdx.x * 32;
   const int64_t r0 = (int64_t)blockIdx.y * 32;
   for (int k = threadIdx.y; k < 32; k += blockDim.y) {
     int64_t r = r0 + k, n = n0 + threadIdx.x;
     double2 v = make_double2(0.0, 0.0);
-    if (r < R && n < N) v = in[r * N + n];
+    if (r < R && n < N) v = in[r * N + (perm ? perm[n] : n)];
     tile[k][threadIdx.x] = v;
   }
   __syncthreads();
@@ -195,7 +201,8 @@ __global__ void to_interleaved_kernel(const double2* __restrict__ in,
 template <typename InT>
 __global__ void from_interleaved_kernel(const InT* __restrict__ in,
                                         double2* __restrict__ out, int64_t N,
-                                        int64_t R, int64_t Rpad) {
+                                        int64_t R, int64_t Rpad,
+                                        const int32_t* __restrict__ perm) {
   __shared__ double2 tile[32][33];
   const int64_t n0 = (int64_t)blockIdx.x * 32;
   const int64_t r0 = (int64_t)blockIdx.y * 32;
@@ -215,7 +222,7 @@ __global__ void from_interleaved_kernel(const InT* __restrict__ in,
   __syncthreads();
   for (int k = threadIdx.y; k < 32; k += blockDim.y) {
     int64_t r = r0 + k, n = n0 + threadIdx.x;
-    if (r < R && n < N) out[r * N + n] = tile[threadIdx.x][k];
+    if (r < R && n < N) out[r * N + (perm ? perm[n] : n)] = tile[threadIdx.x][k];
   }
 }
 
@@ -233,10 +240,10 @@ int upload_vectors(kpm_handle* h, const double* host, int64_t R, int64_t N,
   dim3 blk(32, 8), grd((unsigned)ceil_div(N, 32), (unsigned)ceil_div(Rpad, 32));
   if (h->precision == KPM_PREC_MIXED)
     to_interleaved_kernel<float2><<<grd, blk, 0, h->stream>>>(
-        (const double2*)staging, (float2*)dst, N, R, Rpad);
+        (const double2*)staging, (float2*)dst, N, R, Rpad, h->perm);
   else
     to_interleaved_kernel<double2><<<grd, blk, 0, h->stream>>>(
-        (const double2*)staging, (double2*)dst, N, R, Rpad);
+        (const double2*)staging, (double2*)dst, N, R, Rpad, h->perm);
   count_launch(1);
   e = cudaGetLastError();
   dev_free(staging, h->stream);
@@ -252,10 +259,10 @@ int download_vectors(kpm_handle* h, const void* src, int64_t R, int64_t N,
   dim3 blk(32, 8), grd((unsigned)ceil_div(N, 32), (unsigned)ceil_div(Rpad, 32));
   if (h->precision == KPM_PREC_MIXED)
     from_interleaved_kernel<float2><<<grd, blk, 0, h->stream>>>(
-        (const float2*)src, (double2*)staging, N, R, Rpad);
+        (const float2*)src, (double2*)staging, N, R, Rpad, h->perm);
   else
     from_interleaved_kernel<double2><<<grd, blk, 0, h->stream>>>(
-        (const double2*)src, (double2*)staging, N, R, Rpad);
+        (const double2*)src, (double2*)staging, N, R, Rpad, h->perm);
   count_launch(1);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess)
@@ -302,7 +309,9 @@ cheb_step_kernel(StepArgs p) {
   constexpr int G = T::G;
   const int lane = threadIdx.x & (LANES - 1);
   const int slot = threadIdx.x / LANES;
-  __shared__ double red[DOTS ? SLOTS : 1][DOTS ? G * 3 : 1];
+  // per-slot dot-product partials (DOS dots, or the norm of the odd tail)
+  constexpr bool RED = DOTS || MODE == STEP_NORM;
+  __shared__ double red[RED ? SLOTS : 1][RED ? G * 3 : 1];
 
   const PT* __restrict__ x = reinterpret_cast<const PT*>(p.x);
   const PT* prev = reinterpret_cast<const PT*>(p.prev);
@@ -318,17 +327,35 @@ cheb_step_kernel(StepArgs p) {
     const int g = (int)(w - (int64_t)xi * p.groups);
     const int64_t col = (int64_t)g * LANES + lane;
     double nrm[VPL], cre[VPL], cim[VPL];
+    // complex64 path: FP32 partials over at most FLUSH rows, then added to
+    // the FP64 accumulators.  GB300's FP64 pipe is narrow; per-row FP64 dot
+    // products would bound the kernel.
+    float fn[VPL], fcr[VPL], fci[VPL];
+    int pending = 0;
+    constexpr int FLUSH = 32;
 #pragma unroll
-    for (int k = 0; k < VPL; ++k) nrm[k] = cre[k] = cim[k] = 0.0;
+    for (int k = 0; k < VPL; ++k) {
+      nrm[k] = cre[k] = cim[k] = 0.0;
+      fn[k] = fcr[k] = fci[k] = 0.f;
+    }
+    auto flush = [&]() {
+#pragma unroll
+      for (int k = 0; k < VPL; ++k) {
+        nrm[k] += (double)fn[k];
+        cre[k] += (double)fcr[k];
+        cim[k] += (double)fci[k];
+        fn[k] = fcr[k] = fci[k] = 0.f;
+      }
+      pending = 0;
+    };
 
     for (int64_t i = (int64_t)xi * SLOTS + slot; i < p.rows; i += stride) {
       const PT xv = x[i * p.rp + col];
       if constexpr (MODE == STEP_NORM) {
         if constexpr (MIXED) {
-          nrm[0] = fma((double)xv.x, (double)xv.x,
-                       fma((double)xv.y, (double)xv.y, nrm[0]));
-          nrm[1] = fma((double)xv.z, (double)xv.z,
-                       fma((double)xv.w, (double)xv.w, nrm[1]));
+          fn[0] = fmaf(xv.x, xv.x, fmaf(xv.y, xv.y, fn[0]));
+          fn[1] = fmaf(xv.z, xv.z, fmaf(xv.w, xv.w, fn[1]));
+          if (++pending == FLUSH) flush();
         } else {
           nrm[0] = fma(xv.x, xv.x, fma(xv.y, xv.y, nrm[0]));
         }
@@ -420,14 +447,13 @@ cheb_step_kernel(StepArgs p) {
       if constexpr (DOTS) {
         // <x|x> and <o|x> = sum conj(o) x
         if constexpr (MIXED) {
-          double xr0 = xv.x, xi0 = xv.y, xr1 = xv.z, xi1 = xv.w;
-          double or0 = o.x, oi0 = o.y, or1 = o.z, oi1 = o.w;
-          nrm[0] = fma(xr0, xr0, fma(xi0, xi0, nrm[0]));
-          nrm[1] = fma(xr1, xr1, fma(xi1, xi1, nrm[1]));
-          cre[0] = fma(or0, xr0, fma(oi0, xi0, cre[0]));
-          cre[1] = fma(or1, xr1, fma(oi1, xi1, cre[1]));
-          cim[0] = fma(or0, xi0, fma(-oi0, xr0, cim[0]));
-          cim[1] = fma(or1, xi1, fma(-oi1, xr1, cim[1]));
+          fn[0] = fmaf(xv.x, xv.x, fmaf(xv.y, xv.y, fn[0]));
+          fn[1] = fmaf(xv.z, xv.z, fmaf(xv.w, xv.w, fn[1]));
+          fcr[0] = fmaf(o.x, xv.x, fmaf(o.y, xv.y, fcr[0]));
+          fcr[1] = fmaf(o.z, xv.z, fmaf(o.w, xv.w, fcr[1]));
+          fci[0] = fmaf(o.x, xv.y, fmaf(-o.y, xv.x, fci[0]));
+          fci[1] = fmaf(o.z, xv.w, fmaf(-o.w, xv.z, fci[1]));
+          if (++pending == FLUSH) flush();
         } else {
           nrm[0] = fma(xv.x, xv.x, fma(xv.y, xv.y, nrm[0]));
           cre[0] = fma(o.x, xv.x, fma(o.y, xv.y, cre[0]));
@@ -435,7 +461,8 @@ cheb_step_kernel(StepArgs p) {
         }
       }
     }
-    if constexpr (DOTS || MODE == STEP_NORM) {
+    if constexpr (RED) {
+      if constexpr (MIXED) flush();
 #pragma unroll
       for (int k = 0; k < VPL; ++k) {
         red[slot][(lane * VPL + k) * 3 + 0] = nrm[k];
@@ -714,6 +741,11 @@ int kpm_launch_count(int64_t* count) {
 
 int kpm_create(const kpm_csr_desc* ham, double a, double b, int precision,
                kpm_handle** out) {
+  return kpm_create_ex(ham, a, b, precision, 0, out);
+}
+
+int kpm_create_ex(const kpm_csr_desc* ham, double a, double b, int precision,
+                  int flags, kpm_handle** out) {
   KPM_REQUIRE(ham && out, "kpm_create: null argument");
   KPM_REQUIRE(ham->rows > 0 && ham->nnz >= 0 && ham->indptr && ham->indices &&
                   (ham->nnz == 0 || ham->data),
@@ -742,8 +774,17 @@ int kpm_create(const kpm_csr_desc* ham, double a, double b, int precision,
     return KPM_ECUDA;
   }
   h->own_stream = true;
-  st = upload_matrix(h, ham, h->precision == KPM_PREC_MIXED ? 2.0 / a : 0.0,
-                     &h->H);
+  const double scale = h->precision == KPM_PREC_MIXED ? 2.0 / a : 0.0;
+  if (flags & KPM_FLAG_REORDER) {
+    st = validate_csr(ham);
+    std::vector<int32_t> ip, ix;
+    std::vector<double> data;
+    if (st == KPM_OK) st = setup_reorder(h, ham, ip, ix, data);
+    kpm_csr_desc pd{ham->rows, ham->nnz, ip.data(), ix.data(), data.data()};
+    if (st == KPM_OK) st = upload_matrix(h, &pd, scale, &h->H);
+  } else {
+    st = upload_matrix(h, ham, scale, &h->H);
+  }
   if (st != KPM_OK) {
     kpm_destroy(h);
     return st;
@@ -777,6 +818,7 @@ int kpm_destroy(kpm_handle* h) {
   if (!h) return KPM_OK;
   free_matrix(&h->H, h->stream);
   dev_free(h->partials, h->stream);
+  dev_free(h->perm, h->stream);
   if (h->ev_start) cudaEventDestroy(h->ev_start);
   if (h->ev_stop) cudaEventDestroy(h->ev_stop);
   for (cudaEvent_t e : h->prof_events) cudaEventDestroy(e);

@@ -201,8 +201,8 @@ int kpm_correlator_moments(kpm_handle* h, double a2, double b2,
   Matrix Va, Vb;
   kpm_block *bR = nullptr, *bL = nullptr;
   Store psi, omega;
-  int st = upload_matrix(h, v_alpha, 0.0, &Va);
-  if (st == KPM_OK) st = upload_matrix(h, v_beta, 0.0, &Vb);
+  int st = upload_matrix_for(h, v_alpha, 0.0, &Va);
+  if (st == KPM_OK) st = upload_matrix_for(h, v_beta, 0.0, &Vb);
   const int kind = gemm == 1 ? STORE_BF16X3 : STORE_C128;
   if (st == KPM_OK) st = store_alloc(&psi, kind, M, K, s);
   if (st == KPM_OK) st = store_alloc(&omega, kind, M, K, s);

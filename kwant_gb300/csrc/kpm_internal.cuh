@@ -28,11 +28,21 @@ int dev_alloc(void** p, size_t bytes, cudaStream_t s);
 void dev_free(void* p, cudaStream_t s);
 int init_device(int* device, int* num_sms);
 
+int validate_csr(const kpm_csr_desc* m);
 // CSR upload.  scale == 0 keeps complex128 values; otherwise values are
 // stored as complex64 multiplied by scale.
 int upload_matrix(kpm_handle* h, const kpm_csr_desc* m, double scale,
                   Matrix* out);
 void free_matrix(Matrix* m, cudaStream_t s);
+// upload_matrix in the handle's row order (reordered handles permute rows
+// and columns)
+int upload_matrix_for(kpm_handle* h, const kpm_csr_desc* m, double scale,
+                      Matrix* out);
+// compute the RCM order of m, set h->perm / h->h_iperm, and return the
+// permuted CSR arrays
+int setup_reorder(kpm_handle* h, const kpm_csr_desc* m,
+                  std::vector<int32_t>& ip, std::vector<int32_t>& ix,
+                  std::vector<double>& data);
 
 int upload_vectors(kpm_handle* h, const double* host, int64_t R, int64_t N,
                    int64_t Rpad, void* dst);

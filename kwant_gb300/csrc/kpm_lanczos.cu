@@ -319,8 +319,9 @@ int kpm_bounds(const kpm_csr_desc* ham, const double* v0, double tol,
 
 int kpm_handle_matvec(kpm_handle* h, const double* x, double* y) {
   KPM_REQUIRE(h && x && y, "kpm_handle_matvec: null argument");
-  if (h->precision != KPM_PREC_FP64) {
-    set_error("kpm_handle_matvec: needs a KPM_PREC_FP64 handle");
+  if (h->precision != KPM_PREC_FP64 || h->perm) {
+    set_error("kpm_handle_matvec: needs a KPM_PREC_FP64 handle without "
+              "reordering");
     return KPM_EUNSUPPORTED;
   }
   const int64_t N = h->H.rows;

@@ -250,9 +250,21 @@ int kpm_op_create(kpm_handle* h, const kpm_op_desc* d, kpm_op** out) {
       }
     }
   };
-  up((void**)&op->term_row, d->term_row, T * sizeof(int32_t));
+  // reordered handles: map orbital indices to the device row order
+  std::vector<int32_t> rows_m, cols_m;
+  const int32_t* trow = d->term_row;
+  const int32_t* bcol = d->bra_col;
+  if (h->perm) {
+    rows_m.resize(T);
+    cols_m.resize(E);
+    for (int64_t t = 0; t < T; ++t) rows_m[t] = h->h_iperm[d->term_row[t]];
+    for (int64_t e = 0; e < E; ++e) cols_m[e] = h->h_iperm[d->bra_col[e]];
+    trow = rows_m.data();
+    bcol = cols_m.data();
+  }
+  up((void**)&op->term_row, trow, T * sizeof(int32_t));
   up((void**)&op->bra_ptr, d->bra_ptr, T ? (T + 1) * sizeof(int64_t) : 0);
-  up((void**)&op->bra_col, d->bra_col, E * sizeof(int32_t));
+  up((void**)&op->bra_col, bcol, E * sizeof(int32_t));
   up((void**)&op->bra_val, d->bra_val, E * sizeof(double2));
   up((void**)&op->chunk_ptr, d->chunk_ptr, C ? (C + 1) * sizeof(int64_t) : 0);
   up((void**)&op->out_chunk_ptr, ocp.data(), (W + 1) * sizeof(int64_t));

@@ -347,7 +347,10 @@ int kpm_dos(const kpm_csr_desc* ham, double a, double b, int precision,
             double* moments_out, double* gammas_out, double* densities_out) {
   KPM_REQUIRE(ham && vecs && R > 0 && M >= 2, "kpm_dos: invalid argument");
   kpm_handle* h = nullptr;
-  KPM_TRY(kpm_create(ham, a, b, precision, &h));
+  // the mixed-precision one-shot path stores the Hamiltonian in RCM order
+  KPM_TRY(kpm_create_ex(ham, a, b, precision,
+                        precision == KPM_PREC_MIXED ? KPM_FLAG_REORDER : 0,
+                        &h));
   kpm_block* blk = nullptr;
   int st = kpm_block_create(h, vecs, R, 0, &blk);
   double* mom = nullptr;

@@ -97,6 +97,12 @@ def _precision(precision):
                          % sorted(_PRECISIONS)) from None
 
 
+def _reorder_default(reorder, precision):
+    if reorder is None:
+        return precision == _lib.PREC_MIXED
+    return bool(reorder)
+
+
 def _chebyshev_nodes(n_sampling):
     """kwant/kpm.py:1190-1194."""
     raw, step = np.linspace(np.pi, 0, n_sampling, endpoint=False,
@@ -332,13 +338,17 @@ class SpectralDensity:
     -----------------------------
     precision : 'fp64' (default) or 'mixed'
     bounds_method : 'lanczos' (default) or 'arpack'
+    reorder : bool, optional
+        Store the Hamiltonian in a bandwidth-reducing (RCM) order on the
+        device; default: on for 'mixed', off for 'fp64'.  Results are
+        invariant up to rounding.
     """
 
     def __init__(self, hamiltonian, params=None, operator=None,
                  num_vectors=10, num_moments=None, energy_resolution=None,
                  vector_factory=None, bounds=None, eps=0.05, rng=None,
                  kernel=None, mean=True, accumulate_vectors=True, *,
-                 precision='fp64', bounds_method='lanczos'):
+                 precision='fp64', bounds_method='lanczos', reorder=None):
 
         if num_moments and energy_resolution:
             raise TypeError("either 'num_moments' or 'energy_resolution' "
@@ -424,7 +434,9 @@ class SpectralDensity:
         num_vectors = self._vector_factory.num_vectors
 
         self._handle = _lib.Handle(_lib.Csr(hamiltonian), self._a, self._b,
-                                   self._precision)
+                                   self._precision,
+                                   reorder=_reorder_default(reorder,
+                                                            self._precision))
         self._op = None if self._lowered is None else \
             _lib.Op(self._handle, self._lowered)
         self._batches = []
@@ -657,6 +669,7 @@ class Correlator:
         precision = kwargs.pop('precision', 'fp64')
         bounds_method = kwargs.pop('bounds_method', 'lanczos')
         gemm = kwargs.pop('gemm', 'auto')
+        reorder = kwargs.pop('reorder', None)
         self._gemm = {'auto': 2, 'fp64': 0, 'bf16x3': 1,
                       'bf16x3-simt': 3}[gemm]
         self._precision = _precision(precision)
@@ -730,7 +743,9 @@ class Correlator:
         kernel = kwargs.get('kernel')
         self.kernel = kernel if kernel is not None else jackson_kernel
         self._handle = _lib.Handle(_lib.Csr(hamiltonian), self._a, self._b,
-                                   self._precision)
+                                   self._precision,
+                                   reorder=_reorder_default(reorder,
+                                                            self._precision))
         self._compute()
 
     @property

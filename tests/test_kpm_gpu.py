@@ -298,6 +298,50 @@ def test_conductivity_mixed_bf16x3(kpm):
     assert err < 1e-3 * max(1.0, np.max(np.abs(g['values_xy']))), err
 
 
+# --------------------------------------------------------------- reordering
+def test_reordered_handle_parity(kpm):
+    """KPM_FLAG_REORDER (RCM storage order) leaves results within rounding
+    and keeps the add_vectors bit-identity."""
+    from kwant_gb300.system import LatticeSystem
+    from kwant_gb300.operator import Density
+    g = load('square100')
+    sd = _sd(kpm, csr(g), g, num_moments=100, num_vectors=10, reorder=True)
+    assert _rel(np.array(sd._moments_list), g['moments_list']) < TOL
+    assert _rel(sd.densities, g['densities']) < TOL
+    g = load('honeycomb_ldos')
+    ham = csr(g)
+    n = ham.shape[0]
+    syst = LatticeSystem(ham, [(0, 1, 0), (n, 0, n)], np.zeros((n, 2)))
+    dens = Density(syst, where=list(g['where']))
+    sd = _sd(kpm, ham, g, operator=dens, num_moments=60, num_vectors=4,
+             reorder=True)
+    assert _rel(sd.densities, g['densities']) < TOL
+    g = load('rmt20')
+    sd = _sd(kpm, g['ham'], g, num_moments=200, num_vectors=5, reorder=True)
+    sd.add_vectors(3)
+    fresh = _sd(kpm, g['ham'], g, num_moments=200, num_vectors=8,
+                reorder=True)
+    assert np.array_equal(sd.densities, fresh.densities)
+    assert _rel(np.array(sd._moments_list), g['vec_moments_list']) < TOL
+    c = load('conductivity')
+    cond = kpm.conductivity(csr(c), alpha='x', beta='y',
+                            positions=c['orb_positions'], rng=0,
+                            num_moments=48, num_vectors=4,
+                            bounds=(c['lmin'], c['lmax']), reorder=True)
+    assert _rel(cond.moments_matrix, c['mu_xy']) < 1e-11
+
+
+def test_state_download_matches_oracle(kpm):
+    """_last_two_alphas (device state) equals the oracle's recursion."""
+    g = load('rmt20')
+    sd = _sd(kpm, g['ham'], g, num_moments=10, num_vectors=2, reorder=True)
+    _, vecs = ref_vectors(g['seed'], 20, 2)
+    a, b = ko.rescale_ab(g['lmin'], g['lmax'], 0.05)
+    for r, (prev, cur) in enumerate(sd._last_two_alphas):
+        _, (p_ref, c_ref) = ko.moments_dos(g['ham'], a, b, vecs[r], 10)
+        assert _rel(prev, p_ref) < 1e-13 and _rel(cur, c_ref) < 1e-13
+
+
 # ------------------------------------------------------------- determinism
 def test_repeatable(kpm):
     g = load('square100')
