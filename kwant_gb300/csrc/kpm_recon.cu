@@ -115,7 +115,9 @@ __global__ void dct3_kernel(const double2* __restrict__ x,
   if (gammas) gammas[idx] = make_double2(yr, yi);
   if (rho) {
     const double e = nodes[j];
-    const double gk = M_PI * sqrt(1.0 - e * e);
+    // numpy: pi * sqrt(1 - e**2), each operation rounded (no FMA: near
+    // |e| = 1 the contraction would change 1 - e^2 in its leading digits)
+    const double gk = __dmul_rn(M_PI, sqrt(__dsub_rn(1.0, __dmul_rn(e, e))));
     if (is_real) {
       rho[idx] = make_double2(yr / gk, 0.0);
     } else {
