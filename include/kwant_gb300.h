@@ -168,6 +168,49 @@ KPM_API int kpm_dos(const kpm_csr_desc* ham, double a, double b, int precision,
                     const double* vecs, int64_t R, int64_t M, int kernel,
                     double* moments_out, double* gammas_out, double* densities_out);
 
+/* ---- DOS moments without allocation ----------------------------------------
+ * No counterpart in the reference.  For callers that cannot let this library
+ * allocate device memory -- an application or framework that owns all device
+ * memory through its own arena and passes its libraries preallocated buffers,
+ * or a service with a fixed, audited device-memory budget -- this runs the
+ * same DOS recursion as kpm_block_dos_moments with nothing allocated: no
+ * cudaMalloc/cudaFree, no library allocator, no stream or event creation.
+ * Apart from the caller's buffers it uses one file-scope device array of
+ * KPM_NOALLOC_SCRATCH_BYTES (held by every device that loads the library
+ * until the process exits) for the dot-product partials.
+ *
+ * All pointers are device pointers on the current device:
+ *   ham->indptr/indices: int32 CSR of the Hamiltonian (must be valid: it is
+ *     not checked on the device); ham->data: complex128 H (KPM_PREC_FP64) or
+ *     complex64 values 2H/a (KPM_PREC_MIXED);
+ *   vecs: the R starting vectors in the device layout [N][Rpad] (row-major,
+ *     vectors fastest), complex128 (FP64) or complex64 (MIXED), Rpad = R
+ *     rounded up to 16 (FP64) or 32 (MIXED), padding vectors zero; only read;
+ *   work: 2 * N * Rpad complex elements of the same type; on return it holds
+ *     the last two Chebyshev vectors;
+ *   moments: M * Rpad complex128, written as [moment][vector].
+ * Work is enqueued on `stream` (a cudaStream_t; NULL = default stream) and
+ * the call returns without waiting: results are valid once the stream has
+ * completed.  The first call on a device looks up the scratch array's device
+ * address (cudaGetSymbolAddress, with that device current) and caches it;
+ * make that first call before any stream capture.  Calls whose GPU work
+ * overlaps in time share the scratch array and race; the array keeps the
+ * last call's contents, and every call writes what it reads.  Sizes whose
+ * scratch would exceed KPM_NOALLOC_SCRATCH_BYTES (more than about 160
+ * vectors at the largest row-partition count) are rejected with KPM_EINVAL. */
+typedef struct kpm_device_csr {
+  int64_t rows;
+  int64_t nnz;
+  const int32_t* indptr;
+  const int32_t* indices;
+  const void* data;
+} kpm_device_csr;
+#define KPM_NOALLOC_SCRATCH_BYTES (8u << 20)
+KPM_API int kpm_dos_moments_noalloc(const kpm_device_csr* ham, double a,
+                                    double b, int precision, const void* vecs,
+                                    int64_t R, int64_t M, void* work,
+                                    double* moments, void* stream);
+
 /* ---- reconstruction (device) -------------------------------------------------
  * _moments + _calc_fft_moments, kwant/kpm.py:378-388 and :1197-1222:
  * moments (R x M x W complex128, host) -> mean over R (if mean) -> / a ->

@@ -101,6 +101,7 @@ def _load():
         'kpm_correlator_moments': [P, D, D, P, P, P, I64, I64, I, I, P],
         'kpm_integral_factor': [I64, P, P, P, P],
         'kpm_last_kernel_ms': [P, P],
+        'kpm_dos_moments_noalloc': [P, D, D, I, P, I64, I64, P, P, P],
         'kpm_profile': [P, I],
         'kpm_profile_read': [P, P, P],
         'kpm_launch_count': [P],

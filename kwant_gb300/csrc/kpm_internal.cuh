@@ -53,6 +53,9 @@ int launch_step(kpm_handle* h, int mode, bool dots, const StepArgs& a);
 StepArgs step_args(kpm_block* b, const void* x, const void* prev, void* out);
 int block_advance(kpm_block* b, bool dots);
 int block_norm(kpm_block* b);
+// sum the dot-product partials and write DOS moments (slots < 0 skipped)
+int finalize(kpm_block* b, int mode, double2* mom, int64_t slot_even,
+             int64_t slot_odd);
 int ensure_partials(kpm_handle* h, int groups, int xitems);
 int moments_to_host(kpm_handle* h, const double2* dev, int64_t count,
                     int64_t R, int64_t Rpad, int64_t W, double* host);
