@@ -81,6 +81,11 @@ struct Matrix {
   int32_t* indptr = nullptr;   // rows + 1
   int32_t* indices = nullptr;  // nnz
   void* data = nullptr;        // nnz complex (double2 raw H | float2 2H/a)
+  // ELL copy for the complex64 step kernel: ell_k entries per row (the row's
+  // CSR entries in order, then padding with column = row, value = 0)
+  int ell_k = 0;
+  int32_t* ell_idx = nullptr;  // [rows][ell_k]
+  float2* ell_val = nullptr;   // [rows][ell_k]
 };
 
 }  // namespace kpm
@@ -99,6 +104,8 @@ struct kpm_handle {
   int resident_step_blocks = 0;
   cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
   bool timed = false;
+  // rows per iteration of the ELL step kernel (1 or 2)
+  int step_rpi = 1;
   // optional locality reordering: device row p holds original row perm[p]
   int32_t* perm = nullptr;            // device, new -> old (null: identity)
   std::vector<int32_t> h_iperm;       // host, old -> new

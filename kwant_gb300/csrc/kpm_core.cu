@@ -152,8 +152,46 @@ int upload_matrix(kpm_handle* h, const kpm_csr_desc* m, double scale,
       dev_free(staging, h->stream);
       KPM_CUDA(e);
     }
+    KPM_TRY(build_ell(h, m, scale, out));
   }
   KPM_CUDA(cudaStreamSynchronize(h->stream));
+  return KPM_OK;
+}
+
+// ELL copy (complex64, values * scale) for rows of at most ELL_MAX entries.
+int build_ell(kpm_handle* h, const kpm_csr_desc* m, double scale,
+              Matrix* out) {
+  int64_t maxnnz = 0;
+  for (int64_t i = 0; i < m->rows; ++i)
+    maxnnz = std::max<int64_t>(maxnnz, m->indptr[i + 1] - m->indptr[i]);
+  const int64_t K = round_up(maxnnz > 0 ? maxnnz : 1, 4);
+  if (K > ELL_MAX) return KPM_OK;  // the CSR kernel handles wide rows
+  std::vector<int32_t> idx((size_t)m->rows * K);
+  std::vector<float2> val((size_t)m->rows * K);
+  for (int64_t i = 0; i < m->rows; ++i) {
+    int64_t q = 0;
+    for (int32_t k = m->indptr[i]; k < m->indptr[i + 1]; ++k, ++q) {
+      idx[i * K + q] = m->indices[k];
+      val[i * K + q] = make_float2((float)(m->data[2 * k] * scale),
+                                   (float)(m->data[2 * k + 1] * scale));
+    }
+    for (; q < K; ++q) {
+      idx[i * K + q] = (int32_t)i;
+      val[i * K + q] = make_float2(0.f, 0.f);
+    }
+  }
+  KPM_TRY(dev_alloc((void**)&out->ell_idx, idx.size() * sizeof(int32_t),
+                    h->stream));
+  KPM_TRY(dev_alloc((void**)&out->ell_val, val.size() * sizeof(float2),
+                    h->stream));
+  KPM_CUDA(cudaMemcpyAsync(out->ell_idx, idx.data(),
+                           idx.size() * sizeof(int32_t),
+                           cudaMemcpyHostToDevice, h->stream));
+  KPM_CUDA(cudaMemcpyAsync(out->ell_val, val.data(),
+                           val.size() * sizeof(float2),
+                           cudaMemcpyHostToDevice, h->stream));
+  KPM_CUDA(cudaStreamSynchronize(h->stream));
+  out->ell_k = (int)K;
   return KPM_OK;
 }
 
@@ -161,6 +199,11 @@ void free_matrix(Matrix* m, cudaStream_t s) {
   dev_free(m->indptr, s);
   dev_free(m->indices, s);
   dev_free(m->data, s);
+  dev_free(m->ell_idx, s);
+  dev_free(m->ell_val, s);
+  m->ell_idx = nullptr;
+  m->ell_val = nullptr;
+  m->ell_k = 0;
   m->indptr = nullptr;
   m->indices = nullptr;
   m->data = nullptr;
@@ -580,6 +623,8 @@ static int launch_step_t(kpm_handle* h, const StepArgs& a) {
 
 int launch_step(kpm_handle* h, int mode, bool dots, const StepArgs& a) {
   const bool mixed = h->precision == KPM_PREC_MIXED;
+  if (mixed && h->H.ell_k > 0 && mode != STEP_NORM && a.vals == h->H.data)
+    return launch_step_ell(h, mode, dots, a);
   if (mixed) {
     if (mode == STEP_FIRST)
       return dots ? launch_step_t<true, STEP_FIRST, true>(h, a)
@@ -774,6 +819,7 @@ int kpm_create_ex(const kpm_csr_desc* ham, double a, double b, int precision,
     return KPM_ECUDA;
   }
   h->own_stream = true;
+  if (const char* rpi = getenv("KPM_STEP_RPI")) h->step_rpi = atoi(rpi) == 2 ? 2 : 1;
   const double scale = h->precision == KPM_PREC_MIXED ? 2.0 / a : 0.0;
   if (flags & KPM_FLAG_REORDER) {
     st = validate_csr(ham);

@@ -50,6 +50,11 @@ int download_vectors(kpm_handle* h, const void* src, int64_t R, int64_t N,
                      int64_t Rpad, double* host);
 
 int launch_step(kpm_handle* h, int mode, bool dots, const StepArgs& a);
+// widest ELL row (entries) the complex64 ELL step kernel is built for
+constexpr int ELL_MAX = 16;
+int build_ell(kpm_handle* h, const kpm_csr_desc* m, double scale,
+              Matrix* out);
+int launch_step_ell(kpm_handle* h, int mode, bool dots, const StepArgs& a);
 StepArgs step_args(kpm_block* b, const void* x, const void* prev, void* out);
 int block_advance(kpm_block* b, bool dots);
 int block_norm(kpm_block* b);
