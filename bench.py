@@ -453,8 +453,95 @@ def run_ours(args):
     return 0
 
 
+def run_kubo(args):
+    """Kubo-Bastin workload (not the headline line): square 200 x 200, two
+    orbitals, t = 1, Rashba 0.3, exchange 0.2, W = 1 (seed 0), R = 16
+    vectors, M = 256 moments, sigma_xy.  One step = the device part of
+    conductivity(): both Chebyshev recursions with stored vectors and the
+    moments-matrix contraction on the tensor cores (BF16x3)."""
+    import torch
+    from kwant_gb300 import _lib, kpm, lattices
+    L, R, M = args.kubo_l, args.kubo_vectors, args.kubo_moments
+    syst = lattices.rashba_square(L, t=1.0, alpha=0.3, exchange=0.2, W=1.0,
+                                  seed=0)
+    ham = syst.hamiltonian_submatrix(sparse=True).tocsr()
+    n, nnz = ham.shape[0], ham.nnz
+    pos = syst.orbital_positions()
+    vx = kpm._velocity(ham, None, 'x', pos)
+    vy = kpm._velocity(ham, None, 'y', pos)
+    rng = np.random.RandomState(1)
+    v0 = np.exp(2j * np.pi * rng.random_sample(n))
+    vecs = np.exp(2j * np.pi * rng.random_sample((R, n)))
+    lo, hi = kpm.spectral_bounds(ham, 0.05, v0, 'lanczos')
+    a, b = kpm._rescale_ab(lo, hi, 0.05)
+    _a = a * (1 - 0.05 / 2)
+    a2, b2 = kpm._rescale_ab(b - _a, b + _a, 0.05)
+    h = _lib.Handle(ham, a, b, _lib.PREC_MIXED, reorder=True)
+    cva, cvb = _lib.Csr(vx), _lib.Csr(vy)
+    stream = torch.cuda.ExternalStream(h.stream())
+
+    def step():
+        return _lib.correlator_moments(h, a2, b2, cva, cvb, vecs, M, gemm=1)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    gem = []
+    e0.record(stream)
+    for _ in range(args.steps):
+        mu = step()
+        gem.append(h.last_gemm())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    g_ms = float(np.median([g[0] for g in gem]))
+    g_fl = gem[-1][1]
+    peaks = {}
+    pk = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    tpeak = float(peaks.get('bf16_tflops', 1900.0))
+    achieved = g_fl / (g_ms / 1e3) / 1e12
+    complex_flops = 8.0 * R * M * M * n
+    mu64 = None
+    if args.accuracy:
+        h64 = _lib.Handle(ham, a, b, _lib.PREC_FP64)
+        mu64 = _lib.correlator_moments(h64, a2, b2, cva, cvb, vecs, M, gemm=0)
+        h64.close()
+    line = {
+        'metric': METRIC, 'value': 2 * nnz * R * M / (ms / 1e3), 'unit': UNIT,
+        'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'c64 recursion + bf16x3 GEMM',
+        'data': 'synthetic',
+        'config': {'workload': 'kubo-bastin sigma_xy: rashba square %dx%d x2 '
+                               'orbitals, R=%d, M=%d' % (L, L, R, M),
+                   'nnz': int(nnz), 'orbitals': int(n)},
+        'roofline': {'bound': 'tensor', 'achieved': achieved, 'peak': tpeak,
+                     'unit': 'TFLOP/s', 'frac': achieved / tpeak,
+                     'traffic': None, 'kernel': 'bf16x3_tc_kernel',
+                     'mma_flops_per_launch': g_fl, 'avg_launch_ms': g_ms,
+                     'complex_equivalent_tflops':
+                         complex_flops / (g_ms / 1e3) / 1e12,
+                     'peak_source': 'measured' if 'bf16_tflops' in peaks
+                     else 'fallback'},
+        'accuracy': None if mu64 is None else {
+            'mu_rel_linf_vs_fp64': float(np.max(np.abs(mu - mu64)) /
+                                         np.max(np.abs(mu64)))},
+    }
+    print(json.dumps(line))
+    h.close()
+    return 0
+
+
 def main():
     p = argparse.ArgumentParser()
+    p.add_argument('--workload', default='dos', choices=['dos', 'kubo'])
+    p.add_argument('--kubo-l', type=int, default=200)
+    p.add_argument('--kubo-vectors', type=int, default=16)
+    p.add_argument('--kubo-moments', type=int, default=256)
     p.add_argument('--gpus', type=int, default=1)
     p.add_argument('--steps', type=int, default=5)
     p.add_argument('--warmup', type=int, default=3)
@@ -474,6 +561,8 @@ def main():
         print('warning: fewer than 3 warm-up steps', file=sys.stderr)
     if args.impl == 'reference':
         return run_reference(args)
+    if args.workload == 'kubo':
+        return run_kubo(args)
     return run_ours(args)
 
 

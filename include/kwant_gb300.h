@@ -251,7 +251,8 @@ KPM_API int kpm_handle_matvec(kpm_handle* h, const double* x, double* y);
  * kwant/kpm.py:576-579).  v_alpha, v_beta are CSR (e.g. the velocity of
  * _velocity, kwant/kpm.py:1042-1085).  gemm selects the contraction:
  *   0 = FP64 CUDA-core GEMM, 1 = tensor-core split-BF16 (hi+lo) GEMM with
- *   FP32 accumulation (tcgen05), 2 = automatic (1 for MIXED, 0 for FP64).
+ *   FP32 accumulation (tcgen05), 2 = automatic (1 for MIXED, 0 for FP64),
+ *   3 = the same BF16 hi/lo products on CUDA cores (checks gemm 1).
  * mu_out is the mean over vectors (or R x M x M when per_vector). */
 KPM_API int kpm_correlator_moments(kpm_handle* h, double a2, double b2,
                                    const kpm_csr_desc* v_alpha,
@@ -276,6 +277,10 @@ KPM_API int kpm_last_kernel_ms(kpm_handle* h, double* ms);
 KPM_API int kpm_profile(kpm_handle* h, int enable);
 KPM_API int kpm_profile_read(kpm_handle* h, int64_t* launches,
                              double* total_ms);
+/* Device time (CUDA events around the kernel) of the last tensor-core
+ * moments-matrix contraction of the handle, and the BF16 MMA flops it
+ * executed (12 real products x 2 M^2 K_padded); 0 if none ran. */
+KPM_API int kpm_last_gemm(kpm_handle* h, double* ms, double* flops);
 /* Number of kernel launches issued by this library since load. */
 KPM_API int kpm_launch_count(int64_t* count);
 

@@ -102,6 +102,7 @@ def _load():
         'kpm_integral_factor': [I64, P, P, P, P],
         'kpm_last_kernel_ms': [P, P],
         'kpm_dos_moments_noalloc': [P, D, D, I, P, I64, I64, P, P, P],
+        'kpm_last_gemm': [P, P, P],
         'kpm_profile': [P, I],
         'kpm_profile_read': [P, P, P],
         'kpm_launch_count': [P],
@@ -207,6 +208,11 @@ class Handle:
         ms = C.c_double()
         check(lib.kpm_last_kernel_ms(self._h, C.byref(ms)))
         return ms.value
+
+    def last_gemm(self):
+        ms, fl = C.c_double(), C.c_double()
+        check(lib.kpm_last_gemm(self._h, C.byref(ms), C.byref(fl)))
+        return ms.value, fl.value
 
     def profile(self, enable=True):
         check(lib.kpm_profile(self._h, 1 if enable else 0))

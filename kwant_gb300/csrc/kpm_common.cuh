@@ -104,6 +104,9 @@ struct kpm_handle {
   int resident_step_blocks = 0;
   cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
   bool timed = false;
+  // device time of the last tensor-core contraction and its MMA flops
+  cudaEvent_t ev_gemm0 = nullptr, ev_gemm1 = nullptr;
+  double last_gemm_ms = 0.0, last_gemm_flops = 0.0;
   // rows per iteration of the ELL step kernel (1 or 2)
   int step_rpi = 1;
   // optional locality reordering: device row p holds original row perm[p]

@@ -513,12 +513,14 @@ cheb_step_kernel(StepArgs p) {
         red[slot][(lane * VPL + k) * 3 + 2] = cim[k];
       }
       __syncthreads();
-      double* dst = p.partials + ((int64_t)g * p.xitems + xi) * (G * 3);
+      // layout [group][vector*3 + component][partition]: the finalize
+      // kernel reads each vector's partitions contiguously
+      double* dst = p.partials + (int64_t)g * (G * 3) * p.xitems + xi;
       for (int e = threadIdx.x; e < G * 3; e += blockDim.x) {
         double s = 0.0;
 #pragma unroll
         for (int q = 0; q < SLOTS; ++q) s += red[q][e];
-        dst[e] = s;
+        dst[(int64_t)e * p.xitems] = s;
       }
       __syncthreads();
     }
@@ -536,11 +538,11 @@ __global__ void dos_finalize_kernel(const double* __restrict__ partials,
   const int g = (int)(v / G), e0 = (int)(v % G) * 3;
   __shared__ double s[3][128];
   double acc[3] = {0.0, 0.0, 0.0};
+  const double* src = partials + ((int64_t)g * (G * 3) + e0) * xitems;
   for (int xi = threadIdx.x; xi < xitems; xi += blockDim.x) {
-    const double* src = partials + ((int64_t)g * xitems + xi) * (G * 3) + e0;
-    acc[0] += src[0];
-    acc[1] += src[1];
-    acc[2] += src[2];
+    acc[0] += src[xi];
+    acc[1] += src[xitems + xi];
+    acc[2] += src[2 * (int64_t)xitems + xi];
   }
   for (int c = 0; c < 3; ++c) s[c][threadIdx.x] = acc[c];
   __syncthreads();
@@ -868,6 +870,8 @@ int kpm_destroy(kpm_handle* h) {
   if (h->ev_start) cudaEventDestroy(h->ev_start);
   if (h->ev_stop) cudaEventDestroy(h->ev_stop);
   for (cudaEvent_t e : h->prof_events) cudaEventDestroy(e);
+  if (h->ev_gemm0) cudaEventDestroy(h->ev_gemm0);
+  if (h->ev_gemm1) cudaEventDestroy(h->ev_gemm1);
   cudaStreamSynchronize(h->stream);
   if (h->own_stream) cudaStreamDestroy(h->stream);
   cudaGetLastError();
@@ -895,6 +899,13 @@ int kpm_profile_read(kpm_handle* h, int64_t* launches, double* total_ms) {
   *launches = (int64_t)(h->prof_used / 2);
   *total_ms = tot;
   h->prof_used = 0;
+  return KPM_OK;
+}
+
+int kpm_last_gemm(kpm_handle* h, double* ms, double* flops) {
+  KPM_REQUIRE(h && ms && flops, "kpm_last_gemm: null argument");
+  *ms = h->last_gemm_ms;
+  *flops = h->last_gemm_flops;
   return KPM_OK;
 }
 

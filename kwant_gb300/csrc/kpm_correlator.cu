@@ -190,8 +190,8 @@ int kpm_correlator_moments(kpm_handle* h, double a2, double b2,
               "kpm_correlator_moments: operator shape mismatch");
   KPM_REQUIRE(a2 > 0, "kpm_correlator_moments: a2 must be positive");
   if (gemm == 2) gemm = h->precision == KPM_PREC_MIXED ? 1 : 0;
-  KPM_REQUIRE(gemm == 0 || gemm == 1, "kpm_correlator_moments: bad gemm");
-  if (gemm == 1 && per_vector) {
+  KPM_REQUIRE(gemm >= 0 && gemm <= 3, "kpm_correlator_moments: bad gemm");
+  if (gemm != 0 && per_vector) {
     set_error("kpm_correlator_moments: per-vector moments need gemm=0");
     return KPM_EUNSUPPORTED;
   }
@@ -203,7 +203,7 @@ int kpm_correlator_moments(kpm_handle* h, double a2, double b2,
   Store psi, omega;
   int st = upload_matrix_for(h, v_alpha, 0.0, &Va);
   if (st == KPM_OK) st = upload_matrix_for(h, v_beta, 0.0, &Vb);
-  const int kind = gemm == 1 ? STORE_BF16X3 : STORE_C128;
+  const int kind = gemm == 0 ? STORE_C128 : STORE_BF16X3;
   if (st == KPM_OK) st = store_alloc(&psi, kind, M, K, s);
   if (st == KPM_OK) st = store_alloc(&omega, kind, M, K, s);
   if (st == KPM_OK) st = kpm_block_create(h, vecs, R, 1, &bR);
@@ -261,6 +261,8 @@ int kpm_correlator_moments(kpm_handle* h, double a2, double b2,
   if (st == KPM_OK) {
     if (gemm == 0)
       st = gemm_fp64(h, &omega, &psi, M, K, R, per_vector, mu_out);
+    else if (gemm == 3)
+      st = gemm_bf16x3_simt(h, &omega, &psi, M, K, R, mu_out);
     else
       st = gemm_bf16x3(h, &omega, &psi, M, K, R, mu_out);
   }

@@ -1,6 +1,30 @@
-// Tensor-core (tcgen05) split-BF16 contraction of the correlator moments
-// matrix.  Placeholder dispatch: the CUDA-core evaluation of the same BF16x3
-// products is used until the tcgen05 kernel is enabled.
+// Tensor-core (tcgen05) contraction of the correlator moments matrix.
+//
+//   mu_mn = (1/R) sum_K conj(Omega[m][K]) Psi[n][K]
+//
+// (Correlator._calculate_moments_matrix, kwant/kpm.py:685-695) on BF16x3
+// stores: every real component x is held as hi = bf16(x), lo = bf16(x - hi),
+// in four K-major planes (re_hi, re_lo, im_hi, im_lo).  With A = Omega,
+// B = Psi:
+//   Re mu = Ar Br^T + Ai Bi^T,   Im mu = Ar Bi^T - Ai Br^T,
+// and every real product X Y^T is formed as Xh Yh^T + Xh Yl^T + Xl Yh^T
+// (the lo*lo term, ~2^-16 relative, is dropped): 12 BF16 MMAs per K step,
+// FP32 accumulation in tensor memory, the minus sign through the MMA's
+// negate-A bit.
+//
+// One CTA computes a 128 x NT output tile of both Re and Im (2*NT <= 512
+// TMEM columns) over one K range (split-K); 4 warps: warp 0 allocates TMEM
+// and issues the TMA loads (one 3D box per operand = its four planes),
+// warp 1 issues the MMAs from one thread, all four warps drain TMEM in the
+// epilogue.  Two pipeline stages of 32 K-elements (64-byte swizzle).  The
+// split partials (FP32) are summed in FP64 in a fixed order.
+//
+// Every wait on an mbarrier is bounded (about 2 s of GPU time); on expiry
+// the kernel records an error code, stops issuing work, releases its tensor
+// memory and returns, and the host reports KPM_ETIMEOUT.
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
 
 #include "kpm_common.cuh"
 #include "kpm_internal.cuh"
@@ -8,9 +32,430 @@
 
 namespace kpm {
 
+namespace tc {
+
+constexpr int TM = 128;          // output rows per CTA (MMA M)
+constexpr int KC = 32;           // K elements per stage (64 bytes of bf16)
+constexpr int STAGES = 2;
+constexpr int THREADS = 128;
+constexpr uint64_t WAIT_NS = 2000000000ull;  // bounded waits: 2 s
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile(
+      "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+          smem_u32(bar)),
+      "r"(bytes)
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n"
+      " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait; returns false (and records err) when the deadline passes.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
+                                          int* err, int code) {
+  const uint64_t t0 = global_ns();
+  while (!mbar_try_wait(bar, parity)) {
+    if (*(volatile int*)err) return false;
+    if (global_ns() - t0 > WAIT_NS) {
+      atomicCAS(err, 0, code);
+      return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map,
+                                            uint64_t* bar, int c0, int c1,
+                                            int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx"
+      "::bytes [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(c0),
+      "r"(c1), "r"(c2)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 64-byte swizzle, 8-row groups
+// 512 bytes apart (stride byte offset), version 1.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFF) >> 4);      // start address
+  d |= (uint64_t)1 << 16;                       // leading byte offset (unused)
+  d |= (uint64_t)(512 >> 4) << 32;              // stride byte offset
+  d |= (uint64_t)1 << 46;                       // descriptor version
+  d |= (uint64_t)4 << 61;                       // swizzle: 64B
+  return d;
+}
+
+// Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major,
+// M = 128, N = n; optional negation of A.
+__host__ __device__ constexpr uint32_t instr_desc(int n, bool neg_a) {
+  return (1u << 4)                    // D format F32
+         | (1u << 7)                  // A format BF16
+         | (1u << 10)                 // B format BF16
+         | ((neg_a ? 1u : 0u) << 13)  // negate A
+         | ((uint32_t)(n >> 3) << 17) // N / 8
+         | ((uint32_t)(TM >> 4) << 24);  // M / 16
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc,
+                                         uint64_t b_desc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 "
+      "[%0];" ::"r"(smem_u32(bar))
+      : "memory");
+}
+
+struct TcArgs {
+  int64_t M;        // rows of the output (num_moments)
+  int64_t kchunks;  // K / KC (padded K)
+  int splits;
+  int nt;           // output columns per CTA (multiple of 16, <= 256)
+  int ntiles_n;
+  int tmem_cols;    // power of two >= 2 * nt
+  float2* part;     // [split][M][M] (re, im) partials
+  int* err;
+};
+
+__global__ void __launch_bounds__(THREADS, 1)
+bf16x3_tc_kernel(const __grid_constant__ CUtensorMap map_a,
+                 const __grid_constant__ CUtensorMap map_b, TcArgs args) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  // align the dynamic shared memory to 1024 bytes (swizzle atoms)
+  uint8_t* smem = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int nt = args.nt;
+  const uint32_t a_bytes = 4 * TM * KC * 2;   // 32 KB
+  const uint32_t b_bytes = 4 * nt * KC * 2;   // up to 64 KB
+  uint8_t* sa = smem;                          // STAGES x a_bytes
+  uint8_t* sb = smem + STAGES * a_bytes;       // STAGES x b_bytes
+  uint64_t* full = reinterpret_cast<uint64_t*>(sb + STAGES * b_bytes);
+  uint64_t* empty = full + STAGES;
+  uint64_t* done = empty + STAGES;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  // tile / split of this CTA
+  const int tiles = (int)(ceil_div(args.M, TM) * args.ntiles_n);
+  const int tile = blockIdx.x % tiles;
+  const int split = blockIdx.x / tiles;
+  const int tm = tile / args.ntiles_n, tn = tile % args.ntiles_n;
+  const int64_t c_per = ceil_div(args.kchunks, args.splits);
+  const int64_t kc0 = split * c_per;
+  const int64_t kc1 = kc0 + c_per < args.kchunks ? kc0 + c_per : args.kchunks;
+  const int64_t nk = kc1 > kc0 ? kc1 - kc0 : 0;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile(
+        "tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::
+            "r"(smem_u32(tmem_slot)),
+        "r"(args.tmem_cols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    // ---- TMA producer
+    for (int64_t i = 0; i < nk; ++i) {
+      const int s = (int)(i % STAGES);
+      const uint32_t ph = (uint32_t)((i / STAGES) & 1);
+      if (!mbar_wait(&empty[s], ph ^ 1, args.err, 1)) break;
+      mbar_expect_tx(&full[s], a_bytes + b_bytes);
+      const int kx = (int)((kc0 + i) * KC);
+      tma_load_3d(sa + s * a_bytes, &map_a, &full[s], kx, tm * TM, 0);
+      tma_load_3d(sb + s * b_bytes, &map_b, &full[s], kx, tn * nt, 0);
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---- MMA issuer
+    const uint32_t id_pos = instr_desc(nt, false);
+    const uint32_t id_neg = instr_desc(nt, true);
+    const uint32_t d_re = tmem, d_im = tmem + (uint32_t)nt;
+    const uint32_t plane_a = TM * KC * 2, plane_b = (uint32_t)nt * KC * 2;
+    bool ok = true;
+    for (int64_t i = 0; i < nk && ok; ++i) {
+      const int s = (int)(i % STAGES);
+      const uint32_t ph = (uint32_t)((i / STAGES) & 1);
+      if (!mbar_wait(&full[s], ph, args.err, 2)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t a0 = smem_u32(sa + s * a_bytes);
+      const uint32_t b0 = smem_u32(sb + s * b_bytes);
+#pragma unroll
+      for (int ks = 0; ks < KC / 16; ++ks) {
+        const uint32_t ko = ks * 32;  // bytes along K inside the 64-B rows
+        // planes: 0 re_hi, 1 re_lo, 2 im_hi, 3 im_lo
+        const uint64_t Arh = smem_desc(a0 + 0 * plane_a + ko);
+        const uint64_t Arl = smem_desc(a0 + 1 * plane_a + ko);
+        const uint64_t Aih = smem_desc(a0 + 2 * plane_a + ko);
+        const uint64_t Ail = smem_desc(a0 + 3 * plane_a + ko);
+        const uint64_t Brh = smem_desc(b0 + 0 * plane_b + ko);
+        const uint64_t Brl = smem_desc(b0 + 1 * plane_b + ko);
+        const uint64_t Bih = smem_desc(b0 + 2 * plane_b + ko);
+        const uint64_t Bil = smem_desc(b0 + 3 * plane_b + ko);
+        const uint32_t acc0 = (i > 0 || ks > 0) ? 1u : 0u;
+        // Re += Ar Br + Ai Bi
+        mma_bf16(d_re, Arh, Brh, id_pos, acc0);
+        mma_bf16(d_re, Arh, Brl, id_pos, 1u);
+        mma_bf16(d_re, Arl, Brh, id_pos, 1u);
+        mma_bf16(d_re, Aih, Bih, id_pos, 1u);
+        mma_bf16(d_re, Aih, Bil, id_pos, 1u);
+        mma_bf16(d_re, Ail, Bih, id_pos, 1u);
+        // Im += Ar Bi - Ai Br
+        mma_bf16(d_im, Arh, Bih, id_pos, acc0);
+        mma_bf16(d_im, Arh, Bil, id_pos, 1u);
+        mma_bf16(d_im, Arl, Bih, id_pos, 1u);
+        mma_bf16(d_im, Aih, Brh, id_neg, 1u);
+        mma_bf16(d_im, Aih, Brl, id_neg, 1u);
+        mma_bf16(d_im, Ail, Brh, id_neg, 1u);
+      }
+      mma_commit(&empty[s]);  // frees the stage when these MMAs complete
+    }
+    mma_commit(done);  // all MMAs of this thread
+  }
+
+  // ---- epilogue: all four warps (the MMA thread always commits `done`)
+  __syncwarp();
+  const bool have = mbar_wait(done, 0, args.err, 3) && nk > 0;
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if (have && *(volatile int*)args.err == 0) {
+    const int row = tm * TM + warp * 32 + lane;
+    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    float2* dst = args.part + ((int64_t)split * args.M + row) * args.M;
+    for (int c = 0; c < nt; c += 16) {
+      uint32_t re[16], im[16];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+          "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(re[0]), "=r"(re[1]), "=r"(re[2]), "=r"(re[3]), "=r"(re[4]),
+            "=r"(re[5]), "=r"(re[6]), "=r"(re[7]), "=r"(re[8]), "=r"(re[9]),
+            "=r"(re[10]), "=r"(re[11]), "=r"(re[12]), "=r"(re[13]),
+            "=r"(re[14]), "=r"(re[15])
+          : "r"(tmem + lane_base + (uint32_t)c));
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+          "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(im[0]), "=r"(im[1]), "=r"(im[2]), "=r"(im[3]), "=r"(im[4]),
+            "=r"(im[5]), "=r"(im[6]), "=r"(im[7]), "=r"(im[8]), "=r"(im[9]),
+            "=r"(im[10]), "=r"(im[11]), "=r"(im[12]), "=r"(im[13]),
+            "=r"(im[14]), "=r"(im[15])
+          : "r"(tmem + lane_base + (uint32_t)(nt + c)));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (row < args.M) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int64_t col = (int64_t)tn * nt + c + j;
+          if (col < args.M)
+            dst[col] = make_float2(__uint_as_float(re[j]),
+                                   __uint_as_float(im[j]));
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile(
+        "tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+        "r"(args.tmem_cols));
+  }
+}
+
+// sum the split partials in fixed order (FP64), scale, complex128 out
+__global__ void tc_reduce_kernel(const float2* __restrict__ part, int splits,
+                                 int64_t MM, double scale,
+                                 double2* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= MM) return;
+  double r = 0.0, im = 0.0;
+  for (int s = 0; s < splits; ++s) {
+    const float2 p = part[(int64_t)s * MM + i];
+    r += (double)p.x;
+    im += (double)p.y;
+  }
+  out[i] = make_double2(r * scale, im * scale);
+}
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                         cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    cudaGetLastError();
+  }
+  return fn;
+}
+
+// 3D map over the four planes of a store: dims {Kp, M, 4}, box {KC, rows, 4}
+static int make_map(CUtensorMap* map, const Store* s, int box_rows) {
+  auto fn = encode_fn();
+  if (!fn) {
+    set_error("cuTensorMapEncodeTiled unavailable");
+    return KPM_ECUDA;
+  }
+  cuuint64_t dims[3] = {(cuuint64_t)s->Kp, (cuuint64_t)s->M, 4};
+  cuuint64_t strides[2] = {(cuuint64_t)s->Kp * 2,
+                           (cuuint64_t)s->M * s->Kp * 2};
+  cuuint32_t box[3] = {(cuuint32_t)KC, (cuuint32_t)box_rows, 4};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, s->planes, dims,
+                  strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return KPM_ECUDA;
+  }
+  return KPM_OK;
+}
+
+}  // namespace tc
+
+int gemm_bf16x3_tc(kpm_handle* h, const Store* omega, const Store* psi,
+                   int64_t M, int64_t K, int64_t R, double* mu_host) {
+  using namespace tc;
+  KPM_REQUIRE(omega->kind == STORE_BF16X3 && psi->kind == STORE_BF16X3,
+              "tensor-core contraction needs BF16x3 stores");
+  KPM_REQUIRE(omega->Kp % KC == 0 && omega->Kp == psi->Kp,
+              "store K padding mismatch");
+  KPM_REQUIRE(M < (1 << 20), "too many moments");
+  int nt = (int)round_up(M < 256 ? M : 256, 16);
+  const int ntiles_n = (int)ceil_div(M, nt);
+  int tmem_cols = 32;
+  while (tmem_cols < 2 * nt) tmem_cols *= 2;
+  const int64_t kchunks = omega->Kp / KC;
+  const int tiles = (int)(ceil_div(M, TM) * ntiles_n);
+  // one CTA per SM in total, split K among the tiles
+  int splits = (int)(h->num_sms / tiles);
+  if (splits < 1) splits = 1;
+  if (splits > kchunks) splits = (int)kchunks;
+  // every split gets at least one K chunk (all partials are written)
+  const int64_t c_per = ceil_div(kchunks, splits);
+  splits = (int)ceil_div(kchunks, c_per);
+
+  CUtensorMap map_a, map_b;
+  KPM_TRY(make_map(&map_a, omega, TM));
+  KPM_TRY(make_map(&map_b, psi, nt));
+
+  const size_t a_bytes = 4 * TM * KC * 2, b_bytes = (size_t)4 * nt * KC * 2;
+  const size_t smem = 1024 + STAGES * (a_bytes + b_bytes) +
+                      (2 * STAGES + 1) * 8 + 16;
+  KPM_CUDA(cudaFuncSetAttribute(bf16x3_tc_kernel,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem));
+  float2* part = nullptr;
+  int* err = nullptr;
+  KPM_TRY(dev_alloc((void**)&part, (size_t)splits * M * M * sizeof(float2),
+                    h->stream));
+  int st = dev_alloc((void**)&err, sizeof(int), h->stream);
+  cudaError_t e = cudaSuccess;
+  if (st == KPM_OK) e = cudaMemsetAsync(err, 0, sizeof(int), h->stream);
+  if (st == KPM_OK && e == cudaSuccess && !h->ev_gemm0) {
+    e = cudaEventCreate(&h->ev_gemm0);
+    if (e == cudaSuccess) e = cudaEventCreate(&h->ev_gemm1);
+  }
+  if (st == KPM_OK && e == cudaSuccess) {
+    TcArgs args{M, kchunks, splits, nt, ntiles_n, tmem_cols, part, err};
+    cudaEventRecord(h->ev_gemm0, h->stream);
+    bf16x3_tc_kernel<<<(unsigned)(tiles * splits), THREADS, smem,
+                       h->stream>>>(map_a, map_b, args);
+    count_launch(1);
+    e = cudaGetLastError();
+    cudaEventRecord(h->ev_gemm1, h->stream);
+  }
+  int herr = 0;
+  if (st == KPM_OK && e == cudaSuccess)
+    e = cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost,
+                        h->stream);
+  if (st == KPM_OK && e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (st == KPM_OK && e == cudaSuccess) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, h->ev_gemm0, h->ev_gemm1) == cudaSuccess)
+      h->last_gemm_ms = ms;
+    h->last_gemm_flops = 3.0 * 4.0 * 2.0 * (double)M * (double)M *
+                         (double)omega->Kp;
+  }
+  double2* mu = nullptr;
+  if (st == KPM_OK && e == cudaSuccess && herr == 0) {
+    st = dev_alloc((void**)&mu, (size_t)M * M * sizeof(double2), h->stream);
+    if (st == KPM_OK) {
+      tc_reduce_kernel<<<(unsigned)ceil_div(M * M, 256), 256, 0, h->stream>>>(
+          part, splits, M * M, 1.0 / (double)R, mu);
+      count_launch(1);
+      e = cudaGetLastError();
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(mu_host, mu, (size_t)M * M * sizeof(double2),
+                            cudaMemcpyDeviceToHost, h->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    }
+  }
+  dev_free(mu, h->stream);
+  dev_free(part, h->stream);
+  dev_free(err, h->stream);
+  if (st != KPM_OK) return st;
+  KPM_CUDA(e);
+  if (herr != 0) {
+    set_error("tensor-core contraction: a bounded wait expired (code %d)",
+              herr);
+    return KPM_ETIMEOUT;
+  }
+  return KPM_OK;
+}
+
 int gemm_bf16x3(kpm_handle* h, const Store* omega, const Store* psi,
                 int64_t M, int64_t K, int64_t R, double* mu_host) {
-  return gemm_bf16x3_simt(h, omega, psi, M, K, R, mu_host);
+  return gemm_bf16x3_tc(h, omega, psi, M, K, R, mu_host);
 }
 
 }  // namespace kpm

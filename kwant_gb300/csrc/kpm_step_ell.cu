@@ -17,8 +17,18 @@
 
 namespace kpm {
 
+// Blocks per SM the register budget is sized for (narrow rows need few
+// registers; 6 x 256 threads leaves 40 registers per thread).
+#ifndef KPM_ELL_MIN_BLOCKS
+#define KPM_ELL_MIN_BLOCKS 5
+#endif
+template <int K, int RPI>
+constexpr int ell_min_blocks() {
+  return (K <= 4 && RPI == 1) ? KPM_ELL_MIN_BLOCKS : 1;
+}
+
 template <int K, int MODE, bool DOTS, int RPI>
-__global__ void __launch_bounds__(STEP_THREADS)
+__global__ void __launch_bounds__(STEP_THREADS, ell_min_blocks<K, RPI>())
 cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
                      const float2* __restrict__ eval) {
   constexpr int G = GROUP_FP32;
@@ -139,12 +149,14 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
       my[4] += (double)fr1;
       my[5] += (double)fi1;
       __syncthreads();
-      double* dst = p.partials + ((int64_t)g * p.xitems + xi) * (G * 3);
+      // layout [group][vector*3 + component][partition]: the finalize
+      // kernel reads each vector's partitions contiguously
+      double* dst = p.partials + (int64_t)g * (G * 3) * p.xitems + xi;
       for (int e = threadIdx.x; e < G * 3; e += blockDim.x) {
         double s = 0.0;
 #pragma unroll
         for (int q = 0; q < SLOTS; ++q) s += red[q][e];
-        dst[e] = s;
+        dst[(int64_t)e * p.xitems] = s;
       }
       __syncthreads();
     }

@@ -547,8 +547,27 @@ class SpectralDensity:
         moments /= self._a
         return self.kernel(moments)
 
+    def _check_divergence(self):
+        """Failure detection for spectral bounds that are too tight: the DOS
+        moments of a vector obey |mu_n| <= mu_0 when the rescaled spectrum
+        lies in [-1, 1] (|T_n| <= 1 there); a bound that leaves eigenvalues
+        outside makes T_n grow exponentially.  The reference does not check
+        this; here it is reported with a warning (results are returned
+        unchanged, as the reference would)."""
+        if self._lowered is not None or self._moments_arr is None:
+            return
+        mom = self._moments_arr[:, :, 0]
+        mu0 = np.abs(mom[:, :1].real)
+        if np.any(np.abs(mom) > 1.01 * mu0 + 1e-300):
+            import warnings
+            warnings.warn('Chebyshev moments exceed mu_0: the spectral bounds '
+                          '%r do not enclose the spectrum; the recursion '
+                          'diverged' % (self.bounds,), RuntimeWarning,
+                          stacklevel=3)
+
     def _reconstruct(self):
         """Mean, 1/a, kernel and DCT on the device (kwant/kpm.py:251-252)."""
+        self._check_divergence()
         arr = self._moments_arr                      # (R, M, W)
         R, M, W = arr.shape
         is_real = bool(np.all(np.abs(arr.imag) <

@@ -200,6 +200,17 @@ def test_mixed_operator_moments(kpm):
 
 
 # ------------------------------------------------------------------ bounds
+def test_divergence_warning_on_tight_bounds(kpm):
+    """Failure detection without a GPU fault: bounds that cut the spectrum
+    make the recursion grow; the host flags it from the moments."""
+    g = load('rmt20')
+    with pytest.warns(RuntimeWarning, match='do not enclose'):
+        kpm.SpectralDensity(g['ham'], bounds=(0.5 * g['lmin'],
+                                              0.5 * g['lmax']),
+                            num_moments=200, num_vectors=2, rng=1)
+
+
+
 def test_lanczos_bounds_enclose_spectrum(kpm):
     g = load('rmt20')
     ev = np.linalg.eigvalsh(g['ham'])
@@ -301,6 +312,37 @@ def test_conductivity_mixed_bf16x3(kpm):
     # error with a margin, relative to the largest |sigma|.
     err = np.max(np.abs(vals - g['values_xy']))
     assert err < 2e-2 * max(1.0, np.max(np.abs(g['values_xy']))), err
+
+
+def test_tensor_core_contraction_matches_cuda_cores(kpm):
+    """The tcgen05 split-BF16 GEMM equals the CUDA-core evaluation of the
+    same hi*hi + hi*lo + lo*hi products (FP32 sums in another order), and
+    both approximate the FP64 contraction; moment counts cover partial N
+    tiles (48), several M tiles (160) and several N tiles (300)."""
+    from kwant_gb300 import _lib, lattices
+    syst = lattices.rashba_square(12, seed=3)
+    ham = syst.hamiltonian_submatrix(sparse=True).tocsr()
+    pos = syst.orbital_positions()
+    vx = ko.velocity(ham, pos, 0)
+    vy = ko.velocity(ham, pos, 1)
+    n = ham.shape[0]
+    rng = np.random.RandomState(5)
+    vecs = np.exp(2j * np.pi * rng.random_sample((6, n)))
+    # Gershgorin bound: encloses the spectrum, so the recursion stays bounded
+    g = float(np.max(np.asarray(abs(ham).sum(axis=1))))
+    a, b = ko.rescale_ab(-g, g, 0.05)
+    _a = a * (1 - 0.05 / 2)
+    a2, b2 = ko.rescale_ab(b - _a, b + _a, 0.05)
+    hm = _lib.Handle(ham, a, b, _lib.PREC_MIXED)
+    h64 = _lib.Handle(ham, a, b, _lib.PREC_FP64)
+    for M in (48, 160, 300):
+        mu_tc = _lib.correlator_moments(hm, a2, b2, vx, vy, vecs, M, gemm=1)
+        ms, flops = hm.last_gemm()
+        assert ms > 0 and flops > 0
+        mu_cc = _lib.correlator_moments(hm, a2, b2, vx, vy, vecs, M, gemm=3)
+        mu_64 = _lib.correlator_moments(h64, a2, b2, vx, vy, vecs, M, gemm=0)
+        assert _rel(mu_tc, mu_cc) < 1e-5, M
+        assert _rel(mu_tc, mu_64) < 1e-4, M
 
 
 # --------------------------------------------------------------- reordering
