@@ -107,6 +107,10 @@ struct kpm_handle {
   // device time of the last tensor-core contraction and its MMA flops
   cudaEvent_t ev_gemm0 = nullptr, ev_gemm1 = nullptr;
   double last_gemm_ms = 0.0, last_gemm_flops = 0.0;
+  // K elements per pipeline stage of the tensor-core contraction: 32 (two
+  // stages, 64-byte rows; measured 3.09 ms on the 200x200x2 / R=16 / M=256
+  // workload) or 16 (four stages, 32-byte rows; 6.13 ms)
+  int tc_kc = 32;
   // rows per iteration of the ELL step kernel (1 or 2)
   int step_rpi = 1;
   // optional locality reordering: device row p holds original row perm[p]

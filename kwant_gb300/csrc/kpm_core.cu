@@ -113,7 +113,7 @@ int validate_csr(const kpm_csr_desc* m) {
 }
 
 int upload_matrix(kpm_handle* h, const kpm_csr_desc* m, double scale,
-                  Matrix* out) {
+                  Matrix* out, bool with_ell) {
   KPM_TRY(validate_csr(m));
   out->rows = m->rows;
   out->nnz = m->nnz;
@@ -152,7 +152,7 @@ int upload_matrix(kpm_handle* h, const kpm_csr_desc* m, double scale,
       dev_free(staging, h->stream);
       KPM_CUDA(e);
     }
-    KPM_TRY(build_ell(h, m, scale, out));
+    if (with_ell) KPM_TRY(build_ell(h, m, scale, out));
   }
   KPM_CUDA(cudaStreamSynchronize(h->stream));
   return KPM_OK;
@@ -822,6 +822,7 @@ int kpm_create_ex(const kpm_csr_desc* ham, double a, double b, int precision,
   }
   h->own_stream = true;
   if (const char* rpi = getenv("KPM_STEP_RPI")) h->step_rpi = atoi(rpi) == 2 ? 2 : 1;
+  if (const char* kc = getenv("KPM_TC_KC")) h->tc_kc = atoi(kc) == 32 ? 32 : 16;
   const double scale = h->precision == KPM_PREC_MIXED ? 2.0 / a : 0.0;
   if (flags & KPM_FLAG_REORDER) {
     st = validate_csr(ham);

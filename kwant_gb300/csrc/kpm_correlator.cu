@@ -26,46 +26,53 @@
 
 namespace kpm {
 
+// Complex arithmetic in the recursion's precision: complex64 values, vectors
+// and FP32 math in mixed mode (GB300's FP64 pipe is narrow), complex128 in
+// FP64 mode.
+template <bool MIXED> struct CT;
+template <> struct CT<true> {
+  using S = float;
+  using V2 = float2;
+  static __device__ __forceinline__ V2 make(S a, S b) {
+    return make_float2(a, b);
+  }
+};
+template <> struct CT<false> {
+  using S = double;
+  using V2 = double2;
+  static __device__ __forceinline__ V2 make(S a, S b) {
+    return make_double2(a, b);
+  }
+};
+
 // y[i][r] = sum_j V_ij x[j][r], written to the K-major store row
 // (K index i * R + r).  One thread per (row, vector); vectors fastest.
+// V == nullptr copies x (the Omega side has no operator).
 template <bool MIXED, int STORE>
 __global__ void spmm_to_store_kernel(int64_t rows, int64_t R, int64_t Rpad,
                                      const int32_t* __restrict__ ip,
                                      const int32_t* __restrict__ ix,
-                                     const double2* __restrict__ v,
+                                     const void* __restrict__ vals,
                                      const void* __restrict__ x,
                                      StoreRow dst) {
+  using S = typename CT<MIXED>::S;
+  using V2 = typename CT<MIXED>::V2;
   const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= rows * R) return;
   const int64_t i = idx / R, r = idx % R;
-  double yr = 0.0, yi = 0.0;
-  if (v == nullptr) {
-    if constexpr (MIXED) {
-      const float2 a = reinterpret_cast<const float2*>(x)[i * Rpad + r];
-      yr = a.x;
-      yi = a.y;
-    } else {
-      const double2 a = reinterpret_cast<const double2*>(x)[i * Rpad + r];
-      yr = a.x;
-      yi = a.y;
-    }
+  const V2* __restrict__ X = reinterpret_cast<const V2*>(x);
+  const V2* __restrict__ V = reinterpret_cast<const V2*>(vals);
+  S yr = 0, yi = 0;
+  if (V == nullptr) {
+    const V2 a = X[i * Rpad + r];
+    yr = a.x;
+    yi = a.y;
   } else {
     for (int jj = ip[i]; jj < ip[i + 1]; ++jj) {
-      const double2 h = v[jj];
-      double xr, xi;
-      if constexpr (MIXED) {
-        const float2 a =
-            reinterpret_cast<const float2*>(x)[(int64_t)ix[jj] * Rpad + r];
-        xr = a.x;
-        xi = a.y;
-      } else {
-        const double2 a =
-            reinterpret_cast<const double2*>(x)[(int64_t)ix[jj] * Rpad + r];
-        xr = a.x;
-        xi = a.y;
-      }
-      yr = fma(h.x, xr, fma(-h.y, xi, yr));
-      yi = fma(h.x, xi, fma(h.y, xr, yi));
+      const V2 h = V[jj];
+      const V2 a = X[(int64_t)ix[jj] * Rpad + r];
+      yr = fma(h.x, a.x, fma(-h.y, a.y, yr));
+      yi = fma(h.x, a.y, fma(h.y, a.x, yi));
     }
   }
   store_put<STORE>(dst, idx, yr, yi);
@@ -76,33 +83,23 @@ template <bool MIXED>
 __global__ void spmm_block_kernel(int64_t rows, int64_t Rpad,
                                   const int32_t* __restrict__ ip,
                                   const int32_t* __restrict__ ix,
-                                  const double2* __restrict__ v,
+                                  const void* __restrict__ vals,
                                   const void* __restrict__ x, void* y) {
+  using S = typename CT<MIXED>::S;
+  using V2 = typename CT<MIXED>::V2;
   const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= rows * Rpad) return;
   const int64_t i = idx / Rpad, r = idx % Rpad;
-  double yr = 0.0, yi = 0.0;
+  const V2* __restrict__ X = reinterpret_cast<const V2*>(x);
+  const V2* __restrict__ V = reinterpret_cast<const V2*>(vals);
+  S yr = 0, yi = 0;
   for (int jj = ip[i]; jj < ip[i + 1]; ++jj) {
-    const double2 h = v[jj];
-    double xr, xi;
-    if constexpr (MIXED) {
-      const float2 a =
-          reinterpret_cast<const float2*>(x)[(int64_t)ix[jj] * Rpad + r];
-      xr = a.x;
-      xi = a.y;
-    } else {
-      const double2 a =
-          reinterpret_cast<const double2*>(x)[(int64_t)ix[jj] * Rpad + r];
-      xr = a.x;
-      xi = a.y;
-    }
-    yr = fma(h.x, xr, fma(-h.y, xi, yr));
-    yi = fma(h.x, xi, fma(h.y, xr, yi));
+    const V2 h = V[jj];
+    const V2 a = X[(int64_t)ix[jj] * Rpad + r];
+    yr = fma(h.x, a.x, fma(-h.y, a.y, yr));
+    yi = fma(h.x, a.y, fma(h.y, a.x, yi));
   }
-  if constexpr (MIXED)
-    reinterpret_cast<float2*>(y)[idx] = make_float2((float)yr, (float)yi);
-  else
-    reinterpret_cast<double2*>(y)[idx] = make_double2(yr, yi);
+  reinterpret_cast<V2*>(y)[idx] = CT<MIXED>::make(yr, yi);
 }
 
 template <int STORE>
@@ -113,7 +110,7 @@ static int put_row(kpm_handle* h, const Matrix* V, const void* x, int64_t N,
   const bool mixed = h->precision == KPM_PREC_MIXED;
   const int32_t* ip = V ? V->indptr : nullptr;
   const int32_t* ix = V ? V->indices : nullptr;
-  const double2* vv = V ? (const double2*)V->data : nullptr;
+  const void* vv = V ? V->data : nullptr;
   if (mixed)
     spmm_to_store_kernel<true, STORE><<<grid, 256, 0, h->stream>>>(
         N, R, Rpad, ip, ix, vv, x, dst);
@@ -201,8 +198,10 @@ int kpm_correlator_moments(kpm_handle* h, double a2, double b2,
   Matrix Va, Vb;
   kpm_block *bR = nullptr, *bL = nullptr;
   Store psi, omega;
-  int st = upload_matrix_for(h, v_alpha, 0.0, &Va);
-  if (st == KPM_OK) st = upload_matrix_for(h, v_beta, 0.0, &Vb);
+  // operators in the recursion's precision (complex64 values in mixed mode)
+  const double vscale = h->precision == KPM_PREC_MIXED ? 1.0 : 0.0;
+  int st = upload_matrix_for(h, v_alpha, vscale, &Va, false);
+  if (st == KPM_OK) st = upload_matrix_for(h, v_beta, vscale, &Vb, false);
   const int kind = gemm == 0 ? STORE_C128 : STORE_BF16X3;
   if (st == KPM_OK) st = store_alloc(&psi, kind, M, K, s);
   if (st == KPM_OK) st = store_alloc(&omega, kind, M, K, s);
@@ -222,12 +221,10 @@ int kpm_correlator_moments(kpm_handle* h, double a2, double b2,
       const int64_t n = N * bR->Rpad;
       if (h->precision == KPM_PREC_MIXED)
         spmm_block_kernel<true><<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(
-            N, bR->Rpad, Va.indptr, Va.indices, (const double2*)Va.data,
-            bR->a0, a0L);
+            N, bR->Rpad, Va.indptr, Va.indices, Va.data, bR->a0, a0L);
       else
         spmm_block_kernel<false><<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(
-            N, bR->Rpad, Va.indptr, Va.indices, (const double2*)Va.data,
-            bR->a0, a0L);
+            N, bR->Rpad, Va.indptr, Va.indices, Va.data, bR->a0, a0L);
       count_launch(1);
       if (cudaGetLastError() != cudaSuccess) {
         set_error("kpm_correlator_moments: spmm launch failed");

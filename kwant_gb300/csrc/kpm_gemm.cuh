@@ -39,11 +39,11 @@ __device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& hi,
   lo = __float2bfloat16_rn(x - __bfloat162float(hi));
 }
 
-template <int STORE>
-__device__ __forceinline__ void store_put(const StoreRow& r, int64_t k,
-                                          double re, double im) {
+template <int STORE, typename S>
+__device__ __forceinline__ void store_put(const StoreRow& r, int64_t k, S re,
+                                          S im) {
   if constexpr (STORE == STORE_C128) {
-    r.c128[k] = make_double2(re, im);
+    r.c128[k] = make_double2((double)re, (double)im);
   } else {
     __nv_bfloat16 h, l;
     split_bf16((float)re, h, l);

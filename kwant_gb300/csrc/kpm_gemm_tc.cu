@@ -35,8 +35,6 @@ namespace kpm {
 namespace tc {
 
 constexpr int TM = 128;          // output rows per CTA (MMA M)
-constexpr int KC = 32;           // K elements per stage (64 bytes of bf16)
-constexpr int STAGES = 2;
 constexpr int THREADS = 128;
 constexpr uint64_t WAIT_NS = 2000000000ull;  // bounded waits: 2 s
 
@@ -100,15 +98,30 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map,
       : "memory");
 }
 
-// Shared-memory matrix descriptor: K-major, 64-byte swizzle, 8-row groups
-// 512 bytes apart (stride byte offset), version 1.
+// Per-stage K width: rows of KC bf16 = 2*KC bytes, swizzled over that width
+// (64 B -> 2 stages, 32 B -> 4 stages in the same shared memory).
+template <int KC> struct Stage;
+template <> struct Stage<32> {
+  static constexpr int STAGES = 2;
+  static constexpr uint64_t LAYOUT = 4;   // descriptor: 64-byte swizzle
+  static constexpr uint32_t SBO = 512;    // 8 rows x 64 B
+};
+template <> struct Stage<16> {
+  static constexpr int STAGES = 4;
+  static constexpr uint64_t LAYOUT = 6;   // descriptor: 32-byte swizzle
+  static constexpr uint32_t SBO = 256;    // 8 rows x 32 B
+};
+
+// Shared-memory matrix descriptor: K-major, swizzled rows of 2*KC bytes,
+// 8-row groups SBO bytes apart (stride byte offset), version 1.
+template <int KC>
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
   uint64_t d = 0;
   d |= (uint64_t)((addr & 0x3FFFF) >> 4);      // start address
   d |= (uint64_t)1 << 16;                       // leading byte offset (unused)
-  d |= (uint64_t)(512 >> 4) << 32;              // stride byte offset
+  d |= (uint64_t)(Stage<KC>::SBO >> 4) << 32;   // stride byte offset
   d |= (uint64_t)1 << 46;                       // descriptor version
-  d |= (uint64_t)4 << 61;                       // swizzle: 64B
+  d |= Stage<KC>::LAYOUT << 61;                 // swizzle mode
   return d;
 }
 
@@ -151,16 +164,18 @@ struct TcArgs {
   int* err;
 };
 
+template <int KC>
 __global__ void __launch_bounds__(THREADS, 1)
 bf16x3_tc_kernel(const __grid_constant__ CUtensorMap map_a,
                  const __grid_constant__ CUtensorMap map_b, TcArgs args) {
+  constexpr int STAGES = Stage<KC>::STAGES;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   // align the dynamic shared memory to 1024 bytes (swizzle atoms)
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int nt = args.nt;
-  const uint32_t a_bytes = 4 * TM * KC * 2;   // 32 KB
-  const uint32_t b_bytes = 4 * nt * KC * 2;   // up to 64 KB
+  const uint32_t a_bytes = 4 * TM * KC * 2;   // 4 planes x 128 rows
+  const uint32_t b_bytes = 4 * nt * KC * 2;   // 4 planes x nt rows
   uint8_t* sa = smem;                          // STAGES x a_bytes
   uint8_t* sb = smem + STAGES * a_bytes;       // STAGES x b_bytes
   uint64_t* full = reinterpret_cast<uint64_t*>(sb + STAGES * b_bytes);
@@ -229,16 +244,16 @@ bf16x3_tc_kernel(const __grid_constant__ CUtensorMap map_a,
       const uint32_t b0 = smem_u32(sb + s * b_bytes);
 #pragma unroll
       for (int ks = 0; ks < KC / 16; ++ks) {
-        const uint32_t ko = ks * 32;  // bytes along K inside the 64-B rows
+        const uint32_t ko = ks * 32;  // bytes along K inside a row
         // planes: 0 re_hi, 1 re_lo, 2 im_hi, 3 im_lo
-        const uint64_t Arh = smem_desc(a0 + 0 * plane_a + ko);
-        const uint64_t Arl = smem_desc(a0 + 1 * plane_a + ko);
-        const uint64_t Aih = smem_desc(a0 + 2 * plane_a + ko);
-        const uint64_t Ail = smem_desc(a0 + 3 * plane_a + ko);
-        const uint64_t Brh = smem_desc(b0 + 0 * plane_b + ko);
-        const uint64_t Brl = smem_desc(b0 + 1 * plane_b + ko);
-        const uint64_t Bih = smem_desc(b0 + 2 * plane_b + ko);
-        const uint64_t Bil = smem_desc(b0 + 3 * plane_b + ko);
+        const uint64_t Arh = smem_desc<KC>(a0 + 0 * plane_a + ko);
+        const uint64_t Arl = smem_desc<KC>(a0 + 1 * plane_a + ko);
+        const uint64_t Aih = smem_desc<KC>(a0 + 2 * plane_a + ko);
+        const uint64_t Ail = smem_desc<KC>(a0 + 3 * plane_a + ko);
+        const uint64_t Brh = smem_desc<KC>(b0 + 0 * plane_b + ko);
+        const uint64_t Brl = smem_desc<KC>(b0 + 1 * plane_b + ko);
+        const uint64_t Bih = smem_desc<KC>(b0 + 2 * plane_b + ko);
+        const uint64_t Bil = smem_desc<KC>(b0 + 3 * plane_b + ko);
         const uint32_t acc0 = (i > 0 || ks > 0) ? 1u : 0u;
         // Re += Ar Br + Ai Bi
         mma_bf16(d_re, Arh, Brh, id_pos, acc0);
@@ -337,7 +352,9 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 3D map over the four planes of a store: dims {Kp, M, 4}, box {KC, rows, 4}
+// 3D map over the four planes of a store: dims {Kp, M, 4}, box {KC, rows, 4},
+// swizzled over the 2*KC-byte rows.
+template <int KC>
 static int make_map(CUtensorMap* map, const Store* s, int box_rows) {
   auto fn = encode_fn();
   if (!fn) {
@@ -351,7 +368,9 @@ static int make_map(CUtensorMap* map, const Store* s, int box_rows) {
   cuuint32_t estr[3] = {1, 1, 1};
   CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, s->planes, dims,
                   strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                  CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  KC == 32 ? CU_TENSOR_MAP_SWIZZLE_64B
+                           : CU_TENSOR_MAP_SWIZZLE_32B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
     set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
@@ -362,9 +381,12 @@ static int make_map(CUtensorMap* map, const Store* s, int box_rows) {
 
 }  // namespace tc
 
-int gemm_bf16x3_tc(kpm_handle* h, const Store* omega, const Store* psi,
-                   int64_t M, int64_t K, int64_t R, double* mu_host) {
+template <int KC>
+static int gemm_bf16x3_tc_kc(kpm_handle* h, const Store* omega,
+                             const Store* psi, int64_t M, int64_t R,
+                             double* mu_host) {
   using namespace tc;
+  constexpr int STAGES = Stage<KC>::STAGES;
   KPM_REQUIRE(omega->kind == STORE_BF16X3 && psi->kind == STORE_BF16X3,
               "tensor-core contraction needs BF16x3 stores");
   KPM_REQUIRE(omega->Kp % KC == 0 && omega->Kp == psi->Kp,
@@ -385,13 +407,13 @@ int gemm_bf16x3_tc(kpm_handle* h, const Store* omega, const Store* psi,
   splits = (int)ceil_div(kchunks, c_per);
 
   CUtensorMap map_a, map_b;
-  KPM_TRY(make_map(&map_a, omega, TM));
-  KPM_TRY(make_map(&map_b, psi, nt));
+  KPM_TRY(make_map<KC>(&map_a, omega, TM));
+  KPM_TRY(make_map<KC>(&map_b, psi, nt));
 
   const size_t a_bytes = 4 * TM * KC * 2, b_bytes = (size_t)4 * nt * KC * 2;
   const size_t smem = 1024 + STAGES * (a_bytes + b_bytes) +
                       (2 * STAGES + 1) * 8 + 16;
-  KPM_CUDA(cudaFuncSetAttribute(bf16x3_tc_kernel,
+  KPM_CUDA(cudaFuncSetAttribute(bf16x3_tc_kernel<KC>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem));
   float2* part = nullptr;
@@ -408,8 +430,8 @@ int gemm_bf16x3_tc(kpm_handle* h, const Store* omega, const Store* psi,
   if (st == KPM_OK && e == cudaSuccess) {
     TcArgs args{M, kchunks, splits, nt, ntiles_n, tmem_cols, part, err};
     cudaEventRecord(h->ev_gemm0, h->stream);
-    bf16x3_tc_kernel<<<(unsigned)(tiles * splits), THREADS, smem,
-                       h->stream>>>(map_a, map_b, args);
+    bf16x3_tc_kernel<KC><<<(unsigned)(tiles * splits), THREADS, smem,
+                           h->stream>>>(map_a, map_b, args);
     count_launch(1);
     e = cudaGetLastError();
     cudaEventRecord(h->ev_gemm1, h->stream);
@@ -455,7 +477,10 @@ int gemm_bf16x3_tc(kpm_handle* h, const Store* omega, const Store* psi,
 
 int gemm_bf16x3(kpm_handle* h, const Store* omega, const Store* psi,
                 int64_t M, int64_t K, int64_t R, double* mu_host) {
-  return gemm_bf16x3_tc(h, omega, psi, M, K, R, mu_host);
+  (void)K;
+  if (h->tc_kc == 32)
+    return gemm_bf16x3_tc_kc<32>(h, omega, psi, M, R, mu_host);
+  return gemm_bf16x3_tc_kc<16>(h, omega, psi, M, R, mu_host);
 }
 
 }  // namespace kpm

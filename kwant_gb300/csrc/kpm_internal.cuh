@@ -32,12 +32,12 @@ int validate_csr(const kpm_csr_desc* m);
 // CSR upload.  scale == 0 keeps complex128 values; otherwise values are
 // stored as complex64 multiplied by scale.
 int upload_matrix(kpm_handle* h, const kpm_csr_desc* m, double scale,
-                  Matrix* out);
+                  Matrix* out, bool with_ell = true);
 void free_matrix(Matrix* m, cudaStream_t s);
 // upload_matrix in the handle's row order (reordered handles permute rows
 // and columns)
 int upload_matrix_for(kpm_handle* h, const kpm_csr_desc* m, double scale,
-                      Matrix* out);
+                      Matrix* out, bool with_ell = true);
 // compute the RCM order of m, set h->perm / h->h_iperm, and return the
 // permuted CSR arrays
 int setup_reorder(kpm_handle* h, const kpm_csr_desc* m,

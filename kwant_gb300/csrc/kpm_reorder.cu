@@ -89,8 +89,8 @@ void permute_csr(const kpm_csr_desc* m, const std::vector<int32_t>& perm,
 }
 
 int upload_matrix_for(kpm_handle* h, const kpm_csr_desc* m, double scale,
-                      Matrix* out) {
-  if (!h->perm) return upload_matrix(h, m, scale, out);
+                      Matrix* out, bool with_ell) {
+  if (!h->perm) return upload_matrix(h, m, scale, out, with_ell);
   KPM_REQUIRE(m->rows == (int64_t)h->h_iperm.size(),
               "matrix size does not match the handle");
   // validate before permuting (the permutation indexes with the columns)
@@ -107,7 +107,7 @@ int upload_matrix_for(kpm_handle* h, const kpm_csr_desc* m, double scale,
   std::vector<double> data;
   permute_csr(m, perm, h->h_iperm, ip, ix, data);
   kpm_csr_desc pd{m->rows, m->nnz, ip.data(), ix.data(), data.data()};
-  return upload_matrix(h, &pd, scale, out);
+  return upload_matrix(h, &pd, scale, out, with_ell);
 }
 
 int setup_reorder(kpm_handle* h, const kpm_csr_desc* m,
