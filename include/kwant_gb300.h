@@ -211,6 +211,50 @@ KPM_API int kpm_dos_moments_noalloc(const kpm_device_csr* ham, double a,
                                     int64_t R, int64_t M, void* work,
                                     double* moments, void* stream);
 
+/* ---- batched multi-system DOS ------------------------------------------------
+ * Many independent systems (disorder realisations, parameter points,
+ * lattices of different size) advanced together: every Chebyshev step of all
+ * systems is one launch (work items of all systems in one index space), and
+ * the whole step loop is captured once in a CUDA graph and replayed.  The
+ * matrices are block-sparse with 4 x 4 blocks (BSR4), the recursion is
+ * complex64 with FP64 moment accumulation, and the R random-phase vectors of
+ * every system come from a counter-based generator on the device (SplitMix64
+ * of (seed, system, vector, orbital); u = top 24 bits / 2^24, vector entry
+ * exp(2 pi i u)), not from the reference's MT19937 stream.  Replaces running
+ * SpectralDensity (kwant/kpm.py:163-252) once per realisation. */
+typedef struct kpm_batch kpm_batch;
+typedef struct kpm_bsr_desc {
+  int64_t block_rows;      /* orbitals = 4 * block_rows */
+  int64_t nnzb;
+  const int32_t* indptr;   /* block_rows + 1 */
+  const int32_t* indices;  /* nnzb block columns */
+  const double* data;      /* nnzb row-major 4x4 blocks, complex128 */
+} kpm_bsr_desc;
+KPM_API int kpm_batch_create(int64_t num_vectors, int64_t num_moments,
+                             uint64_t seed, kpm_batch** out);
+/* Add a system given as a host BSR4 matrix with its rescaling (a, b). */
+KPM_API int kpm_batch_add_bsr(kpm_batch* bt, const kpm_bsr_desc* ham,
+                              double a, double b);
+/* Add an L^3 Wilson-Dirac system generated on the device: onsite
+ * (m - 3) G0 + w 1, hopping H[r + e_j, r] = (G0 - i Gj) / 2, open
+ * boundaries, G0 = tau_z (x) sigma_0, Gj = tau_x (x) sigma_j; disorder
+ * w = W (u - 1/2), u = SplitMix64(seed, site) / 2^64 (53 bits).  Rescaled
+ * with (a, b). */
+KPM_API int kpm_batch_add_wilson_dirac(kpm_batch* bt, int64_t L, double m,
+                                       double W, uint64_t seed, double a,
+                                       double b);
+/* Run the DOS recursion of every system (moments averaged over the R
+ * vectors): out is num_systems x num_moments complex128.  The first call
+ * allocates the vectors, picks the kernel variant (autotuner over variants
+ * with identical arithmetic) and captures the step loop in a CUDA graph;
+ * later calls replay the graph. */
+KPM_API int kpm_batch_run(kpm_batch* bt, double* out);
+/* Device time (ms) of the last kpm_batch_run's graph and the number of
+ * kernel nodes it contains; the chosen variant (vectors per lane). */
+KPM_API int kpm_batch_stats(kpm_batch* bt, double* ms, int64_t* nodes,
+                            int* vectors_per_lane);
+KPM_API int kpm_batch_destroy(kpm_batch* bt);
+
 /* ---- reconstruction (device) -------------------------------------------------
  * _moments + _calc_fft_moments, kwant/kpm.py:378-388 and :1197-1222:
  * moments (R x M x W complex128, host) -> mean over R (if mean) -> / a ->

@@ -56,6 +56,12 @@ class CsrDesc(C.Structure):
                 ('data', C.c_void_p)]
 
 
+class BsrDesc(C.Structure):
+    _fields_ = [('block_rows', C.c_int64), ('nnzb', C.c_int64),
+                ('indptr', C.c_void_p), ('indices', C.c_void_p),
+                ('data', C.c_void_p)]
+
+
 class OpDesc(C.Structure):
     _fields_ = [('num_terms', C.c_int64), ('num_outputs', C.c_int64),
                 ('num_chunks', C.c_int64), ('term_row', C.c_void_p),
@@ -103,6 +109,12 @@ def _load():
         'kpm_last_kernel_ms': [P, P],
         'kpm_dos_moments_noalloc': [P, D, D, I, P, I64, I64, P, P, P],
         'kpm_last_gemm': [P, P, P],
+        'kpm_batch_create': [I64, I64, C.c_uint64, P],
+        'kpm_batch_add_bsr': [P, P, D, D],
+        'kpm_batch_add_wilson_dirac': [P, I64, D, D, C.c_uint64, D, D],
+        'kpm_batch_run': [P, P],
+        'kpm_batch_stats': [P, P, P, P],
+        'kpm_batch_destroy': [P],
         'kpm_profile': [P, I],
         'kpm_profile_read': [P, P, P],
         'kpm_launch_count': [P],
@@ -383,3 +395,54 @@ def dos(csr, a, b, precision, vecs, M, kernel=KERNEL_JACKSON):
     check(lib.kpm_dos(csr.ref(), float(a), float(b), precision, ptr(vecs), R,
                       M, kernel, ptr(mom), ptr(gam), ptr(rho)))
     return mom, gam, rho
+
+
+class Batch:
+    """Many systems advanced together (kpm_batch_* C ABI)."""
+
+    def __init__(self, num_vectors, num_moments, seed=0):
+        b = C.c_void_p()
+        check(lib.kpm_batch_create(int(num_vectors), int(num_moments),
+                                   C.c_uint64(int(seed) & (2**64 - 1)),
+                                   C.byref(b)))
+        self._b = b
+        self.R, self.M = int(num_vectors), int(num_moments)
+        self.num_systems = 0
+        self._keep = []
+
+    def add_bsr(self, bsr, a, b):
+        import scipy.sparse as sp
+        m = sp.bsr_matrix(bsr, blocksize=(4, 4))
+        m.sort_indices()
+        indptr = np.ascontiguousarray(m.indptr, dtype=np.int32)
+        indices = np.ascontiguousarray(m.indices, dtype=np.int32)
+        data = np.ascontiguousarray(m.data, dtype=np.complex128)
+        d = BsrDesc(m.shape[0] // 4, len(indices), ptr(indptr), ptr(indices),
+                    ptr(data))
+        check(lib.kpm_batch_add_bsr(self._b, C.byref(d), float(a), float(b)))
+        self.num_systems += 1
+
+    def add_wilson_dirac(self, L, m, W, seed, a, b):
+        check(lib.kpm_batch_add_wilson_dirac(
+            self._b, int(L), float(m), float(W),
+            C.c_uint64(int(seed) & (2**64 - 1)), float(a), float(b)))
+        self.num_systems += 1
+
+    def run(self):
+        out = np.empty((self.num_systems, self.M), dtype=np.complex128)
+        check(lib.kpm_batch_run(self._b, ptr(out)))
+        return out
+
+    def stats(self):
+        ms, nodes, vpl = C.c_double(), C.c_int64(), C.c_int()
+        check(lib.kpm_batch_stats(self._b, C.byref(ms), C.byref(nodes),
+                                  C.byref(vpl)))
+        return ms.value, nodes.value, vpl.value
+
+    def close(self):
+        if getattr(self, '_b', None):
+            lib.kpm_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        self.close()

@@ -1,0 +1,738 @@
+// Batched multi-system KPM DOS on block-sparse (4 x 4) Hamiltonians.
+//
+// Many disorder realisations / lattices of different size are advanced
+// together: one launch per Chebyshev step covers every system (the work
+// items of all systems form one index space, found by binary search over a
+// prefix array), and the step loop of a run is captured once into a CUDA
+// graph and replayed.  Replaces one SpectralDensity per realisation
+// (kwant/kpm.py:163-252) for the batched-realisation workload.
+//
+// BSR4 step: a 16-lane slot owns one block row (4 orbitals) for a group of
+// 16 * VPL vectors; each lane holds VPL vectors (8 or 16 bytes) of all four
+// orbital rows.  Blocks are stored ELL-style, KB = 8 per block row, the
+// diagonal block first with the -2b/a shift folded in (so the first
+// neighbour rows loaded are the row's own entries, reused for the DOS dot
+// products), padding blocks are zero and point at the row itself.
+// Arithmetic per vector is independent of VPL (same FMA order, same flush
+// points, same reduction order), so the autotuner's choice of VPL never
+// changes results.
+//
+// Random-phase vectors: counter-based SplitMix64 (Steele, Lea & Flood 2014;
+// Vigna's constants) of (seed, system, vector) then orbital; the top 24 bits
+// give u in [0, 1) and the entry is exp(2 pi i u).
+
+#include <algorithm>
+#include <vector>
+
+#include "kpm_common.cuh"
+#include "kpm_internal.cuh"
+
+namespace kpm {
+namespace bt {
+
+constexpr int KB = 8;            // blocks per block row
+constexpr int BS = 4;            // block size
+
+__host__ __device__ inline uint64_t mix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+struct SysDev {
+  int64_t nb;            // block rows
+  int xitems;            // row partitions (depends only on nb)
+  const int32_t* bidx;   // [nb][KB]
+  const float2* bval;    // [nb][KB][16], 2 (H - b) / a
+  void* v[3];            // a0, b0, b1: [4 nb][Rpad] complex64
+  double* partials;      // [Rpad * 3][xitems]
+  double2* mu01;         // [Rpad][2]
+  double2* mom;          // [M][Rpad]
+};
+
+template <int VPL> struct Pay;
+template <> struct Pay<1> { using T = float2; };
+template <> struct Pay<2> { using T = float4; };
+
+// complex MAC of block entry h (float2) into acc (re, im) for one vector
+__device__ __forceinline__ void cmac(float& ar, float& ai, float hr, float hi,
+                                     float xr, float xi) {
+  ar = fmaf(hr, xr, ar);
+  ar = fmaf(-hi, xi, ar);
+  ai = fmaf(hr, xi, ai);
+  ai = fmaf(hi, xr, ai);
+}
+
+// PHASE 0: x = a0 -> b0 (first step); 1: x = b0, prev = a0 -> b1;
+// 2: x = b1, prev = b0 -> b0; 3: x = b0, prev = b1 -> b1.
+template <int VPL, int PHASE>
+__global__ void __launch_bounds__(STEP_THREADS, VPL == 1 ? 4 : 3)
+bsr_step_kernel(const SysDev* __restrict__ sys,
+                const int64_t* __restrict__ prefix, int nsys, int64_t total,
+                int64_t Rpad) {
+  using PT = typename Pay<VPL>::T;
+  constexpr int G = 16 * VPL;
+  constexpr int FLUSH = 8;       // block rows (32 orbital rows)
+  const int lane = threadIdx.x & 15;
+  const int slot = threadIdx.x >> 4;
+  __shared__ double red[SLOTS][G * 3];
+  const int64_t groups = Rpad / G;
+  const int64_t rp = Rpad / VPL;
+
+  for (int64_t w = blockIdx.x; w < total; w += gridDim.x) {
+    int lo = 0, hi = nsys;   // largest s with prefix[s] <= w
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (prefix[mid] <= w) lo = mid; else hi = mid;
+    }
+    const SysDev& S = sys[lo];
+    const int64_t local = w - prefix[lo];
+    const int xi = (int)(local / groups);
+    const int g = (int)(local - (int64_t)xi * groups);
+    const int64_t col = (int64_t)g * 16 + lane;
+    const PT* __restrict__ X;
+    const PT* P = nullptr;
+    PT* O;
+    if constexpr (PHASE == 0) {
+      X = (const PT*)S.v[0]; O = (PT*)S.v[1];
+    } else if constexpr (PHASE == 1) {
+      X = (const PT*)S.v[1]; P = (const PT*)S.v[0]; O = (PT*)S.v[2];
+    } else if constexpr (PHASE == 2) {
+      X = (const PT*)S.v[2]; P = (const PT*)S.v[1]; O = (PT*)S.v[1];
+    } else {
+      X = (const PT*)S.v[1]; P = (const PT*)S.v[2]; O = (PT*)S.v[2];
+    }
+    double* my = &red[slot][lane * VPL * 3];
+#pragma unroll
+    for (int e = 0; e < VPL * 3; ++e) my[e] = 0.0;
+    float fn[VPL], fr[VPL], fi[VPL];
+#pragma unroll
+    for (int k = 0; k < VPL; ++k) fn[k] = fr[k] = fi[k] = 0.f;
+    int pending = 0;
+    const int64_t stride = (int64_t)S.xitems * SLOTS;
+
+    for (int64_t i = (int64_t)xi * SLOTS + slot; i < S.nb; i += stride) {
+      float acc[BS][VPL][2];
+#pragma unroll
+      for (int rr = 0; rr < BS; ++rr)
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) acc[rr][k][0] = acc[rr][k][1] = 0.f;
+      PT xo[BS];
+#pragma unroll 1
+      for (int q = 0; q < KB; ++q) {
+        const int64_t c = __ldg(S.bidx + i * KB + q);
+        PT xn[BS];
+#pragma unroll
+        for (int cc = 0; cc < BS; ++cc) xn[cc] = X[(c * BS + cc) * rp + col];
+        if (q == 0) {
+#pragma unroll
+          for (int cc = 0; cc < BS; ++cc) xo[cc] = xn[cc];
+        }
+        const float4* bv =
+            reinterpret_cast<const float4*>(S.bval + (i * KB + q) * 16);
+#pragma unroll
+        for (int rr = 0; rr < BS; ++rr) {
+          const float4 b01 = __ldg(bv + 2 * rr), b23 = __ldg(bv + 2 * rr + 1);
+          const float hr[4] = {b01.x, b01.z, b23.x, b23.z};
+          const float hi[4] = {b01.y, b01.w, b23.y, b23.w};
+#pragma unroll
+          for (int cc = 0; cc < BS; ++cc) {
+            if constexpr (VPL == 1) {
+              cmac(acc[rr][0][0], acc[rr][0][1], hr[cc], hi[cc], xn[cc].x,
+                   xn[cc].y);
+            } else {
+              cmac(acc[rr][0][0], acc[rr][0][1], hr[cc], hi[cc], xn[cc].x,
+                   xn[cc].y);
+              cmac(acc[rr][1][0], acc[rr][1][1], hr[cc], hi[cc], xn[cc].z,
+                   xn[cc].w);
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int rr = 0; rr < BS; ++rr) {
+        const int64_t orow = (i * BS + rr) * rp + col;
+        float o[VPL][2];
+        if constexpr (PHASE == 0) {
+#pragma unroll
+          for (int k = 0; k < VPL; ++k) {
+            o[k][0] = 0.5f * acc[rr][k][0];
+            o[k][1] = 0.5f * acc[rr][k][1];
+          }
+        } else {
+          const PT pv = P[orow];
+          if constexpr (VPL == 1) {
+            o[0][0] = acc[rr][0][0] - pv.x;
+            o[0][1] = acc[rr][0][1] - pv.y;
+          } else {
+            o[0][0] = acc[rr][0][0] - pv.x;
+            o[0][1] = acc[rr][0][1] - pv.y;
+            o[1][0] = acc[rr][1][0] - pv.z;
+            o[1][1] = acc[rr][1][1] - pv.w;
+          }
+        }
+        PT ov;
+        if constexpr (VPL == 1) {
+          ov = make_float2(o[0][0], o[0][1]);
+        } else {
+          ov = make_float4(o[0][0], o[0][1], o[1][0], o[1][1]);
+        }
+        O[orow] = ov;
+        // DOS dots of this vector: <x|x>, <o|x> (x = the row's own entries)
+        float xr[VPL], xim[VPL];
+        if constexpr (VPL == 1) {
+          xr[0] = xo[rr].x; xim[0] = xo[rr].y;
+        } else {
+          xr[0] = xo[rr].x; xim[0] = xo[rr].y;
+          xr[1] = xo[rr].z; xim[1] = xo[rr].w;
+        }
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) {
+          fn[k] = fmaf(xr[k], xr[k], fmaf(xim[k], xim[k], fn[k]));
+          fr[k] = fmaf(o[k][0], xr[k], fmaf(o[k][1], xim[k], fr[k]));
+          fi[k] = fmaf(o[k][0], xim[k], fmaf(-o[k][1], xr[k], fi[k]));
+        }
+      }
+      if (++pending == FLUSH) {
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) {
+          my[k * 3 + 0] += (double)fn[k];
+          my[k * 3 + 1] += (double)fr[k];
+          my[k * 3 + 2] += (double)fi[k];
+          fn[k] = fr[k] = fi[k] = 0.f;
+        }
+        pending = 0;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < VPL; ++k) {
+      my[k * 3 + 0] += (double)fn[k];
+      my[k * 3 + 1] += (double)fr[k];
+      my[k * 3 + 2] += (double)fi[k];
+    }
+    __syncthreads();
+    // partials [vector * 3 + component][partition]
+    double* dst = S.partials + (int64_t)g * G * 3 * S.xitems + xi;
+    for (int e = threadIdx.x; e < G * 3; e += blockDim.x) {
+      double s = 0.0;
+#pragma unroll
+      for (int q = 0; q < SLOTS; ++q) s += red[q][e];
+      dst[(int64_t)e * S.xitems] = s;
+    }
+    __syncthreads();
+  }
+}
+
+// grid (Rpad, nsys): fixed-order sums of the partials into DOS moments
+__global__ void bsr_finalize_kernel(const SysDev* __restrict__ sys,
+                                    int64_t Rpad, int mode, int64_t m_even,
+                                    int64_t m_odd) {
+  const int64_t v = blockIdx.x;
+  const SysDev& S = sys[blockIdx.y];
+  __shared__ double sh[3][128];
+  double acc[3] = {0.0, 0.0, 0.0};
+  const double* src = S.partials + v * 3 * (int64_t)S.xitems;
+  for (int xi = threadIdx.x; xi < S.xitems; xi += blockDim.x) {
+    acc[0] += src[xi];
+    acc[1] += src[S.xitems + xi];
+    acc[2] += src[2 * (int64_t)S.xitems + xi];
+  }
+  for (int c = 0; c < 3; ++c) sh[c][threadIdx.x] = acc[c];
+  __syncthreads();
+  for (int w = 64; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+      for (int c = 0; c < 3; ++c) sh[c][threadIdx.x] += sh[c][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x != 0) return;
+  const double nrm = sh[0][0], cre = sh[1][0], cim = sh[2][0];
+  if (mode == 0) {
+    const double2 m0 = make_double2(nrm, 0.0), m1 = make_double2(cre, -cim);
+    S.mu01[2 * v] = m0;
+    S.mu01[2 * v + 1] = m1;
+    S.mom[0 * Rpad + v] = m0;
+    S.mom[1 * Rpad + v] = m1;
+  } else {
+    const double2 m0 = S.mu01[2 * v], m1 = S.mu01[2 * v + 1];
+    S.mom[m_even * Rpad + v] = make_double2(2.0 * nrm - m0.x, 0.0 - m0.y);
+    S.mom[m_odd * Rpad + v] = make_double2(2.0 * cre - m1.x, 2.0 * cim - m1.y);
+  }
+}
+
+// out[s][m] = mean over the R real vectors (fixed order), grid (M, nsys)
+__global__ void bsr_mean_kernel(const SysDev* __restrict__ sys, int64_t R,
+                                int64_t Rpad, int64_t M, double2* out) {
+  const int64_t m = blockIdx.x;
+  const SysDev& S = sys[blockIdx.y];
+  __shared__ double sr[128], si[128];
+  double r = 0.0, im = 0.0;
+  for (int64_t v = threadIdx.x; v < R; v += blockDim.x) {
+    const double2 x = S.mom[m * Rpad + v];
+    r += x.x;
+    im += x.y;
+  }
+  sr[threadIdx.x] = r;
+  si[threadIdx.x] = im;
+  __syncthreads();
+  for (int w = 64; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      sr[threadIdx.x] += sr[threadIdx.x + w];
+      si[threadIdx.x] += si[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double inv = 1.0 / (double)R;
+    out[blockIdx.y * M + m] = make_double2(sr[0] * inv, si[0] * inv);
+  }
+}
+
+// random-phase starting vectors, complex64, zero padding vectors
+__global__ void rng_vectors_kernel(float2* __restrict__ a0, int64_t N,
+                                   int64_t R, int64_t Rpad, uint64_t key) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= N * Rpad) return;
+  const int64_t n = idx / Rpad, r = idx % Rpad;
+  float2 v = make_float2(0.f, 0.f);
+  if (r < R) {
+    const uint64_t h = mix64(mix64(key ^ (uint64_t)r) + (uint64_t)n);
+    const float u = (float)(h >> 40) * 0x1.0p-24f;
+    float s, c;
+    sincospif(2.0f * u, &s, &c);
+    v = make_float2(c, s);
+  }
+  a0[idx] = v;
+}
+
+struct WdBlocks {
+  float2 diag[16];          // (m - 3) G0 (before disorder, shift, scale)
+  float2 fwd[3][16];        // H[s, s + e_j] = T_j^dagger
+  float2 bwd[3][16];        // H[s, s - e_j] = T_j
+};
+
+// Wilson-Dirac BSR rows, scaled: 2 (H - b) / a
+__global__ void wd_generate_kernel(int64_t L, WdBlocks blk, double W,
+                                   uint64_t key, double scale, double shift,
+                                   int32_t* __restrict__ bidx,
+                                   float2* __restrict__ bval) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nb = L * L * L;
+  if (s >= nb) return;
+  const int64_t x = s / (L * L), y = (s / L) % L, z = s % L;
+  const uint64_t h = mix64(mix64(key ^ 0xD15C0ull) + (uint64_t)s);
+  const double w = W * ((double)(h >> 11) * 0x1.0p-53 - 0.5);
+  int q = 0;
+  auto put = [&](int64_t col, const float2* b, bool diag) {
+    bidx[s * KB + q] = (int32_t)col;
+    for (int e = 0; e < 16; ++e) {
+      double re = b ? b[e].x : 0.0, im = b ? b[e].y : 0.0;
+      if (diag && (e % 5 == 0)) re += w - shift;
+      bval[(s * KB + q) * 16 + e] =
+          make_float2((float)(re * scale), (float)(im * scale));
+    }
+    ++q;
+  };
+  put(s, blk.diag, true);
+  const int64_t coord[3] = {x, y, z};
+  const int64_t strides[3] = {L * L, L, 1};
+  for (int j = 0; j < 3; ++j) {
+    if (coord[j] + 1 < L) put(s + strides[j], blk.fwd[j], false);
+    if (coord[j] - 1 >= 0) put(s - strides[j], blk.bwd[j], false);
+  }
+  while (q < KB) put(s, nullptr, false);
+}
+
+}  // namespace bt
+}  // namespace kpm
+
+using namespace kpm;
+using namespace kpm::bt;
+
+struct kpm_batch {
+  int64_t R = 0, Rpad = 0, M = 0;
+  uint64_t seed = 0;
+  int device = 0, num_sms = 0;
+  cudaStream_t stream = nullptr;
+  struct Sys {
+    int64_t nb = 0;
+    double a = 1, b = 0;
+    int32_t* bidx = nullptr;
+    float2* bval = nullptr;
+    void* v[3] = {nullptr, nullptr, nullptr};
+    double* partials = nullptr;
+    double2* mu01 = nullptr;
+    double2* mom = nullptr;
+  };
+  std::vector<Sys> sys;
+  SysDev* d_sys = nullptr;
+  int64_t* d_prefix[2] = {nullptr, nullptr};  // VPL 1, 2
+  int64_t total[2] = {0, 0};
+  double2* d_out = nullptr;
+  int vpl = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int64_t nodes = 0;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  double last_ms = 0.0;
+  bool ready = false;
+};
+
+namespace {
+
+int batch_free(kpm_batch* bt) {
+  if (!bt) return KPM_OK;
+  cudaStream_t s = bt->stream;
+  if (bt->exec) cudaGraphExecDestroy(bt->exec);
+  if (bt->graph) cudaGraphDestroy(bt->graph);
+  for (auto& y : bt->sys) {
+    dev_free(y.bidx, s);
+    dev_free(y.bval, s);
+    for (int k = 0; k < 3; ++k) dev_free(y.v[k], s);
+    dev_free(y.partials, s);
+    dev_free(y.mu01, s);
+    dev_free(y.mom, s);
+  }
+  dev_free(bt->d_sys, s);
+  dev_free(bt->d_prefix[0], s);
+  dev_free(bt->d_prefix[1], s);
+  dev_free(bt->d_out, s);
+  if (s) {
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+  }
+  if (bt->e0) cudaEventDestroy(bt->e0);
+  if (bt->e1) cudaEventDestroy(bt->e1);
+  cudaGetLastError();
+  delete bt;
+  return KPM_OK;
+}
+
+template <int VPL, int PHASE>
+int launch_bsr(kpm_batch* bt) {
+  static int occ = -1;
+  if (occ < 0) {
+    int blocks = 0;
+    KPM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &blocks, bsr_step_kernel<VPL, PHASE>, STEP_THREADS, 0));
+    occ = blocks > 0 ? blocks : 1;
+  }
+  const int64_t total = bt->total[VPL - 1];
+  int64_t grid = (int64_t)occ * bt->num_sms;
+  if (grid > total) grid = total;
+  bsr_step_kernel<VPL, PHASE><<<(unsigned)grid, STEP_THREADS, 0, bt->stream>>>(
+      bt->d_sys, bt->d_prefix[VPL - 1], (int)bt->sys.size(), total, bt->Rpad);
+  count_launch(1);
+  KPM_CHECK_LAUNCH();
+  return KPM_OK;
+}
+
+template <int VPL>
+int launch_phase(kpm_batch* bt, int phase) {
+  switch (phase) {
+    case 0: return launch_bsr<VPL, 0>(bt);
+    case 1: return launch_bsr<VPL, 1>(bt);
+    case 2: return launch_bsr<VPL, 2>(bt);
+    default: return launch_bsr<VPL, 3>(bt);
+  }
+}
+
+int launch_step_phase(kpm_batch* bt, int vpl, int phase) {
+  return vpl == 1 ? launch_phase<1>(bt, phase) : launch_phase<2>(bt, phase);
+}
+
+int finalize_all(kpm_batch* bt, int mode, int64_t me, int64_t mo) {
+  dim3 grid((unsigned)bt->Rpad, (unsigned)bt->sys.size());
+  bsr_finalize_kernel<<<grid, 128, 0, bt->stream>>>(bt->d_sys, bt->Rpad, mode,
+                                                    me, mo);
+  count_launch(1);
+  KPM_CHECK_LAUNCH();
+  return KPM_OK;
+}
+
+// Enqueue one complete DOS run (steps + finalizes + means) on the stream.
+int enqueue_run(kpm_batch* bt, int vpl) {
+  KPM_TRY(launch_step_phase(bt, vpl, 0));
+  KPM_TRY(finalize_all(bt, 0, 0, 1));
+  for (int64_t n = 1; n < bt->M / 2; ++n) {
+    const int phase = n == 1 ? 1 : (n % 2 == 0 ? 2 : 3);
+    KPM_TRY(launch_step_phase(bt, vpl, phase));
+    KPM_TRY(finalize_all(bt, 1, 2 * n, 2 * n + 1));
+  }
+  dim3 grid((unsigned)bt->M, (unsigned)bt->sys.size());
+  bsr_mean_kernel<<<grid, 128, 0, bt->stream>>>(bt->d_sys, bt->R, bt->Rpad,
+                                                bt->M, bt->d_out);
+  count_launch(1);
+  KPM_CHECK_LAUNCH();
+  return KPM_OK;
+}
+
+int prepare(kpm_batch* bt) {
+  cudaStream_t s = bt->stream;
+  const int S = (int)bt->sys.size();
+  KPM_REQUIRE(S > 0, "kpm_batch_run: no systems added");
+  std::vector<SysDev> hs(S);
+  std::vector<int64_t> pre[2] = {std::vector<int64_t>(S + 1, 0),
+                                 std::vector<int64_t>(S + 1, 0)};
+  for (int i = 0; i < S; ++i) {
+    auto& y = bt->sys[i];
+    const int64_t N = y.nb * BS;
+    const size_t vb = (size_t)N * bt->Rpad * sizeof(float2);
+    for (int k = 0; k < 3; ++k) KPM_TRY(dev_alloc(&y.v[k], vb, s));
+    const int xitems = xitems_for_rows(y.nb);
+    KPM_TRY(dev_alloc((void**)&y.partials,
+                      (size_t)bt->Rpad * 3 * xitems * sizeof(double), s));
+    KPM_TRY(dev_alloc((void**)&y.mu01, (size_t)bt->Rpad * 2 * 16, s));
+    KPM_TRY(dev_alloc((void**)&y.mom, (size_t)bt->M * bt->Rpad * 16, s));
+    // starting vectors: (seed, system) key
+    const uint64_t key = mix64(bt->seed ^ ((uint64_t)i << 32));
+    rng_vectors_kernel<<<(unsigned)ceil_div(N * bt->Rpad, 256), 256, 0, s>>>(
+        (float2*)y.v[0], N, bt->R, bt->Rpad, key);
+    count_launch(1);
+    KPM_CHECK_LAUNCH();
+    hs[i] = SysDev{y.nb, xitems, y.bidx, y.bval,
+                   {y.v[0], y.v[1], y.v[2]}, y.partials, y.mu01, y.mom};
+    for (int v = 0; v < 2; ++v)
+      pre[v][i + 1] = pre[v][i] + (int64_t)xitems * (bt->Rpad / (16 * (v + 1)));
+  }
+  KPM_TRY(dev_alloc((void**)&bt->d_sys, S * sizeof(SysDev), s));
+  KPM_CUDA(cudaMemcpyAsync(bt->d_sys, hs.data(), S * sizeof(SysDev),
+                           cudaMemcpyHostToDevice, s));
+  for (int v = 0; v < 2; ++v) {
+    KPM_TRY(dev_alloc((void**)&bt->d_prefix[v], (S + 1) * sizeof(int64_t), s));
+    KPM_CUDA(cudaMemcpyAsync(bt->d_prefix[v], pre[v].data(),
+                             (S + 1) * sizeof(int64_t),
+                             cudaMemcpyHostToDevice, s));
+    bt->total[v] = pre[v][S];
+  }
+  KPM_TRY(dev_alloc((void**)&bt->d_out, (size_t)S * bt->M * 16, s));
+  KPM_CUDA(cudaEventCreate(&bt->e0));
+  KPM_CUDA(cudaEventCreate(&bt->e1));
+  KPM_CUDA(cudaStreamSynchronize(s));
+
+  // autotuner: time three steps of each variant (identical arithmetic)
+  float best = 1e30f;
+  for (int vpl = 1; vpl <= 2; ++vpl) {
+    if (bt->Rpad % (16 * vpl)) continue;
+    KPM_TRY(launch_step_phase(bt, vpl, 0));  // warm-up
+    KPM_CUDA(cudaEventRecord(bt->e0, s));
+    KPM_TRY(launch_step_phase(bt, vpl, 0));
+    KPM_TRY(launch_step_phase(bt, vpl, 1));
+    KPM_TRY(launch_step_phase(bt, vpl, 2));
+    KPM_CUDA(cudaEventRecord(bt->e1, s));
+    KPM_TRY(launch_step_phase(bt, vpl, 3));  // (occupancy query before capture)
+    KPM_CUDA(cudaEventSynchronize(bt->e1));
+    float ms = 0.f;
+    KPM_CUDA(cudaEventElapsedTime(&ms, bt->e0, bt->e1));
+    if (ms < best) {
+      best = ms;
+      bt->vpl = vpl;
+    }
+  }
+  // capture the whole run in a CUDA graph
+  KPM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  int st = enqueue_run(bt, bt->vpl);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(s, &g);
+  if (st != KPM_OK) {
+    if (g) cudaGraphDestroy(g);
+    return st;
+  }
+  KPM_CUDA(e);
+  bt->graph = g;
+  KPM_CUDA(cudaGraphInstantiate(&bt->exec, g, 0));
+  size_t nn = 0;
+  KPM_CUDA(cudaGraphGetNodes(g, nullptr, &nn));
+  bt->nodes = (int64_t)nn;
+  bt->ready = true;
+  return KPM_OK;
+}
+
+// Host BSR -> ELL-BSR (diagonal block first, KB blocks per row), scaled.
+int upload_bsr(kpm_batch* bt, const kpm_bsr_desc* m, double a, double b,
+               kpm_batch::Sys* y) {
+  const int64_t nb = m->block_rows;
+  KPM_REQUIRE(m->indptr[0] == 0 && m->indptr[nb] == m->nnzb,
+              "BSR indptr must start at 0 and end at nnzb");
+  std::vector<int32_t> idx((size_t)nb * KB);
+  std::vector<float2> val((size_t)nb * KB * 16, make_float2(0.f, 0.f));
+  const double sc = 2.0 / a;
+  for (int64_t i = 0; i < nb; ++i) {
+    KPM_REQUIRE(m->indptr[i] <= m->indptr[i + 1], "BSR indptr not monotone");
+    const int64_t cnt = m->indptr[i + 1] - m->indptr[i];
+    int64_t diag = -1;
+    for (int32_t k = m->indptr[i]; k < m->indptr[i + 1]; ++k) {
+      KPM_REQUIRE(m->indices[k] >= 0 && m->indices[k] < nb,
+                  "BSR column out of range");
+      if (m->indices[k] == i) diag = k;
+    }
+    KPM_REQUIRE(cnt + (diag < 0 ? 1 : 0) <= KB,
+                "BSR row %lld has more than %d blocks", (long long)i, KB);
+    int q = 0;
+    auto put = [&](int32_t col, const double* blk, bool is_diag) {
+      idx[i * KB + q] = col;
+      for (int e = 0; e < 16; ++e) {
+        double re = blk ? blk[2 * e] : 0.0, im = blk ? blk[2 * e + 1] : 0.0;
+        if (is_diag && e % 5 == 0) re -= b;
+        val[(i * KB + q) * 16 + e] =
+            make_float2((float)(re * sc), (float)(im * sc));
+      }
+      ++q;
+    };
+    put((int32_t)i, diag >= 0 ? m->data + 32 * diag : nullptr, true);
+    for (int32_t k = m->indptr[i]; k < m->indptr[i + 1]; ++k)
+      if (k != diag) put(m->indices[k], m->data + 32 * k, false);
+    while (q < KB) put((int32_t)i, nullptr, false);
+  }
+  KPM_TRY(dev_alloc((void**)&y->bidx, idx.size() * 4, bt->stream));
+  KPM_TRY(dev_alloc((void**)&y->bval, val.size() * 8, bt->stream));
+  KPM_CUDA(cudaMemcpyAsync(y->bidx, idx.data(), idx.size() * 4,
+                           cudaMemcpyHostToDevice, bt->stream));
+  KPM_CUDA(cudaMemcpyAsync(y->bval, val.data(), val.size() * 8,
+                           cudaMemcpyHostToDevice, bt->stream));
+  KPM_CUDA(cudaStreamSynchronize(bt->stream));
+  return KPM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int kpm_batch_create(int64_t num_vectors, int64_t num_moments, uint64_t seed,
+                     kpm_batch** out) {
+  KPM_REQUIRE(out && num_vectors > 0 && num_moments >= 2 &&
+                  num_moments % 2 == 0,
+              "kpm_batch_create: need num_vectors > 0 and an even "
+              "num_moments >= 2");
+  auto* bt = new kpm_batch();
+  bt->R = num_vectors;
+  bt->Rpad = round_up(num_vectors, 32);
+  bt->M = num_moments;
+  bt->seed = seed;
+  int st = init_device(&bt->device, &bt->num_sms);
+  if (st == KPM_OK &&
+      cudaStreamCreateWithFlags(&bt->stream, cudaStreamNonBlocking) !=
+          cudaSuccess) {
+    set_error("kpm_batch_create: stream creation failed");
+    st = KPM_ECUDA;
+  }
+  if (st != KPM_OK) {
+    batch_free(bt);
+    return st;
+  }
+  *out = bt;
+  return KPM_OK;
+}
+
+int kpm_batch_add_bsr(kpm_batch* bt, const kpm_bsr_desc* ham, double a,
+                      double b) {
+  KPM_REQUIRE(bt && ham && ham->indptr && ham->indices && ham->data,
+              "kpm_batch_add_bsr: null argument");
+  KPM_REQUIRE(!bt->ready, "kpm_batch_add_bsr: batch already run");
+  KPM_REQUIRE(ham->block_rows > 0 && ham->block_rows * BS < INT32_MAX,
+              "kpm_batch_add_bsr: invalid size");
+  KPM_REQUIRE(a > 0 && std::isfinite(a) && std::isfinite(b),
+              "kpm_batch_add_bsr: scale a must be positive");
+  kpm_batch::Sys y;
+  y.nb = ham->block_rows;
+  y.a = a;
+  y.b = b;
+  int st = upload_bsr(bt, ham, a, b, &y);
+  bt->sys.push_back(y);  // freed with the batch even on failure
+  return st;
+}
+
+int kpm_batch_add_wilson_dirac(kpm_batch* bt, int64_t L, double m, double W,
+                               uint64_t seed, double a, double b) {
+  KPM_REQUIRE(bt, "kpm_batch_add_wilson_dirac: null batch");
+  KPM_REQUIRE(!bt->ready, "kpm_batch_add_wilson_dirac: batch already run");
+  KPM_REQUIRE(L >= 2 && L * L * L * BS < INT32_MAX,
+              "kpm_batch_add_wilson_dirac: invalid L");
+  KPM_REQUIRE(a > 0 && std::isfinite(a), "scale a must be positive");
+  // Gamma matrices: G0 = tau_z (x) s0, Gj = tau_x (x) sj
+  auto kron = [](const double t[2][2][2], const double s[2][2][2],
+                 double out[4][4][2]) {
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 2; ++j)
+        for (int k = 0; k < 2; ++k)
+          for (int l = 0; l < 2; ++l) {
+            const double ar = t[i][j][0], ai = t[i][j][1];
+            const double br = s[k][l][0], bi = s[k][l][1];
+            out[2 * i + k][2 * j + l][0] = ar * br - ai * bi;
+            out[2 * i + k][2 * j + l][1] = ar * bi + ai * br;
+          }
+  };
+  const double s0[2][2][2] = {{{1, 0}, {0, 0}}, {{0, 0}, {1, 0}}};
+  const double sx[2][2][2] = {{{0, 0}, {1, 0}}, {{1, 0}, {0, 0}}};
+  const double sy[2][2][2] = {{{0, 0}, {0, -1}}, {{0, 1}, {0, 0}}};
+  const double sz[2][2][2] = {{{1, 0}, {0, 0}}, {{0, 0}, {-1, 0}}};
+  double G0[4][4][2], Gj[3][4][4][2];
+  kron(sz, s0, G0);
+  kron(sx, sx, Gj[0]);
+  kron(sx, sy, Gj[1]);
+  kron(sx, sz, Gj[2]);
+  WdBlocks blk;
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) {
+      blk.diag[4 * r + c] =
+          make_float2((float)((m - 3) * G0[r][c][0]), 0.f);
+      for (int j = 0; j < 3; ++j) {
+        // T = (G0 - i Gj) / 2 ;  T[r][c]
+        const double tr = (G0[r][c][0] + Gj[j][r][c][1]) / 2;
+        const double ti = (G0[r][c][1] - Gj[j][r][c][0]) / 2;
+        blk.bwd[j][4 * r + c] = make_float2((float)tr, (float)ti);
+        // T^dagger[r][c] = conj(T[c][r])
+        const double ur = (G0[c][r][0] + Gj[j][c][r][1]) / 2;
+        const double ui = (G0[c][r][1] - Gj[j][c][r][0]) / 2;
+        blk.fwd[j][4 * r + c] = make_float2((float)ur, (float)(-ui));
+      }
+    }
+  kpm_batch::Sys y;
+  y.nb = L * L * L;
+  y.a = a;
+  y.b = b;
+  int st = dev_alloc((void**)&y.bidx, (size_t)y.nb * KB * 4, bt->stream);
+  if (st == KPM_OK)
+    st = dev_alloc((void**)&y.bval, (size_t)y.nb * KB * 16 * 8, bt->stream);
+  if (st == KPM_OK) {
+    wd_generate_kernel<<<(unsigned)ceil_div(y.nb, 256), 256, 0, bt->stream>>>(
+        L, blk, W, mix64(seed), 2.0 / a, b, y.bidx, y.bval);
+    count_launch(1);
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaStreamSynchronize(bt->stream) != cudaSuccess) {
+      set_error("kpm_batch_add_wilson_dirac: generation failed");
+      st = KPM_ECUDA;
+    }
+  }
+  bt->sys.push_back(y);
+  return st;
+}
+
+int kpm_batch_run(kpm_batch* bt, double* out) {
+  KPM_REQUIRE(bt && out, "kpm_batch_run: null argument");
+  if (!bt->ready) KPM_TRY(prepare(bt));
+  KPM_CUDA(cudaEventRecord(bt->e0, bt->stream));
+  KPM_CUDA(cudaGraphLaunch(bt->exec, bt->stream));
+  KPM_CUDA(cudaEventRecord(bt->e1, bt->stream));
+  KPM_CUDA(cudaMemcpyAsync(out, bt->d_out, bt->sys.size() * bt->M * 16,
+                           cudaMemcpyDeviceToHost, bt->stream));
+  KPM_CUDA(cudaStreamSynchronize(bt->stream));
+  float ms = 0.f;
+  KPM_CUDA(cudaEventElapsedTime(&ms, bt->e0, bt->e1));
+  bt->last_ms = ms;
+  return KPM_OK;
+}
+
+int kpm_batch_stats(kpm_batch* bt, double* ms, int64_t* nodes,
+                    int* vectors_per_lane) {
+  KPM_REQUIRE(bt && ms && nodes && vectors_per_lane,
+              "kpm_batch_stats: null argument");
+  *ms = bt->last_ms;
+  *nodes = bt->nodes;
+  *vectors_per_lane = bt->vpl;
+  return KPM_OK;
+}
+
+int kpm_batch_destroy(kpm_batch* bt) { return batch_free(bt); }
+
+}  // extern "C"
