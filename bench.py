@@ -567,7 +567,8 @@ def run_batch(args):
     orbs = int(sum(4 * L ** 3 for L in Ls))
     Rpad = -(-R // 32) * 32
     # algorithmic bytes per step: ELL-BSR index + blocks, 3 vector passes
-    B = sum(L ** 3 * 8 * (4 + 16 * 8) for L in Ls) + 3 * orbs * Rpad * 8
+    B = int(sum(int(L) ** 3 * 8 * (4 + 16 * 8) for L in Ls)
+            + 3 * orbs * Rpad * 8)
     steps = M // 2
     achieved = B * steps / (ms / 1e3) / 1e9
     peaks = {}
