@@ -29,129 +29,11 @@
 #include "kpm_common.cuh"
 #include "kpm_internal.cuh"
 #include "kpm_gemm.cuh"
+#include "kpm_tc.cuh"
 
 namespace kpm {
 
 namespace tc {
-
-constexpr int TM = 128;          // output rows per CTA (MMA M)
-constexpr int THREADS = 128;
-constexpr uint64_t WAIT_NS = 2000000000ull;  // bounded waits: 2 s
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ uint64_t global_ns() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
-               "r"(count));
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile(
-      "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
-          smem_u32(bar)),
-      "r"(bytes)
-      : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n"
-      " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// Bounded wait; returns false (and records err) when the deadline passes.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
-                                          int* err, int code) {
-  const uint64_t t0 = global_ns();
-  while (!mbar_try_wait(bar, parity)) {
-    if (*(volatile int*)err) return false;
-    if (global_ns() - t0 > WAIT_NS) {
-      atomicCAS(err, 0, code);
-      return false;
-    }
-  }
-  return true;
-}
-
-__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map,
-                                            uint64_t* bar, int c0, int c1,
-                                            int c2) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx"
-      "::bytes [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(c0),
-      "r"(c1), "r"(c2)
-      : "memory");
-}
-
-// Per-stage K width: rows of KC bf16 = 2*KC bytes, swizzled over that width
-// (64 B -> 2 stages, 32 B -> 4 stages in the same shared memory).
-template <int KC> struct Stage;
-template <> struct Stage<32> {
-  static constexpr int STAGES = 2;
-  static constexpr uint64_t LAYOUT = 4;   // descriptor: 64-byte swizzle
-  static constexpr uint32_t SBO = 512;    // 8 rows x 64 B
-};
-template <> struct Stage<16> {
-  static constexpr int STAGES = 4;
-  static constexpr uint64_t LAYOUT = 6;   // descriptor: 32-byte swizzle
-  static constexpr uint32_t SBO = 256;    // 8 rows x 32 B
-};
-
-// Shared-memory matrix descriptor: K-major, swizzled rows of 2*KC bytes,
-// 8-row groups SBO bytes apart (stride byte offset), version 1.
-template <int KC>
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((addr & 0x3FFFF) >> 4);      // start address
-  d |= (uint64_t)1 << 16;                       // leading byte offset (unused)
-  d |= (uint64_t)(Stage<KC>::SBO >> 4) << 32;   // stride byte offset
-  d |= (uint64_t)1 << 46;                       // descriptor version
-  d |= Stage<KC>::LAYOUT << 61;                 // swizzle mode
-  return d;
-}
-
-// Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major,
-// M = 128, N = n; optional negation of A.
-__host__ __device__ constexpr uint32_t instr_desc(int n, bool neg_a) {
-  return (1u << 4)                    // D format F32
-         | (1u << 7)                  // A format BF16
-         | (1u << 10)                 // B format BF16
-         | ((neg_a ? 1u : 0u) << 13)  // negate A
-         | ((uint32_t)(n >> 3) << 17) // N / 8
-         | ((uint32_t)(TM >> 4) << 24);  // M / 16
-}
-
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc,
-                                         uint64_t b_desc, uint32_t idesc,
-                                         uint32_t accumulate) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
-          d_tmem),
-      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate));
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t* bar) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 "
-      "[%0];" ::"r"(smem_u32(bar))
-      : "memory");
-}
 
 struct TcArgs {
   int64_t M;        // rows of the output (num_moments)
@@ -335,21 +217,6 @@ __global__ void tc_reduce_kernel(const float2* __restrict__ part, int splits,
     im += (double)p.y;
   }
   out[i] = make_double2(r * scale, im * scale);
-}
-
-static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
-    cudaDriverEntryPointQueryResult q;
-    void* p = nullptr;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
-                                         cudaEnableDefault,
-                                         &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    cudaGetLastError();
-  }
-  return fn;
 }
 
 // 3D map over the four planes of a store: dims {Kp, M, 4}, box {KC, rows, 4},
