@@ -310,6 +310,56 @@ KPM_API int kpm_correlator_moments(kpm_handle* h, double a2, double b2,
 KPM_API int kpm_integral_factor(int64_t M, const double* mu, const double* g,
                                 const double* nodes, double* factor_out);
 
+/* ---- parametric Hamiltonian family (parameter sweeps) -----------------------
+ * A three-parameter family on the handle's sparsity structure,
+ *   H(phi, s1, s2) = B .* exp(i phi Theta) + s1 D1 + s2 D2,
+ * e.g. hoppings B with Peierls phases Theta per unit flux phi, and onsite
+ * terms D1 (a fixed disorder pattern, s1 = its strength) and D2 (a staggered
+ * mass, s2 = the mass).  The four CSR matrices must have exactly the
+ * structure (indptr, indices) the handle was created with; Theta must be
+ * real.  kpm_family_point regenerates the handle's matrix values on the
+ * device for one parameter point (FP64: H; MIXED: 2H/a, the ELL copy
+ * included); the handle's (a, b) must bound the spectrum of every point
+ * used.  Blocks created on the handle must be rewound after a point change.
+ * Replaces re-running the reference's Hamiltonian assembly
+ * (hamiltonian_submatrix, kwant/_system.pyx:233-338) with new params per
+ * sweep point. */
+KPM_API int kpm_family_set(kpm_handle* h, const kpm_csr_desc* base,
+                           const kpm_csr_desc* theta, const kpm_csr_desc* d1,
+                           const kpm_csr_desc* d2);
+KPM_API int kpm_family_point(kpm_handle* h, double phi, double s1, double s2);
+
+/* ---- learned moment surrogate: multilayer perceptron ---------------------
+ * widths[0] -> widths[1] -> ... -> widths[num_layers] with exact-erf GELU
+ * after every hidden layer and a linear output.  Parameters (FP32 master
+ * copy, flat): for each layer l, W_l (widths[l+1] x widths[l], row-major)
+ * then b_l (widths[l+1]).  Matmuls in BF16 with FP32 accumulation on the
+ * tensor cores (tcgen05, TMA-fed); loss = mean squared error over all
+ * outputs; optimiser Adam (beta1 0.9, beta2 0.999, eps 1e-8).  Hidden and
+ * output widths must be multiples of 32; batches multiples of 32.
+ * x: n x widths[0] float32, y: n x widths[num_layers] float32 (host).
+ * No counterpart in the reference: the plain KPM path is its fallback. */
+typedef struct kpm_mlp kpm_mlp;
+KPM_API int kpm_mlp_create(int num_layers, const int32_t* widths,
+                           int max_batch, uint64_t seed, kpm_mlp** out);
+KPM_API int kpm_mlp_num_params(kpm_mlp* net, int64_t* count);
+KPM_API int kpm_mlp_get_params(kpm_mlp* net, float* out);
+/* Sets the parameters and resets the Adam state. */
+KPM_API int kpm_mlp_set_params(kpm_mlp* net, const float* in);
+KPM_API int kpm_mlp_forward(kpm_mlp* net, const float* x, int64_t n,
+                            float* y);
+/* Gradient of the loss on one batch (n <= max_batch) at the current
+ * parameters (flat, like the parameters) and the loss itself. */
+KPM_API int kpm_mlp_gradients(kpm_mlp* net, const float* x, const float* y,
+                              int64_t n, float* grads, double* loss);
+/* Mini-batch Adam over (x, y): every epoch shuffles the n samples
+ * (mt19937_64 from seed) and takes floor(n / batch) steps; final_loss is
+ * the mean batch loss of the last epoch. */
+KPM_API int kpm_mlp_train(kpm_mlp* net, const float* x, const float* y,
+                          int64_t n, int batch, int64_t epochs, double lr,
+                          uint64_t seed, double* final_loss);
+KPM_API int kpm_mlp_destroy(kpm_mlp* net);
+
 /* ---- diagnostics -------------------------------------------------------------- */
 /* Device time (ms) of the last recursion call on the handle, measured with
  * CUDA events on the handle's stream around the kernels only. */

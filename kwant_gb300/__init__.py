@@ -20,7 +20,7 @@ from . import system, lattices  # noqa: F401  (host-only modules)
 def __getattr__(name):
     # Modules that need the CUDA library load lazily, so that the host-only
     # parts import without it.
-    if name in ('kpm', 'operator', '_lib', 'batch'):
+    if name in ('kpm', 'operator', '_lib', 'batch', 'surrogate'):
         import importlib
         return importlib.import_module('.' + name, __name__)
     raise AttributeError(name)

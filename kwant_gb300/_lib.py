@@ -118,6 +118,16 @@ def _load():
         'kpm_profile': [P, I],
         'kpm_profile_read': [P, P, P],
         'kpm_launch_count': [P],
+        'kpm_family_set': [P, P, P, P, P],
+        'kpm_family_point': [P, D, D, D],
+        'kpm_mlp_create': [I, P, I, C.c_uint64, P],
+        'kpm_mlp_num_params': [P, P],
+        'kpm_mlp_get_params': [P, P],
+        'kpm_mlp_set_params': [P, P],
+        'kpm_mlp_forward': [P, P, I64, P],
+        'kpm_mlp_gradients': [P, P, P, I64, P, P],
+        'kpm_mlp_train': [P, P, P, I64, I, I64, D, C.c_uint64, P],
+        'kpm_mlp_destroy': [P],
     }
     for name, args in sigs.items():
         fn = getattr(lib, name)
@@ -239,6 +249,17 @@ class Handle:
         y = np.empty_like(x)
         check(lib.kpm_handle_matvec(self._h, ptr(x), ptr(y)))
         return y
+
+    def family_set(self, base, theta, d1, d2):
+        """Coefficient matrices of H(phi, s1, s2) = base .* exp(i phi
+        theta) + s1 d1 + s2 d2 (scipy CSR, the handle's structure)."""
+        self._family = [m if isinstance(m, Csr) else Csr(m)
+                        for m in (base, theta, d1, d2)]
+        check(lib.kpm_family_set(self._h, *[m.ref() for m in self._family]))
+
+    def family_point(self, phi, s1, s2):
+        check(lib.kpm_family_point(self._h, float(phi), float(s1),
+                                   float(s2)))
 
     def close(self):
         if getattr(self, '_h', None):
@@ -443,6 +464,67 @@ class Batch:
         if getattr(self, '_b', None):
             lib.kpm_batch_destroy(self._b)
             self._b = None
+
+    def __del__(self):
+        self.close()
+
+
+class Mlp:
+    """Multilayer perceptron on the device (kpm_mlp_* C ABI)."""
+
+    def __init__(self, widths, max_batch=4096, seed=0):
+        self.widths = [int(w) for w in widths]
+        w = np.ascontiguousarray(self.widths, dtype=np.int32)
+        m = C.c_void_p()
+        check(lib.kpm_mlp_create(len(w) - 1, ptr(w), int(max_batch),
+                                 C.c_uint64(int(seed) & (2**64 - 1)),
+                                 C.byref(m)))
+        self._m = m
+        self.max_batch = int(max_batch)
+        n = C.c_int64()
+        check(lib.kpm_mlp_num_params(m, C.byref(n)))
+        self.num_params = n.value
+
+    def get_params(self):
+        out = np.empty(self.num_params, dtype=np.float32)
+        check(lib.kpm_mlp_get_params(self._m, ptr(out)))
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        if p.shape != (self.num_params,):
+            raise ValueError('expected %d parameters' % self.num_params)
+        check(lib.kpm_mlp_set_params(self._m, ptr(p)))
+
+    def forward(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.empty((x.shape[0], self.widths[-1]), dtype=np.float32)
+        check(lib.kpm_mlp_forward(self._m, ptr(x), x.shape[0], ptr(y)))
+        return y
+
+    def gradients(self, x, y):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        g = np.empty(self.num_params, dtype=np.float32)
+        loss = C.c_double()
+        check(lib.kpm_mlp_gradients(self._m, ptr(x), ptr(y), x.shape[0],
+                                    ptr(g), C.byref(loss)))
+        return g, loss.value
+
+    def train(self, x, y, batch, epochs, lr, seed=0):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        loss = C.c_double()
+        check(lib.kpm_mlp_train(self._m, ptr(x), ptr(y), x.shape[0],
+                                int(batch), int(epochs), float(lr),
+                                C.c_uint64(int(seed) & (2**64 - 1)),
+                                C.byref(loss)))
+        return loss.value
+
+    def close(self):
+        if getattr(self, '_m', None):
+            lib.kpm_mlp_destroy(self._m)
+            self._m = None
 
     def __del__(self):
         self.close()

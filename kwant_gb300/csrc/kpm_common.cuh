@@ -120,6 +120,12 @@ struct kpm_handle {
   bool profiling = false;
   std::vector<cudaEvent_t> prof_events;
   size_t prof_used = 0;
+  // parametric family: CSR-ordered complex128 B, Theta (real part), D1, D2
+  // in the handle's row order (null: no family set)
+  double2* fam_base = nullptr;
+  double2* fam_theta = nullptr;
+  double2* fam_d1 = nullptr;
+  double2* fam_d2 = nullptr;
 };
 
 struct kpm_block {

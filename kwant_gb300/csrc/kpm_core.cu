@@ -866,6 +866,7 @@ int kpm_synchronize(kpm_handle* h) {
 int kpm_destroy(kpm_handle* h) {
   if (!h) return KPM_OK;
   free_matrix(&h->H, h->stream);
+  free_family(h);
   dev_free(h->partials, h->stream);
   dev_free(h->perm, h->stream);
   if (h->ev_start) cudaEventDestroy(h->ev_start);

@@ -44,6 +44,8 @@ int setup_reorder(kpm_handle* h, const kpm_csr_desc* m,
                   std::vector<int32_t>& ip, std::vector<int32_t>& ix,
                   std::vector<double>& data);
 
+void free_family(kpm_handle* h);
+
 int upload_vectors(kpm_handle* h, const double* host, int64_t R, int64_t N,
                    int64_t Rpad, void* dst);
 int download_vectors(kpm_handle* h, const void* src, int64_t R, int64_t N,

@@ -22,10 +22,10 @@ that the CSR matrices agree.
 import numpy as np
 import scipy.sparse as sp
 
-from .system import LatticeSystem
+from .system import LatticeSystem, HamiltonianFamily
 
-__all__ = ['square', 'honeycomb', 'rashba_square', 'wilson_dirac_cubic',
-           'peierls_phase']
+__all__ = ['square', 'honeycomb', 'honeycomb_family', 'rashba_square',
+           'wilson_dirac_cubic', 'peierls_phase']
 
 SQRT3 = np.sqrt(3)
 
@@ -130,6 +130,50 @@ def honeycomb(n, t=1.0, flux=0.0, W=0.0, mass=0.0, seed=0):
     H = _assemble(N, rows, cols, vals)
     return LatticeSystem(H, [(0, 1, 0), (N, 0, N)], pos,
                          name='honeycomb%d' % n)
+
+
+def honeycomb_family(n, t=1.0, seed=0):
+    """The ``honeycomb`` flake as a family over (flux, W, mass):
+    ``family.hamiltonian(flux, W, mass)`` equals ``honeycomb(n, t, flux, W,
+    mass, seed).hamiltonian`` up to explicit zeros and rounding (the
+    disorder pattern ``u - 1/2`` with ``u = RandomState(seed).uniform(0, 1,
+    2 n^2)`` is scaled by W, the Peierls phases per unit flux by flux).
+    Every onsite and hopping entry is kept in the structure."""
+    i, j, pa, pb = _honeycomb_positions(n)
+    n2 = n * n
+    N = 2 * n2
+    pos = np.concatenate([pa, pb])
+    cell = 0.5 * SQRT3
+    u = np.random.RandomState(seed).uniform(0.0, 1.0, size=N)
+    diag = np.arange(N)
+    rows, cols = [diag], [diag]
+    base, theta = [np.zeros(N, complex)], [np.zeros(N)]
+    dis = [u - 0.5]
+    mass = [np.concatenate([np.ones(n2), -np.ones(n2)])]
+    for di, dj in ((0, 0), (0, -1), (1, -1)):
+        ib, jb = i + di, j + dj
+        ok = (ib >= 0) & (ib < n) & (jb >= 0) & (jb < n)
+        a_idx = np.nonzero(ok)[0]
+        b_idx = n2 + ib[ok] * n + jb[ok]
+        th = peierls_phase(pos[a_idx], pos[b_idx], 1.0, cell)
+        rows += [a_idx, b_idx]
+        cols += [b_idx, a_idx]
+        base += [np.full(len(a_idx), t, complex)] * 2
+        theta += [th, -th]
+        dis += [np.zeros(len(a_idx))] * 2
+        mass += [np.zeros(len(a_idx))] * 2
+    r = np.concatenate(rows)
+    c = np.concatenate(cols)
+    order = np.lexsort((c, r))
+    r, c = r[order], c[order]
+    indptr = np.concatenate([[0], np.cumsum(np.bincount(r, minlength=N))])
+    mats = []
+    for vals in (base, theta, dis, mass):
+        v = np.concatenate(vals).astype(complex)[order]
+        mats.append(sp.csr_matrix((v, c.astype(np.int32), indptr),
+                                  shape=(N, N)))
+    return HamiltonianFamily(*mats, names=('flux', 'W', 'mass'),
+                             name='honeycomb%d' % n)
 
 
 SIGMA0 = np.eye(2, dtype=complex)

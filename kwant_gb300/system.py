@@ -16,7 +16,7 @@ It is also what ``kwant_gb300.operator.Density``/``Current`` need: the graph
 import numpy as np
 import scipy.sparse as sp
 
-__all__ = ['LatticeSystem', 'SiteGraph']
+__all__ = ['LatticeSystem', 'SiteGraph', 'HamiltonianFamily']
 
 
 class SiteGraph:
@@ -160,3 +160,68 @@ class LatticeSystem:
             for k, w in enumerate(sel):
                 out[w] = vals[k]
         return out
+
+
+class HamiltonianFamily:
+    """A three-parameter Hamiltonian family on one sparsity structure,
+
+        H(phi, s1, s2) = base .* exp(1j * phi * theta) + s1 * d1 + s2 * d2,
+
+    e.g. hoppings with Peierls phases ``theta`` per unit flux ``phi`` and two
+    onsite terms (a fixed disorder pattern of strength ``s1``, a staggered
+    mass ``s2``).  The four matrices are scipy CSR with identical
+    ``indptr``/``indices`` (entries that vanish at some points are kept as
+    explicit zeros); ``theta`` is real.  ``names`` labels the parameters.
+    The sweep path (``kwant_gb300.surrogate``) keeps the four matrices on the
+    device and regenerates H on the device per point.
+    """
+
+    def __init__(self, base, theta, d1, d2, names=('phi', 's1', 's2'),
+                 name='family'):
+        mats = [sp.csr_matrix(m, dtype=complex) for m in (base, theta, d1, d2)]
+        for m in mats:
+            m.sort_indices()
+        ref = mats[0]
+        for m in mats[1:]:
+            if (m.shape != ref.shape or
+                    not np.array_equal(m.indptr, ref.indptr) or
+                    not np.array_equal(m.indices, ref.indices)):
+                raise ValueError('family matrices must share one structure')
+        if np.any(mats[1].data.imag != 0):
+            raise ValueError('theta must be real')
+        self.base, self.theta, self.d1, self.d2 = mats
+        self.names = tuple(names)
+        self.name = name
+        self.shape = ref.shape
+
+    def hamiltonian(self, phi, s1, s2):
+        """H at one point, on the family's structure (explicit zeros kept)."""
+        data = (self.base.data * np.exp(1j * phi * self.theta.data.real) +
+                s1 * self.d1.data + s2 * self.d2.data)
+        return sp.csr_matrix((data, self.base.indices.copy(),
+                              self.base.indptr.copy()), shape=self.shape)
+
+    def gershgorin_bounds(self, box):
+        """(lmin, lmax) enclosing the spectrum of every point of the
+        parameter box ``((phi_lo, phi_hi), (s1_lo, s1_hi), (s2_lo, s2_hi))``.
+        Gershgorin discs with radius sum_j (|base_ij| + |s1 d1_ij + s2
+        d2_ij|) off the diagonal; the phase leaves |base| unchanged and the
+        rest is linear in (s1, s2), so the corners of the box bound it."""
+        n = self.shape[0]
+        rows = np.repeat(np.arange(n), np.diff(self.base.indptr))
+        diag = rows == self.base.indices
+        fixed_diag = diag & (self.theta.data.real == 0)
+        b = self.base.data
+        lo, hi = np.full(n, np.inf), np.full(n, -np.inf)
+        for s1 in box[1]:
+            for s2 in box[2]:
+                v = s1 * self.d1.data + s2 * self.d2.data
+                rad = np.where(diag, 0.0, np.abs(v)) + \
+                    np.where(fixed_diag, 0.0, np.abs(b))
+                cen = np.where(diag, v.real, 0.0) + \
+                    np.where(fixed_diag, b.real, 0.0)
+                r = np.bincount(rows, weights=rad, minlength=n)
+                c = np.bincount(rows, weights=cen, minlength=n)
+                lo = np.minimum(lo, c - r)
+                hi = np.maximum(hi, c + r)
+        return float(lo.min()), float(hi.max())
