@@ -598,10 +598,116 @@ def run_batch(args):
     return 0
 
 
+def run_surrogate(args):
+    """Learned-moment-surrogate workload (not the headline line): the
+    honeycomb family over W in [0, 3], flux in [0, 0.02], mass in [0, 0.3]
+    on 500 x 500 cells; 4096 training points (3584 fit + 512 calibration)
+    and 1024 held-out points, M = 512, R = 32 (complex64 recursion).  The
+    held-out sweep runs twice: plain KPM at every point, and surrogate with
+    KPM fallback where the estimated DOS error exceeds the tolerance."""
+    from kwant_gb300 import lattices, surrogate as S
+    box = ((0.0, 0.02), (0.0, 3.0), (0.0, 0.3))
+    M, R = args.sur_moments, args.sur_vectors
+    t0 = time.perf_counter()
+    fam = lattices.honeycomb_family(args.sur_cells, seed=0)
+    sweep = S.MomentSweep(fam, box, num_moments=M, num_vectors=R,
+                          precision='mixed', rng=1)
+    A, _ = S.dos_operator(M, sweep.a, sweep.b)
+    setup_s = time.perf_counter() - t0
+    Xtr = S.random_points(box, args.sur_train, 11)
+    Xte = S.random_points(box, args.sur_test, 12)
+    sweep.moments(Xtr[:max(3, args.warmup)])            # warm-up
+    t0 = time.perf_counter()
+    Ytr = sweep.moments(Xtr)
+    gen_s = time.perf_counter() - t0
+    ncal = min(512, args.sur_train // 8)
+    sur = S.MomentSurrogate(box, M, members=args.sur_members, seed=1,
+                            input_map=('sqrt', 'linear', 'linear'))
+    t0 = time.perf_counter()
+    losses = sur.fit(Xtr[:-ncal], Ytr[:-ncal], epochs=args.sur_epochs,
+                     batch=256, lr=1e-3)
+    train_s = time.perf_counter() - t0
+    cal_err, cal_spread = sur.calibrate(Xtr[-ncal:], Ytr[-ncal:], A)
+    # plain sweep of the held-out points (also the judge of the errors)
+    t0 = time.perf_counter()
+    Yte = sweep.moments(Xte)
+    plain_s = time.perf_counter() - t0
+    hybrid = S.SurrogateSweep(sur, sweep, A, tol=args.sur_tol)
+    t0 = time.perf_counter()
+    mom, accept, info = hybrid.run(Xte)
+    hybrid_s = time.perf_counter() - t0
+    err = np.abs((mom - Yte) @ A.T).max(axis=1)
+    sur_only = sur.predict(Xte, A)[0]
+    err_sur = np.abs((sur_only - Yte) @ A.T).max(axis=1)
+    est = info['estimate']
+    per_pt = plain_s / len(Xte)
+    curve = []
+    for tol in (1e-4, 3e-4, 1e-3, 3e-3, 1e-2, 3e-2):
+        acc = est <= tol
+        curve.append({'tol': tol, 'accepted': float(acc.mean()),
+                      'max_err_accepted': float(err_sur[acc].max())
+                      if acc.any() else None,
+                      'frac_accepted_within_tol': float(
+                          (err_sur[acc] <= tol).mean()) if acc.any() else None,
+                      'sweep_s_model': info['surrogate_s'] +
+                      float((~acc).sum()) * per_pt})
+    # stochastic error of the plain sweep itself (spread over its vectors)
+    pv = sweep.moments(Xte[:16], per_vector=True).real
+    noise = (np.std(pv @ A.T, axis=1, ddof=1) / np.sqrt(R)).max(axis=1)
+    n = len(Xte)
+    line = {
+        'metric': 'held-out sweep points/s at DOS Linf error <= tol '
+                  '(surrogate + KPM fallback)',
+        'value': n / hybrid_s, 'unit': 'points/s', 'n_gpus': 1,
+        'steps': 1, 'warmup': max(3, args.warmup),
+        'ms_per_step': hybrid_s * 1e3, 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'bf16 mlp + c64/f64acc kpm', 'data': 'synthetic',
+        'config': {'workload': 'surrogate sweep: honeycomb %dx%d, W in '
+                               '[0,3], flux in [0,0.02], mass in [0,0.3], '
+                               'M=%d, R=%d' % (args.sur_cells,
+                                               args.sur_cells, M, R),
+                   'train_points': args.sur_train, 'fit_points':
+                   args.sur_train - ncal, 'calibration_points': ncal,
+                   'heldout_points': n, 'members': args.sur_members,
+                   'epochs': args.sur_epochs, 'tol': args.sur_tol,
+                   'dos_units': 'per site per unit energy, Jackson, '
+                                '|x| <= 0.95'},
+        'plain_sweep': {'points_per_s': n / plain_s, 'seconds': plain_s,
+                        'ms_per_point': per_pt * 1e3},
+        'hybrid_sweep': {'seconds': hybrid_s, 'accepted':
+                         float(accept.mean()), 'kpm_points':
+                         int((~accept).sum()), 'max_err':
+                         float(err.max()), 'surrogate_s':
+                         info['surrogate_s'], 'kpm_s': info['kpm_s']},
+        'surrogate_only': {'err_median': float(np.median(err_sur)),
+                           'err_p10': float(np.quantile(err_sur, 0.1)),
+                           'err_p90': float(np.quantile(err_sur, 0.9)),
+                           'err_max': float(err_sur.max()),
+                           'estimate_scale': sur.scale,
+                           'estimate_median': float(np.median(est))},
+        'tolerance_curve': curve,
+        'kpm_noise_linf_median': float(np.median(noise)),
+        'costs_s': {'setup': setup_s, 'dataset': gen_s, 'train': train_s,
+                    'train_loss': [float(x) for x in losses]},
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument('--workload', default='dos', choices=['dos', 'kubo',
-                                                         'batch'])
+                                                         'batch',
+                                                         'surrogate'])
+    p.add_argument('--sur-cells', type=int, default=500)
+    p.add_argument('--sur-moments', type=int, default=512)
+    p.add_argument('--sur-vectors', type=int, default=32)
+    p.add_argument('--sur-train', type=int, default=4096)
+    p.add_argument('--sur-test', type=int, default=1024)
+    p.add_argument('--sur-members', type=int, default=4)
+    p.add_argument('--sur-epochs', type=int, default=2000)
+    p.add_argument('--sur-tol', type=float, default=1e-4)
     p.add_argument('--batch-systems', type=int, default=32)
     p.add_argument('--batch-lmin', type=int, default=32)
     p.add_argument('--batch-lmax', type=int, default=64)
@@ -634,6 +740,8 @@ def main():
         return run_kubo(args)
     if args.workload == 'batch':
         return run_batch(args)
+    if args.workload == 'surrogate':
+        return run_surrogate(args)
     return run_ours(args)
 
 

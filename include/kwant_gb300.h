@@ -130,6 +130,13 @@ KPM_API int kpm_block_create(kpm_handle* h, const double* vecs, int64_t R,
                              int keep_a0, kpm_block** out);
 /* Restart the recursion from |r> (requires keep_a0). */
 KPM_API int kpm_block_rewind(kpm_block* blk);
+/* Replace the starting vectors with new random-phase vectors generated on
+ * the device (exp(2 pi i u), u from SplitMix64 of (seed, vector, device
+ * row); 24 random bits for MIXED, 53 for FP64) and rewind (requires
+ * keep_a0).  A fresh, independent vector set per sweep point without a
+ * host upload; not the reference's MT19937 stream (RandomVectors,
+ * kwant/kpm.py:932-952, draws from numpy). */
+KPM_API int kpm_block_randomize(kpm_block* blk, uint64_t seed);
 KPM_API int kpm_block_destroy(kpm_block* blk);
 /* Copy the current recursion state (alpha_{n-1}, alpha_n) to the host, each
  * R x N complex128 (the reference's _last_two_alphas, kwant/kpm.py:486-488). */

@@ -92,6 +92,7 @@ def _load():
         'kpm_destroy': [P],
         'kpm_block_create': [P, P, I64, I, P],
         'kpm_block_rewind': [P],
+        'kpm_block_randomize': [P, C.c_uint64],
         'kpm_block_destroy': [P],
         'kpm_block_state': [P, P, P],
         'kpm_block_dos_moments': [P, I64, I64, P],
@@ -297,6 +298,11 @@ class Block:
 
     def rewind(self):
         check(lib.kpm_block_rewind(self._b))
+
+    def randomize(self, seed):
+        """New random-phase starting vectors generated on the device."""
+        check(lib.kpm_block_randomize(self._b,
+                                      C.c_uint64(int(seed) & (2**64 - 1))))
 
     def state(self):
         prev = np.empty((self.R, self.handle.N), dtype=np.complex128)

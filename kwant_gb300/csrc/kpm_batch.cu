@@ -33,13 +33,6 @@ namespace bt {
 constexpr int KB = 8;            // blocks per block row
 constexpr int BS = 4;            // block size
 
-__host__ __device__ inline uint64_t mix64(uint64_t z) {
-  z += 0x9E3779B97F4A7C15ull;
-  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-  return z ^ (z >> 31);
-}
-
 struct SysDev {
   int64_t nb;            // block rows
   int xitems;            // row partitions (depends only on nb)

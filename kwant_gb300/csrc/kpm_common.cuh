@@ -68,6 +68,15 @@ __host__ __device__ inline int64_t ceil_div(int64_t x, int64_t m) {
   return (x + m - 1) / m;
 }
 
+// SplitMix64 finaliser (Steele, Lea & Flood 2014; Vigna's constants): the
+// counter-based generator of the device-side random-phase vectors.
+__host__ __device__ inline uint64_t mix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
 inline int xitems_for_rows(int64_t rows) {
   int64_t x = ceil_div(rows, (int64_t)SLOTS);
   if (x > MAX_XITEMS) x = MAX_XITEMS;

@@ -758,6 +758,33 @@ using namespace kpm;
 // ======================================================================
 //                                C ABI
 // ======================================================================
+namespace kpm {
+// Random-phase vectors exp(2 pi i u) in the device layout [N][Rpad] (device
+// row order), padding vectors zero; u from SplitMix64 of (key, vector) then
+// row: the top 24 bits (complex64) or 53 bits (complex128).
+template <typename T>
+__global__ void random_phase_kernel(T* __restrict__ a0, int64_t N, int64_t R,
+                                    int64_t Rpad, uint64_t key) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= N * Rpad) return;
+  const int64_t n = idx / Rpad, r = idx % Rpad;
+  const uint64_t hsh = mix64(mix64(key ^ (uint64_t)r) + (uint64_t)n);
+  T v;
+  if constexpr (sizeof(T) == 8) {
+    float s = 0.f, c = 0.f;
+    if (r < R) sincospif(2.0f * ((float)(hsh >> 40) * 0x1.0p-24f), &s, &c);
+    v.x = c;
+    v.y = s;
+  } else {
+    double s = 0.0, c = 0.0;
+    if (r < R) sincospi(2.0 * ((double)(hsh >> 11) * 0x1.0p-53), &s, &c);
+    v.x = c;
+    v.y = s;
+  }
+  a0[idx] = v;
+}
+}  // namespace kpm
+
 extern "C" {
 
 int kpm_version(void) { return 10000; }
@@ -960,6 +987,27 @@ int kpm_block_create(kpm_handle* h, const double* vecs, int64_t R,
   b->p_prev = nullptr;
   *out = b;
   return KPM_OK;
+}
+
+int kpm_block_randomize(kpm_block* b, uint64_t seed) {
+  KPM_REQUIRE(b, "kpm_block_randomize: null block");
+  if (!b->keep_a0) {
+    set_error("kpm_block_randomize: block was created without keep_a0");
+    return KPM_ESTATE;
+  }
+  kpm_handle* h = b->h;
+  const int64_t total = b->N * b->Rpad;
+  const unsigned grid = (unsigned)ceil_div(total, 256);
+  const uint64_t key = mix64(seed ^ 0x5EEDB10Cull);
+  if (h->precision == KPM_PREC_MIXED)
+    random_phase_kernel<float2><<<grid, 256, 0, h->stream>>>(
+        static_cast<float2*>(b->a0), b->N, b->R, b->Rpad, key);
+  else
+    random_phase_kernel<double2><<<grid, 256, 0, h->stream>>>(
+        static_cast<double2*>(b->a0), b->N, b->R, b->Rpad, key);
+  count_launch(1);
+  KPM_CHECK_LAUNCH();
+  return kpm_block_rewind(b);
 }
 
 int kpm_block_rewind(kpm_block* b) {

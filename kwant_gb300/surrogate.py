@@ -72,11 +72,17 @@ class MomentSweep:
     FP64 Lanczos bounds at the corners of the box (flux at its ends and
     middle), widened by ``margin`` of the width, then rescaled with
     ``eps`` like kwant/kpm.py:1174-1180.
+
+    ``fresh_vectors``: False keeps one vector set for every point (the
+    moments are then a deterministic function of the point); True draws an
+    independent random-phase set per point on the device
+    (``kpm_block_randomize``, keyed by ``rng`` and the running point count),
+    so that the stochastic errors of different points are independent.
     """
 
     def __init__(self, family, box, num_moments=512, num_vectors=32,
                  precision='mixed', rng=1, bounds=None, eps=0.05,
-                 margin=0.01, reorder=None):
+                 margin=0.01, reorder=None, fresh_vectors=False):
         from .kpm import _precision
         self.family = family
         self.box = tuple(tuple(map(float, b)) for b in box)
@@ -105,6 +111,8 @@ class MomentSweep:
         self.block = _lib.Block(self.handle, vecs, keep_a0=True)
         self.seconds = 0.0
         self.points_done = 0
+        self.fresh = bool(fresh_vectors)
+        self.seed = int(rng)
 
     def _corner_bounds(self, eps):
         (f0, f1), (w0, w1), (m0, m1) = self.box
@@ -125,7 +133,11 @@ class MomentSweep:
         t0 = time.perf_counter()
         for i, p in enumerate(points):
             self.handle.family_point(*p)
-            self.block.rewind()
+            if self.fresh:
+                self.block.randomize(self.seed * 1000003 +
+                                     self.points_done + i)
+            else:
+                self.block.rewind()
             mom = self.block.dos_moments(0, self.M) / self.N
             out[i] = mom if per_vector else mom.mean(axis=0).real
         self.seconds += time.perf_counter() - t0
@@ -140,15 +152,22 @@ class MomentSweep:
 class MomentSurrogate:
     """Ensemble of MLPs mapping a parameter point to normalised moments.
 
-    Inputs are mapped to [-1, 1] over ``box``; targets are the moments
-    standardised per index (mean and standard deviation over the training
-    set).  Every member has the widths ``(len(box),) + hidden + (M,)`` and
-    its own initialisation and shuffling seed.
+    Inputs are mapped to [-1, 1] over ``box``, per coordinate either
+    linearly or through a square root (``input_map`` entries 'linear' /
+    'sqrt'; 'sqrt' suits a flux, whose Landau levels move like its square
+    root); targets are the moments standardised per index (mean and
+    standard deviation over the training set).  Every member has the widths
+    ``(len(box),) + hidden + (M,)`` and its own initialisation and shuffling
+    seed.
     """
 
     def __init__(self, box, num_moments, hidden=(256, 256, 256), members=4,
-                 seed=0, max_batch=4096):
+                 seed=0, max_batch=4096, input_map=None):
         self.box = np.asarray(box, float)
+        self.input_map = tuple(input_map or ('linear',) * len(self.box))
+        if len(self.input_map) != len(self.box) or not set(
+                self.input_map) <= {'linear', 'sqrt'}:
+            raise ValueError("input_map: one 'linear' or 'sqrt' per input")
         self.M = int(num_moments)
         self.widths = (self.box.shape[0],) + tuple(hidden) + (self.M,)
         self.nets = [_lib.Mlp(self.widths, max_batch=max_batch,
@@ -159,8 +178,11 @@ class MomentSurrogate:
 
     def _x(self, points):
         lo, hi = self.box[:, 0], self.box[:, 1]
-        return (2 * (np.asarray(points, float) - lo) / (hi - lo) - 1
-                ).astype(np.float32)
+        u = (np.asarray(points, float) - lo) / (hi - lo)
+        for i, m in enumerate(self.input_map):
+            if m == 'sqrt':
+                u[:, i] = np.sqrt(np.clip(u[:, i], 0.0, None))
+        return (2 * u - 1).astype(np.float32)
 
     def fit(self, points, moments, epochs=2000, batch=256, lr=1e-3,
             decay_stages=4):

@@ -158,3 +158,97 @@ def test_family_rejects_other_structure(lib):
     with pytest.raises(ValueError):
         h.family_point(0.0, 1.0, 0.0)      # nothing set yet
     h.close()
+
+
+def test_block_randomize(lib):
+    from kwant_gb300 import lattices
+    fam = lattices.honeycomb_family(12, seed=1)
+    H = fam.hamiltonian(0.01, 1.0, 0.1)
+    N = H.shape[0]
+    for prec, tol in ((lib.PREC_FP64, 1e-12), (lib.PREC_MIXED, 1e-6)):
+        h = lib.Handle(H, 5.0, 0.0, prec)
+        blk = lib.Block(h, np.ones((5, N), complex))
+        blk.randomize(7)
+        m7 = blk.dos_moments(0, 16)
+        # |v_i| = 1: mu_0 = N for every vector
+        assert np.allclose(m7[:, 0].real, N, rtol=tol)
+        blk.randomize(7)
+        assert np.array_equal(blk.dos_moments(0, 16), m7)
+        blk.randomize(8)
+        m8 = blk.dos_moments(0, 16)
+        assert np.abs(m8[:, 1:] - m7[:, 1:]).max() > 1e-3 * N
+        blk.close()
+        h.close()
+
+
+def _truth_moments(fam, X, a, b, M):
+    out = []
+    for p in X:
+        ev = np.linalg.eigvalsh(fam.hamiltonian(*p).toarray())
+        out.append(np.cos(np.outer(np.arange(M),
+                                   np.arccos((ev - b) / a))).mean(axis=1))
+    return np.array(out)
+
+
+def test_surrogate_beats_plain_sweep_against_exact_dos(lib):
+    """What the network gains: trained on independent noisy KPM sweeps
+    (R = 4 random vectors per point), its DOS is several times closer to
+    the exact (diagonalisation) DOS than the plain KPM sweep's at the same
+    points, at a fraction of the per-point cost."""
+    from kwant_gb300 import lattices, surrogate as S
+    box = ((0.0, 0.02), (0.0, 3.0), (0.0, 0.3))
+    fam = lattices.honeycomb_family(16, seed=0)            # 512 sites
+    M = 64
+    sw = S.MomentSweep(fam, box, num_moments=M, num_vectors=4,
+                       precision='mixed', rng=1, fresh_vectors=True)
+    A, _ = S.dos_operator(M, sw.a, sw.b)
+    Xtr = S.random_points(box, 2048, 11)
+    Xte = S.random_points(box, 64, 12)
+    Ytr = sw.moments(Xtr)
+    Yte = sw.moments(Xte)
+    truth = _truth_moments(fam, Xte, sw.a, sw.b, M)
+    sur = S.MomentSurrogate(box, M, hidden=(128, 128), members=3, seed=2,
+                            max_batch=1024,
+                            input_map=('sqrt', 'linear', 'linear'))
+    sur.fit(Xtr, Ytr, epochs=300, batch=128, lr=2e-3)
+    mom, _ = sur.predict(Xte, A)
+    e_kpm = np.abs((Yte - truth) @ A.T).max(axis=1)
+    e_sur = np.abs((mom - truth) @ A.T).max(axis=1)
+    print('DOS Linf vs exact: plain KPM median %.2e max %.2e; surrogate '
+          'median %.2e max %.2e' % (np.median(e_kpm), e_kpm.max(),
+                                    np.median(e_sur), e_sur.max()))
+    assert np.median(e_sur) < 0.4 * np.median(e_kpm)
+    assert e_sur.max() < e_kpm.max()
+    sur.close()
+    sw.close()
+
+
+def test_surrogate_sweep_fallback_is_plain_kpm(lib):
+    """Points whose estimated error exceeds tol are answered by the plain
+    KPM (bit-identical to the plain sweep with the same vectors); accepted
+    points stay within tol of it."""
+    from kwant_gb300 import lattices, surrogate as S
+    box = ((0.0, 0.02), (0.0, 3.0), (0.0, 0.3))
+    fam = lattices.honeycomb_family(16, seed=0)
+    M = 64
+    sw = S.MomentSweep(fam, box, num_moments=M, num_vectors=4,
+                       precision='mixed', rng=1)
+    A, _ = S.dos_operator(M, sw.a, sw.b)
+    Xtr = S.random_points(box, 1024, 11)
+    Xte = S.random_points(box, 64, 12)
+    Ytr = sw.moments(Xtr)
+    Yte = sw.moments(Xte)
+    sur = S.MomentSurrogate(box, M, hidden=(128, 128), members=3, seed=2,
+                            max_batch=1024,
+                            input_map=('sqrt', 'linear', 'linear'))
+    sur.fit(Xtr[:-256], Ytr[:-256], epochs=300, batch=128, lr=2e-3)
+    sur.calibrate(Xtr[-256:], Ytr[-256:], A)
+    _, est = sur.predict(Xte, A)
+    tol = float(np.median(est))
+    mom, accept, info = S.SurrogateSweep(sur, sw, A, tol=tol).run(Xte)
+    assert 0 < accept.sum() < len(Xte)
+    assert np.array_equal(mom[~accept], Yte[~accept])
+    err = np.abs((mom - Yte) @ A.T).max(axis=1)
+    assert np.mean(err[accept] <= tol) >= 0.8
+    sur.close()
+    sw.close()
