@@ -57,8 +57,50 @@ __device__ __forceinline__ void cmac(float& ar, float& ai, float hr, float hi,
   ai = fmaf(hi, xr, ai);
 }
 
+// 16-byte asynchronous global -> shared copy (L2 only), grouped per thread
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                   static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_prev() {
+  asm volatile("cp.async.wait_group 1;" ::: "memory");
+}
+
+// Block rows per CTA tile: one per 16-lane slot.
+constexpr int TILE = SLOTS;
+// 16-byte chunks of one tile's block values and indices
+constexpr int VAL_CHUNKS = TILE * KB * 16 * 8 / 16;   // 1024
+constexpr int IDX_CHUNKS = TILE * KB * 4 / 16;        // 32
+
+// Stage the block values and block-column indices of block rows
+// [base, base + TILE) (those below nb) into shared memory, asynchronously.
+__device__ __forceinline__ void stage_tile(const SysDev& S, int64_t base,
+                                           float2* sval, int32_t* sidx) {
+  const float4* gv = reinterpret_cast<const float4*>(S.bval + base * KB * 16);
+  float4* dv = reinterpret_cast<float4*>(sval);
+  for (int c = threadIdx.x; c < VAL_CHUNKS; c += STEP_THREADS)
+    if (base + c / (KB * 16 * 8 / 16) < S.nb) cp_async16(dv + c, gv + c);
+  if (threadIdx.x < IDX_CHUNKS && base + threadIdx.x / (KB * 4 / 16) < S.nb)
+    cp_async16(reinterpret_cast<int4*>(sidx) + threadIdx.x,
+               reinterpret_cast<const int4*>(S.bidx + base * KB) +
+                   threadIdx.x);
+}
+
 // PHASE 0: x = a0 -> b0 (first step); 1: x = b0, prev = a0 -> b1;
 // 2: x = b1, prev = b0 -> b0; 3: x = b0, prev = b1 -> b1.
+//
+// The CTA walks its partition in tiles of TILE consecutive block rows (one
+// per slot).  The block values and indices of tile t + 1 are copied into
+// shared memory with cp.async while tile t computes, so the only global
+// loads on a row's critical path are the gathered vector rows; those are
+// double-buffered one block ahead in registers.  Padding blocks (column ==
+// the row itself after the diagonal block) skip their products: adding
+// 0 * x would not change the sums.
 template <int VPL, int PHASE>
 __global__ void __launch_bounds__(STEP_THREADS, VPL == 1 ? 4 : 3)
 bsr_step_kernel(const SysDev* __restrict__ sys,
@@ -70,6 +112,8 @@ bsr_step_kernel(const SysDev* __restrict__ sys,
   const int lane = threadIdx.x & 15;
   const int slot = threadIdx.x >> 4;
   __shared__ double red[SLOTS][G * 3];
+  __shared__ __align__(16) float2 sval[2][TILE * KB * 16];
+  __shared__ __align__(16) int32_t sidx[2][TILE * KB];
   const int64_t groups = Rpad / G;
   const int64_t rp = Rpad / VPL;
 
@@ -104,99 +148,125 @@ bsr_step_kernel(const SysDev* __restrict__ sys,
     for (int k = 0; k < VPL; ++k) fn[k] = fr[k] = fi[k] = 0.f;
     int pending = 0;
     const int64_t stride = (int64_t)S.xitems * SLOTS;
+    const int64_t first = (int64_t)xi * SLOTS;
+    const int64_t tiles = first < S.nb ? (S.nb - first + stride - 1) / stride
+                                       : 0;
+    if (tiles > 0) stage_tile(S, first, sval[0], sidx[0]);
+    cp_async_commit();
 
-    for (int64_t i = (int64_t)xi * SLOTS + slot; i < S.nb; i += stride) {
-      float acc[BS][VPL][2];
+    for (int64_t t = 0; t < tiles; ++t) {
+      const int buf = (int)(t & 1);
+      if (t + 1 < tiles)
+        stage_tile(S, first + (t + 1) * stride, sval[buf ^ 1], sidx[buf ^ 1]);
+      cp_async_commit();
+      cp_async_wait_prev();
+      __syncthreads();
+      const int64_t i = first + t * stride + slot;
+      if (i < S.nb) {
+        const float4* bvs =
+            reinterpret_cast<const float4*>(sval[buf] + slot * KB * 16);
+        const int4* ip = reinterpret_cast<const int4*>(sidx[buf] + slot * KB);
+        const int4 i0 = ip[0], i1 = ip[1];
+        const int cidx[KB] = {i0.x, i0.y, i0.z, i0.w,
+                              i1.x, i1.y, i1.z, i1.w};
+        float acc[BS][VPL][2];
 #pragma unroll
-      for (int rr = 0; rr < BS; ++rr)
+        for (int rr = 0; rr < BS; ++rr)
 #pragma unroll
-        for (int k = 0; k < VPL; ++k) acc[rr][k][0] = acc[rr][k][1] = 0.f;
-      PT xo[BS];
-#pragma unroll 1
-      for (int q = 0; q < KB; ++q) {
-        const int64_t c = __ldg(S.bidx + i * KB + q);
-        PT xn[BS];
+          for (int k = 0; k < VPL; ++k) acc[rr][k][0] = acc[rr][k][1] = 0.f;
+        PT xbuf[2][BS];
 #pragma unroll
-        for (int cc = 0; cc < BS; ++cc) xn[cc] = X[(c * BS + cc) * rp + col];
-        if (q == 0) {
+        for (int cc = 0; cc < BS; ++cc)
+          xbuf[0][cc] = X[((int64_t)cidx[0] * BS + cc) * rp + col];
 #pragma unroll
-          for (int cc = 0; cc < BS; ++cc) xo[cc] = xn[cc];
-        }
-        const float4* bv =
-            reinterpret_cast<const float4*>(S.bval + (i * KB + q) * 16);
+        for (int q = 0; q < KB; ++q) {
+          PT* xn = xbuf[q & 1];
+          if (q + 1 < KB && cidx[q + 1] != (int)i) {
 #pragma unroll
-        for (int rr = 0; rr < BS; ++rr) {
-          const float4 b01 = __ldg(bv + 2 * rr), b23 = __ldg(bv + 2 * rr + 1);
-          const float hr[4] = {b01.x, b01.z, b23.x, b23.z};
-          const float hi[4] = {b01.y, b01.w, b23.y, b23.w};
+            for (int cc = 0; cc < BS; ++cc)
+              xbuf[(q + 1) & 1][cc] =
+                  X[((int64_t)cidx[q + 1] * BS + cc) * rp + col];
+          }
+          if (q > 0 && cidx[q] == (int)i) continue;   // padding block
+          const float4* bv = bvs + q * 8;
 #pragma unroll
-          for (int cc = 0; cc < BS; ++cc) {
-            if constexpr (VPL == 1) {
-              cmac(acc[rr][0][0], acc[rr][0][1], hr[cc], hi[cc], xn[cc].x,
-                   xn[cc].y);
-            } else {
-              cmac(acc[rr][0][0], acc[rr][0][1], hr[cc], hi[cc], xn[cc].x,
-                   xn[cc].y);
-              cmac(acc[rr][1][0], acc[rr][1][1], hr[cc], hi[cc], xn[cc].z,
-                   xn[cc].w);
+          for (int rr = 0; rr < BS; ++rr) {
+            const float4 b01 = bv[2 * rr], b23 = bv[2 * rr + 1];
+            const float hr[4] = {b01.x, b01.z, b23.x, b23.z};
+            const float hi[4] = {b01.y, b01.w, b23.y, b23.w};
+#pragma unroll
+            for (int cc = 0; cc < BS; ++cc) {
+              if constexpr (VPL == 1) {
+                cmac(acc[rr][0][0], acc[rr][0][1], hr[cc], hi[cc], xn[cc].x,
+                     xn[cc].y);
+              } else {
+                cmac(acc[rr][0][0], acc[rr][0][1], hr[cc], hi[cc], xn[cc].x,
+                     xn[cc].y);
+                cmac(acc[rr][1][0], acc[rr][1][1], hr[cc], hi[cc], xn[cc].z,
+                     xn[cc].w);
+              }
             }
           }
         }
-      }
 #pragma unroll
-      for (int rr = 0; rr < BS; ++rr) {
-        const int64_t orow = (i * BS + rr) * rp + col;
-        float o[VPL][2];
-        if constexpr (PHASE == 0) {
+        for (int rr = 0; rr < BS; ++rr) {
+          const int64_t orow = (i * BS + rr) * rp + col;
+          float o[VPL][2];
+          if constexpr (PHASE == 0) {
+#pragma unroll
+            for (int k = 0; k < VPL; ++k) {
+              o[k][0] = 0.5f * acc[rr][k][0];
+              o[k][1] = 0.5f * acc[rr][k][1];
+            }
+          } else {
+            const PT pv = P[orow];
+            if constexpr (VPL == 1) {
+              o[0][0] = acc[rr][0][0] - pv.x;
+              o[0][1] = acc[rr][0][1] - pv.y;
+            } else {
+              o[0][0] = acc[rr][0][0] - pv.x;
+              o[0][1] = acc[rr][0][1] - pv.y;
+              o[1][0] = acc[rr][1][0] - pv.z;
+              o[1][1] = acc[rr][1][1] - pv.w;
+            }
+          }
+          PT ov;
+          if constexpr (VPL == 1) {
+            ov = make_float2(o[0][0], o[0][1]);
+          } else {
+            ov = make_float4(o[0][0], o[0][1], o[1][0], o[1][1]);
+          }
+          O[orow] = ov;
+          // DOS dots of this vector: <x|x>, <o|x> (x = the row's own
+          // entries, read again: they were loaded as block 0, the diagonal
+          // block)
+          const PT xo = X[orow];
+          float xr[VPL], xim[VPL];
+          if constexpr (VPL == 1) {
+            xr[0] = xo.x; xim[0] = xo.y;
+          } else {
+            xr[0] = xo.x; xim[0] = xo.y;
+            xr[1] = xo.z; xim[1] = xo.w;
+          }
 #pragma unroll
           for (int k = 0; k < VPL; ++k) {
-            o[k][0] = 0.5f * acc[rr][k][0];
-            o[k][1] = 0.5f * acc[rr][k][1];
-          }
-        } else {
-          const PT pv = P[orow];
-          if constexpr (VPL == 1) {
-            o[0][0] = acc[rr][0][0] - pv.x;
-            o[0][1] = acc[rr][0][1] - pv.y;
-          } else {
-            o[0][0] = acc[rr][0][0] - pv.x;
-            o[0][1] = acc[rr][0][1] - pv.y;
-            o[1][0] = acc[rr][1][0] - pv.z;
-            o[1][1] = acc[rr][1][1] - pv.w;
+            fn[k] = fmaf(xr[k], xr[k], fmaf(xim[k], xim[k], fn[k]));
+            fr[k] = fmaf(o[k][0], xr[k], fmaf(o[k][1], xim[k], fr[k]));
+            fi[k] = fmaf(o[k][0], xim[k], fmaf(-o[k][1], xr[k], fi[k]));
           }
         }
-        PT ov;
-        if constexpr (VPL == 1) {
-          ov = make_float2(o[0][0], o[0][1]);
-        } else {
-          ov = make_float4(o[0][0], o[0][1], o[1][0], o[1][1]);
-        }
-        O[orow] = ov;
-        // DOS dots of this vector: <x|x>, <o|x> (x = the row's own entries)
-        float xr[VPL], xim[VPL];
-        if constexpr (VPL == 1) {
-          xr[0] = xo[rr].x; xim[0] = xo[rr].y;
-        } else {
-          xr[0] = xo[rr].x; xim[0] = xo[rr].y;
-          xr[1] = xo[rr].z; xim[1] = xo[rr].w;
-        }
+        if (++pending == FLUSH) {
 #pragma unroll
-        for (int k = 0; k < VPL; ++k) {
-          fn[k] = fmaf(xr[k], xr[k], fmaf(xim[k], xim[k], fn[k]));
-          fr[k] = fmaf(o[k][0], xr[k], fmaf(o[k][1], xim[k], fr[k]));
-          fi[k] = fmaf(o[k][0], xim[k], fmaf(-o[k][1], xr[k], fi[k]));
+          for (int k = 0; k < VPL; ++k) {
+            my[k * 3 + 0] += (double)fn[k];
+            my[k * 3 + 1] += (double)fr[k];
+            my[k * 3 + 2] += (double)fi[k];
+            fn[k] = fr[k] = fi[k] = 0.f;
+          }
+          pending = 0;
         }
       }
-      if (++pending == FLUSH) {
-#pragma unroll
-        for (int k = 0; k < VPL; ++k) {
-          my[k * 3 + 0] += (double)fn[k];
-          my[k * 3 + 1] += (double)fr[k];
-          my[k * 3 + 2] += (double)fi[k];
-          fn[k] = fr[k] = fi[k] = 0.f;
-        }
-        pending = 0;
-      }
+      __syncthreads();   // buffer buf is restaged at t + 2
     }
 #pragma unroll
     for (int k = 0; k < VPL; ++k) {
