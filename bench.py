@@ -561,14 +561,20 @@ def run_batch(args):
         times.append(bd.stats()[0])
     ms = float(np.median(times))
     _, nodes, vpl = bd.stats()
+    ell_k = bd.ell_width()
     # Kwant CSR nnz (exact zeros dropped): 4 per site onsite, 8 per
     # directed hopping block (Gamma_0 diagonal + tau_x (x) sigma_j)
     nnz = int(sum(4 * L ** 3 + 8 * 6 * L * L * (L - 1) for L in Ls))
     orbs = int(sum(4 * L ** 3 for L in Ls))
     Rpad = -(-R // 32) * 32
-    # algorithmic bytes per step: ELL-BSR index + blocks, 3 vector passes
-    B = int(sum(int(L) ** 3 * 8 * (4 + 16 * 8) for L in Ls)
-            + 3 * orbs * Rpad * 8)
+    # algorithmic bytes per step: the stored matrix once (orbital-row ELL:
+    # K entries of 4 + 8 bytes per row; BSR: 8 blocks of 4 + 128 bytes per
+    # block row), 3 vector passes (x, alpha_{n-1}, out)
+    if ell_k:
+        mat = orbs * ell_k * 12
+    else:
+        mat = int(sum(int(L) ** 3 * 8 * (4 + 16 * 8) for L in Ls))
+    B = int(mat + 3 * orbs * Rpad * 8)
     steps = M // 2
     achieved = B * steps / (ms / 1e3) / 1e9
     peaks = {}
@@ -587,6 +593,8 @@ def run_batch(args):
                                           R, M),
                    'L': [int(x) for x in Ls], 'orbitals': orbs, 'nnz': nnz,
                    'graph_nodes': nodes, 'vectors_per_lane': vpl,
+                   'step_format': ('orbital-row ELL, width %d' % ell_k)
+                   if ell_k else 'BSR 4x4',
                    'prepare_s': prep_s},
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm,
                      'unit': 'GB/s', 'frac': achieved / hbm, 'traffic': None,

@@ -115,6 +115,7 @@ def _load():
         'kpm_batch_add_wilson_dirac': [P, I64, D, D, C.c_uint64, D, D],
         'kpm_batch_run': [P, P],
         'kpm_batch_stats': [P, P, P, P],
+        'kpm_batch_format': [P, P],
         'kpm_batch_destroy': [P],
         'kpm_profile': [P, I],
         'kpm_profile_read': [P, P, P],
@@ -465,6 +466,11 @@ class Batch:
         check(lib.kpm_batch_stats(self._b, C.byref(ms), C.byref(nodes),
                                   C.byref(vpl)))
         return ms.value, nodes.value, vpl.value
+
+    def ell_width(self):
+        k = C.c_int()
+        check(lib.kpm_batch_format(self._b, C.byref(k)))
+        return k.value
 
     def close(self):
         if getattr(self, '_b', None):

@@ -126,3 +126,8 @@ class BatchedDOS:
         """(device ms of the last run, graph kernel nodes, vectors per
         lane chosen by the autotuner)."""
         return self._b.stats()
+
+    def ell_width(self):
+        """Orbital-row ELL width of the step kernel (0: dense 4 x 4 blocks);
+        chosen at the first run."""
+        return self._b.ell_width()

@@ -76,3 +76,55 @@ def test_batch_rejects_bad_input():
     wide = sp.random(40, 40, density=1.0, format='csr') + 0j
     with pytest.raises(ValueError):
         bd.add_matrix(wide + wide.conj().T, (-50.0, 50.0))  # > 8 blocks/row
+
+
+def test_sparse_blocks_run_as_orbital_ell(monkeypatch):
+    """Wilson-Dirac blocks are half empty: the batch can convert them to an
+    orbital-row ELL (13 entries per row, width 16) on the device; forced
+    either way, the two step kernels agree with each other and with the
+    oracle (the autotuner picks the faster one)."""
+    from kwant_gb300 import batch
+    R, M, seed = 8, 40, 3
+    mats = [_host_wilson_dirac(4, 1.5, 2.0, 5), _host_wilson_dirac(3, 1.5, 0.7, 6)]
+
+    def run():
+        bd = batch.BatchedDOS(R, M, seed=seed)
+        for H in mats:
+            bd.add_matrix(H, _gershgorin(H))
+        bd.add_wilson_dirac(5, m=1.5, W=1.0, seed=9,
+                            bounds=_gershgorin(_host_wilson_dirac(5, 1.5, 1.0, 9)))
+        return bd, bd.moments()
+
+    monkeypatch.setenv('KPM_BATCH_FORMAT', 'ell')
+    bd_ell, m_ell = run()
+    assert bd_ell.ell_width() == 16
+    monkeypatch.setenv('KPM_BATCH_FORMAT', 'bsr')
+    bd_bsr, m_bsr = run()
+    assert bd_bsr.ell_width() == 0
+    assert np.max(np.abs(m_ell - m_bsr)) <= 1e-6 * np.max(np.abs(m_bsr))
+    for s, H in enumerate(mats):
+        a, b = bd_ell.scales[s]
+        vecs = batch.random_phase_vectors(seed, s, R, H.shape[0])
+        ref = _oracle_mean(H, a, b, vecs, M)
+        assert np.max(np.abs(m_ell[s] - ref)) / np.max(np.abs(ref)) < 1e-5
+
+
+def test_dense_blocks_stay_bsr():
+    from kwant_gb300 import batch
+    rng = np.random.RandomState(0)
+    n = 32                # 8 block rows, 5 dense 4x4 blocks: 20 per row
+    A = sp.random(n, n, density=1.0, random_state=rng, dtype=float)
+    mask = sp.kron(sp.diags([1.0] * 5, [-2, -1, 0, 1, 2], shape=(8, 8)),
+                   np.ones((4, 4)))
+    H = A.multiply(mask) * (1 + 0.5j)
+    H = (H + H.conj().T).tocsr()
+    assert np.diff(H.indptr).max() == 20
+    R, M = 4, 16
+    bd = batch.BatchedDOS(R, M, seed=1)
+    bd.add_matrix(H, _gershgorin(H))
+    mom = bd.moments()
+    assert bd.ell_width() == 0
+    a, b = bd.scales[0]
+    vecs = batch.random_phase_vectors(1, 0, R, n)
+    ref = _oracle_mean(H, a, b, vecs, M)
+    assert np.max(np.abs(mom[0] - ref)) / np.max(np.abs(ref)) < 1e-5
