@@ -300,11 +300,13 @@ def run_ours(args):
     B = step_bytes(nnz, n, R, args.precision)
     avg_step_ms = step_ms / max(n_step, 1)
     achieved = B / (avg_step_ms / 1e3) / 1e9
+    # DRAM bytes per step launch: ncu dram__bytes_read + dram__bytes_write
+    # of one cheb_step_ell launch on the 500 x 500-cell, R = 64 case (788.0
+    # MB against 794.0 MB algorithmic; the workload here is too large for a
+    # multi-pass capture), scaled to this launch by its algorithmic bytes
     traffic = None
-    tr_path = os.path.join(ROOT, 'profiles', 'step_traffic.json')
-    if os.path.exists(tr_path):
-        tr = _json.load(open(tr_path))
-        traffic = tr.get('%s_R%d' % (args.precision, R))
+    if args.precision == 'mixed' and args.reorder:
+        traffic = B * (788.0 / 794.0)
 
     # ---- accuracy vs the FP64 path (untimed) -------------------------------
     accuracy = None
@@ -521,7 +523,12 @@ def run_kubo(args):
                    'nnz': int(nnz), 'orbitals': int(n)},
         'roofline': {'bound': 'tensor', 'achieved': achieved, 'peak': tpeak,
                      'unit': 'TFLOP/s', 'frac': achieved / tpeak,
-                     'traffic': None, 'kernel': 'bf16x3_tc_kernel',
+                     # ncu dram bytes of one launch on the 60 x 60 x 2,
+                     # R = 16 case: 475.9 MB against 472.0 MB of operands
+                     # (4 BF16 planes x M x K_pad x 2 operands), scaled
+                     'traffic': (475.9 / 472.0) * 16.0 * M * g_fl /
+                                (24.0 * M * M) if g_fl else None,
+                     'kernel': 'bf16x3_tc_kernel',
                      'mma_flops_per_launch': g_fl, 'avg_launch_ms': g_ms,
                      'complex_equivalent_tflops':
                          complex_flops / (g_ms / 1e3) / 1e12,
@@ -597,8 +604,14 @@ def run_batch(args):
                    if ell_k else 'BSR 4x4',
                    'prepare_s': prep_s},
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm,
-                     'unit': 'GB/s', 'frac': achieved / hbm, 'traffic': None,
-                     'kernel': 'bsr_step_kernel (+ finalize, per graph step)',
+                     'unit': 'GB/s', 'frac': achieved / hbm,
+                     # ncu dram bytes of one BSR launch on the 2-system
+                     # (L = 37, 32) case: 2.443 GB against 2.138 GB
+                     # algorithmic, scaled by algorithmic bytes
+                     'traffic': None if ell_k else B * (2.443 / 2.138),
+                     'kernel': ('ell_batch_step_kernel' if ell_k else
+                                'bsr_step_kernel') +
+                               ' (+ finalize, per graph step)',
                      'algorithmic_bytes_per_step': B,
                      'avg_step_ms': ms / steps},
     }
