@@ -141,6 +141,20 @@ KPM_API int kpm_block_destroy(kpm_block* blk);
 /* Copy the current recursion state (alpha_{n-1}, alpha_n) to the host, each
  * R x N complex128 (the reference's _last_two_alphas, kwant/kpm.py:486-488). */
 KPM_API int kpm_block_state(kpm_block* blk, double* alpha_prev, double* alpha_cur);
+/* Checkpoint / restore of a block's recursion, for resuming long moment runs
+ * in another process (the reference keeps _moments_list and
+ * _last_two_alphas in memory only, kwant/kpm.py:486-490).  checkpoint
+ * reports the number of matvecs applied, the mode (-1 none, 0 DOS,
+ * 1 operator) and, if mu01 is not NULL, the per-vector mu_0, mu_1 of the DOS
+ * doubling (R x 2 complex128).  restore sets that state on a block created
+ * with the same starting vectors and handle: alpha_prev, alpha_cur as
+ * returned by kpm_block_state (R x N complex128; not needed when
+ * steps_done is 0). */
+KPM_API int kpm_block_checkpoint(kpm_block* blk, int64_t* steps_done, int* mode,
+                                 double* mu01);
+KPM_API int kpm_block_restore(kpm_block* blk, int64_t steps_done, int mode,
+                              const double* alpha_prev, const double* alpha_cur,
+                              const double* mu01);
 
 /* ---- moments -----------------------------------------------------------------
  * DOS moments (operator=None) of SpectralDensity._update_moments_list,

@@ -6,6 +6,7 @@ raises ``ImportError``, and every compute call without a CUDA device raises
 """
 
 import ctypes as C
+import weakref
 import os
 
 import numpy as np
@@ -95,6 +96,8 @@ def _load():
         'kpm_block_randomize': [P, C.c_uint64],
         'kpm_block_destroy': [P],
         'kpm_block_state': [P, P, P],
+        'kpm_block_checkpoint': [P, P, P, P],
+        'kpm_block_restore': [P, I64, I, P, P, P],
         'kpm_block_dos_moments': [P, I64, I64, P],
         'kpm_op_create': [P, P, P],
         'kpm_op_destroy': [P],
@@ -215,6 +218,7 @@ class Handle:
         self.N = csr.shape[0]
         self.reorder = bool(reorder)
         h = C.c_void_p()
+        self._children = weakref.WeakSet()
         check(lib.kpm_create_ex(csr.ref(), self.a, self.b, precision,
                                 FLAG_REORDER if reorder else 0, C.byref(h)))
         self._h = h
@@ -264,6 +268,11 @@ class Handle:
                                    float(s2)))
 
     def close(self):
+        # blocks and operators hold device state tied to the handle: free
+        # them first (they are weakly tracked; see Block.close for the
+        # order-free case of garbage collection at interpreter exit)
+        for child in list(getattr(self, '_children', ())):
+            child.close()
         if getattr(self, '_h', None):
             lib.kpm_destroy(self._h)
             self._h = None
@@ -285,6 +294,7 @@ class Block:
         check(lib.kpm_block_create(handle.ptr, ptr(vecs), self.R,
                                    1 if keep_a0 else 0, C.byref(b)))
         self._b = b
+        handle._children.add(self)
 
     def dos_moments(self, m_start, m_end):
         out = np.empty((self.R, m_end - m_start), dtype=np.complex128)
@@ -311,9 +321,34 @@ class Block:
         check(lib.kpm_block_state(self._b, ptr(prev), ptr(cur)))
         return prev, cur
 
+    def checkpoint(self):
+        """(steps_done, mode, mu01 (R x 2), alpha_prev, alpha_cur); the
+        vectors are None before the first step."""
+        steps, mode = C.c_int64(), C.c_int()
+        mu01 = np.empty((self.R, 2), dtype=np.complex128)
+        check(lib.kpm_block_checkpoint(self._b, C.byref(steps),
+                                       C.byref(mode), ptr(mu01)))
+        prev = cur = None
+        if steps.value > 0:
+            prev, cur = self.state()
+        return steps.value, mode.value, mu01, prev, cur
+
+    def restore(self, steps, mode, mu01, prev=None, cur=None):
+        mu01 = c128(mu01)
+        if steps > 0:
+            prev, cur = c128(prev), c128(cur)
+            check(lib.kpm_block_restore(self._b, int(steps), int(mode),
+                                        ptr(prev), ptr(cur), ptr(mu01)))
+        else:
+            check(lib.kpm_block_restore(self._b, 0, int(mode), None, None,
+                                        ptr(mu01)))
+
     def close(self):
         if getattr(self, '_b', None):
-            lib.kpm_block_destroy(self._b)
+            # a block outliving its handle (finalizers of a reference cycle
+            # run in any order) must not touch the destroyed handle
+            if getattr(self.handle, '_h', None):
+                lib.kpm_block_destroy(self._b)
             self._b = None
 
     def __del__(self):
@@ -335,6 +370,7 @@ class Op:
         o = C.c_void_p()
         check(lib.kpm_op_create(handle.ptr, C.byref(d), C.byref(o)))
         self._o = o
+        handle._children.add(self)
 
     @property
     def ptr(self):
@@ -348,7 +384,8 @@ class Op:
 
     def close(self):
         if getattr(self, '_o', None):
-            lib.kpm_op_destroy(self._o)
+            if getattr(self.handle, '_h', None):
+                lib.kpm_op_destroy(self._o)
             self._o = None
 
     def __del__(self):

@@ -1037,6 +1037,57 @@ int kpm_block_destroy(kpm_block* b) {
   return KPM_OK;
 }
 
+int kpm_block_checkpoint(kpm_block* b, int64_t* steps_done, int* mode,
+                         double* mu01) {
+  KPM_REQUIRE(b && steps_done && mode, "kpm_block_checkpoint: null argument");
+  *steps_done = b->steps_done;
+  *mode = b->mode;
+  if (mu01) {
+    KPM_CUDA(cudaMemcpyAsync(mu01, b->mu01, (size_t)b->R * 2 * sizeof(double2),
+                             cudaMemcpyDeviceToHost, b->h->stream));
+    KPM_CUDA(cudaStreamSynchronize(b->h->stream));
+  }
+  return KPM_OK;
+}
+
+int kpm_block_restore(kpm_block* b, int64_t steps_done, int mode,
+                      const double* alpha_prev, const double* alpha_cur,
+                      const double* mu01) {
+  KPM_REQUIRE(b, "kpm_block_restore: null block");
+  KPM_REQUIRE(steps_done >= 0 && mode >= -1 && mode <= 1,
+              "kpm_block_restore: invalid state (steps %lld, mode %d)",
+              (long long)steps_done, mode);
+  kpm_handle* h = b->h;
+  if (steps_done == 0) {
+    if (!b->keep_a0 && b->steps_done != 0) {
+      set_error("kpm_block_restore: block was created without keep_a0");
+      return KPM_ESTATE;
+    }
+    b->p_cur = b->a0;
+    b->p_prev = nullptr;
+  } else {
+    KPM_REQUIRE(alpha_prev && alpha_cur,
+                "kpm_block_restore: both Chebyshev vectors are needed");
+    // alpha_n in buf[0], alpha_{n-1} in buf[1]; the next step writes
+    // alpha_{n+1} over alpha_{n-1} (when the block does not keep a0, a0
+    // is buf[1] and is not needed again)
+    KPM_TRY(upload_vectors(h, alpha_cur, b->R, b->N, b->Rpad, b->buf[0]));
+    KPM_TRY(upload_vectors(h, alpha_prev, b->R, b->N, b->Rpad, b->buf[1]));
+    b->p_cur = b->buf[0];
+    b->p_prev = b->buf[1];
+  }
+  if (mu01) {
+    KPM_CUDA(cudaMemsetAsync(b->mu01, 0, (size_t)b->Rpad * 2 * sizeof(double2),
+                             h->stream));
+    KPM_CUDA(cudaMemcpyAsync(b->mu01, mu01, (size_t)b->R * 2 * sizeof(double2),
+                             cudaMemcpyHostToDevice, h->stream));
+  }
+  KPM_CUDA(cudaStreamSynchronize(h->stream));
+  b->steps_done = steps_done;
+  b->mode = mode;
+  return KPM_OK;
+}
+
 int kpm_block_state(kpm_block* b, double* alpha_prev, double* alpha_cur) {
   KPM_REQUIRE(b && alpha_cur, "kpm_block_state: null argument");
   if (alpha_prev) {

@@ -310,7 +310,9 @@ int kpm_block_op_moments(kpm_block* b, kpm_op* op, int64_t m_start,
       return KPM_ESTATE;
     }
   } else if (b->mode != 1 || b->steps_done != m_start - 1 ||
-             b->op_tag != (const void*)op) {
+             (b->op_tag != nullptr && b->op_tag != (const void*)op)) {
+    // (a block restored from a checkpoint has no operator yet: its bra
+    // factors are recomputed below from a0)
     set_error("kpm_block_op_moments: cannot resume at moment %lld",
               (long long)m_start);
     return KPM_ESTATE;

@@ -74,7 +74,7 @@ def _is_system(obj):
 
 
 def _is_local_operator(obj):
-    return type(obj).__name__ in ('Density', 'Current') and \
+    return type(obj).__name__ in ('Density', 'Current', 'Source') and \
         hasattr(obj, 'where') and hasattr(obj, 'bind')
 
 
@@ -356,40 +356,12 @@ class SpectralDensity:
         self.eps = eps
         self._precision = _precision(precision)
 
-        if _is_system(hamiltonian):
-            hamiltonian = hamiltonian.hamiltonian_submatrix(params=params,
-                                                            sparse=True)
-        try:
-            hamiltonian = csr_matrix(hamiltonian)
-        except Exception:
-            raise ValueError("'hamiltonian' is neither a matrix "
-                             "nor a Kwant system.")
-        if hamiltonian.ndim != 2 or hamiltonian.shape[0] != \
-                hamiltonian.shape[1]:
-            raise ValueError("'hamiltonian' is neither a matrix "
-                             "nor a Kwant system.")
-
-        # operator: lowered to the device term form (kwant/kpm.py:187-198)
-        if operator is None:
-            self.operator = None
-            self._lowered = None
-        elif _is_local_operator(operator):
-            self.operator = operator.bind(params=params)
-            self._lowered = _operator.lower(self.operator, params=params)
-        elif callable(operator):
-            raise NotImplementedError(
-                'an arbitrary Python callable operator cannot run on the '
-                'device; pass a kwant Density/Current operator or a matrix')
-        elif hasattr(operator, 'dot'):
-            operator = csr_matrix(operator)
-            self.operator = operator
-            self._lowered = _operator.lower_matrix(operator)
-        else:
-            raise ValueError("Parameter 'operator' has no '.dot' "
-                             "attribute and is not callable.")
+        hamiltonian = self._bind(hamiltonian, params, operator)
 
         self.mean = mean
         rng = ensure_rng(rng)
+        self._rng = rng if vector_factory is None else None
+        self._reorder = _reorder_default(reorder, self._precision)
         self._v0 = np.exp(2j * np.pi * rng.random_sample(hamiltonian.shape[0]))
 
         if eps <= 0:
@@ -434,9 +406,7 @@ class SpectralDensity:
         num_vectors = self._vector_factory.num_vectors
 
         self._handle = _lib.Handle(_lib.Csr(hamiltonian), self._a, self._b,
-                                   self._precision,
-                                   reorder=_reorder_default(reorder,
-                                                            self._precision))
+                                   self._precision, reorder=self._reorder)
         self._op = None if self._lowered is None else \
             _lib.Op(self._handle, self._lowered)
         self._batches = []
@@ -448,6 +418,42 @@ class SpectralDensity:
 
         self.kernel = kernel if kernel is not None else jackson_kernel
         self._reconstruct()
+
+    def _bind(self, hamiltonian, params, operator):
+        """Hamiltonian as CSR and the operator lowered to the device term
+        form (kwant/kpm.py:172-198)."""
+        if _is_system(hamiltonian):
+            hamiltonian = hamiltonian.hamiltonian_submatrix(params=params,
+                                                            sparse=True)
+        try:
+            hamiltonian = csr_matrix(hamiltonian)
+        except Exception:
+            raise ValueError("'hamiltonian' is neither a matrix "
+                             "nor a Kwant system.")
+        if hamiltonian.ndim != 2 or hamiltonian.shape[0] != \
+                hamiltonian.shape[1]:
+            raise ValueError("'hamiltonian' is neither a matrix "
+                             "nor a Kwant system.")
+
+        # operator: lowered to the device term form (kwant/kpm.py:187-198)
+        if operator is None:
+            self.operator = None
+            self._lowered = None
+        elif _is_local_operator(operator):
+            self.operator = operator.bind(params=params)
+            self._lowered = _operator.lower(self.operator, params=params)
+        elif callable(operator):
+            raise NotImplementedError(
+                'an arbitrary Python callable operator cannot run on the '
+                'device; pass a kwant Density/Current operator or a matrix')
+        elif hasattr(operator, 'dot'):
+            operator = csr_matrix(operator)
+            self.operator = operator
+            self._lowered = _operator.lower_matrix(operator)
+        else:
+            raise ValueError("Parameter 'operator' has no '.dot' "
+                             "attribute and is not callable.")
+        return hamiltonian
 
     # -- public properties -------------------------------------------------
     @property
@@ -638,6 +644,116 @@ class SpectralDensity:
         self.num_moments += int(num_moments)
         self._reconstruct()
 
+    # -- checkpoints (no reference counterpart) ------------------------------
+    def save(self, file):
+        """Write a checkpoint (numpy .npz) from which ``load`` resumes the
+        recursion exactly: the moments, the state the reference keeps in
+        memory (``_last_two_alphas`` and the per-vector mu_0, mu_1 of the
+        DOS doubling, kwant/kpm.py:486-490), the starting vectors, the
+        rescaling, the settings and the random-vector stream's state."""
+        if not self._vector_factory.accumulate:
+            raise ValueError("a checkpoint needs accumulate_vectors=True "
+                             "(the recursion state of every vector)")
+        kname = {jackson_kernel: 'jackson', lorentz_kernel: 'lorentz'}.get(
+            self.kernel, '')
+        d = {'version': 1, 'a': self._a, 'b': self._b, 'eps': self.eps,
+             'n': self._ham_csr.shape[0], 'num_moments': self.num_moments,
+             'mean': self.mean, 'precision': self._precision,
+             'reorder': self._reorder, 'kernel': kname,
+             'moments': self._moments_arr, 'num_blocks': len(self._batches)}
+        if self._rng is not None and hasattr(self._rng, 'get_state'):
+            _, keys, pos, has_gauss, gauss = self._rng.get_state()
+            d.update(rng_keys=keys, rng_pos=pos, rng_has_gauss=has_gauss,
+                     rng_gauss=gauss)
+        saved = self._vector_factory.saved_vectors
+        for k, batch in enumerate(self._batches):
+            steps, mode, mu01, prev, cur = batch.block.checkpoint()
+            R = batch.block.R
+            d['b%d_r0' % k] = batch.r0
+            d['b%d_a0' % k] = np.array([saved[r] for r in
+                                        range(batch.r0, batch.r0 + R)],
+                                       dtype=complex)
+            d['b%d_steps' % k] = steps
+            d['b%d_mode' % k] = mode
+            d['b%d_mu01' % k] = mu01
+            if steps > 0:
+                d['b%d_prev' % k] = prev
+                d['b%d_cur' % k] = cur
+        np.savez(file, **d)
+
+    @classmethod
+    def load(cls, file, hamiltonian, params=None, operator=None, *,
+             vector_factory=None, kernel=None):
+        """A SpectralDensity resumed from ``save``'s checkpoint, on the same
+        ``hamiltonian`` (and ``operator``, ``params``).  ``add_moments``
+        continues the saved recursion; ``add_vectors`` continues the saved
+        random-vector stream (or draws from ``vector_factory`` when the
+        vectors were user-supplied).  ``kernel`` is needed when a custom
+        kernel was used."""
+        z = np.load(file, allow_pickle=False)
+        if int(z['version']) != 1:
+            raise ValueError('unknown checkpoint version')
+        self = cls.__new__(cls)
+        self.eps = float(z['eps'])
+        self._precision = int(z['precision'])
+        hamiltonian = self._bind(hamiltonian, params, operator)
+        if hamiltonian.shape[0] != int(z['n']):
+            raise ValueError('the checkpoint was written for a Hamiltonian '
+                             'of size %d' % int(z['n']))
+        self.mean = bool(z['mean'])
+        self._a, self._b = float(z['a']), float(z['b'])
+        self._v0 = None
+        self._ham_csr = hamiltonian
+        self.hamiltonian = _RescaledHamiltonian(hamiltonian, self._a, self._b)
+        self.bounds = (self._b - self._a, self._b + self._a)
+        self._reorder = bool(z['reorder'])
+        nblk = int(z['num_blocks'])
+        a0s = [z['b%d_a0' % k] for k in range(nblk)]
+        nvec = sum(len(a) for a in a0s)
+        self._rng = None
+        if vector_factory is not None:
+            source = vector_factory
+        elif 'rng_keys' in z.files:
+            rng = np.random.RandomState()
+            rng.set_state(('MT19937', z['rng_keys'], int(z['rng_pos']),
+                           int(z['rng_has_gauss']), float(z['rng_gauss'])))
+            self._rng = rng
+            source = RandomVectors(hamiltonian, rng=rng)
+        else:
+            source = iter(())
+        self._vector_factory = _VectorFactory(source, num_vectors=nvec,
+                                              accumulate=True)
+        for k, a0 in enumerate(a0s):
+            r0 = int(z['b%d_r0' % k])
+            for j, v in enumerate(a0):
+                self._vector_factory.saved_vectors[r0 + j] = v
+        self._handle = _lib.Handle(_lib.Csr(hamiltonian), self._a, self._b,
+                                   self._precision, reorder=self._reorder)
+        self._op = None if self._lowered is None else \
+            _lib.Op(self._handle, self._lowered)
+        self._batches = []
+        for k, a0 in enumerate(a0s):
+            block = _lib.Block(self._handle, a0, keep_a0=True)
+            steps = int(z['b%d_steps' % k])
+            block.restore(steps, int(z['b%d_mode' % k]), z['b%d_mu01' % k],
+                          z['b%d_prev' % k] if steps else None,
+                          z['b%d_cur' % k] if steps else None)
+            self._batches.append(_Batch(int(z['b%d_r0' % k]), block))
+        self._moments_arr = z['moments']
+        self.num_moments = int(z['num_moments'])
+        kname = str(z['kernel'])
+        if kernel is not None:
+            self.kernel = kernel
+        elif kname == 'jackson':
+            self.kernel = jackson_kernel
+        elif kname == 'lorentz':
+            self.kernel = lorentz_kernel
+        else:
+            raise ValueError('the checkpoint used a custom kernel; pass it '
+                             'as kernel=')
+        self._reconstruct()
+        return self
+
     def add_vectors(self, num_vectors=None):
         """kwant/kpm.py:360-376."""
         self._vector_factory.add_vectors(num_vectors)
@@ -692,6 +808,7 @@ class Correlator:
         self._gemm = {'auto': 2, 'fp64': 0, 'bf16x3': 1,
                       'bf16x3-simt': 3}[gemm]
         self._precision = _precision(precision)
+        self._reorder = _reorder_default(reorder, self._precision)
         kwargs.pop('operator', None)
         if _is_system(hamiltonian):
             hamiltonian = hamiltonian.hamiltonian_submatrix(params=params,
@@ -762,9 +879,7 @@ class Correlator:
         kernel = kwargs.get('kernel')
         self.kernel = kernel if kernel is not None else jackson_kernel
         self._handle = _lib.Handle(_lib.Csr(hamiltonian), self._a, self._b,
-                                   self._precision,
-                                   reorder=_reorder_default(reorder,
-                                                            self._precision))
+                                   self._precision, reorder=self._reorder)
         self._compute()
 
     @property

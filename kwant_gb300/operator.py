@@ -22,7 +22,7 @@ from dataclasses import dataclass
 import numpy as np
 import scipy.sparse as sp
 
-__all__ = ['Density', 'Current', 'lower', 'lower_matrix', 'act_matrix',
+__all__ = ['Density', 'Current', 'Source', 'lower', 'lower_matrix', 'act_matrix',
            'LoweredOperator']
 
 gint_dtype = np.int32
@@ -456,6 +456,17 @@ class Density(_LocalOperator):
                          check_hermiticity=check_hermiticity, sum=sum)
 
 
+class Source(_LocalOperator):
+    """kwant/operator.pyx:1003-1126: the source of a density M, the
+    per-site tensor i [(H_aa)^dagger M_a - M_a H_aa]."""
+
+    def __init__(self, syst, onsite=1, where=None, *, check_hermiticity=True,
+                 sum=False):
+        where = _normalize_site_where(syst, where)
+        super().__init__(syst, onsite, where,
+                         check_hermiticity=check_hermiticity, sum=sum)
+
+
 class Current(_LocalOperator):
     """kwant/operator.pyx:871-1000."""
 
@@ -514,7 +525,7 @@ def _operator_info(op, params=None):
     """Kind, where, onsite matrices and hopping blocks of a Density or
     Current, from this module or from the reference kwant.operator."""
     name = type(op).__name__
-    if name not in ('Density', 'Current'):
+    if name not in ('Density', 'Current', 'Source'):
         raise NotImplementedError(
             'operator %r cannot be lowered to the device' % (op,))
     where = np.asarray(op.where, dtype=np.int64)
@@ -523,7 +534,7 @@ def _operator_info(op, params=None):
     ours = isinstance(op, _LocalOperator)
     if ours:
         params = op._bound_params if op._bound else params
-    kind = 'density' if name == 'Density' else 'current'
+    kind = 'current' if name == 'Current' else 'density'
     if callable(onsite) or isinstance(onsite, collections.abc.Mapping):
         bound = getattr(op, '_bound_onsite', None) if not ours else None
         if bound is not None:
@@ -532,6 +543,24 @@ def _operator_info(op, params=None):
             mats = _eval_onsites(op.syst, onsite, where[:, 0], params)
     else:
         mats = np.asarray(onsite, complex)
+    if name == 'Source':
+        # Source MAT_ELS / ACT (kwant/operator.pyx:1062-1126) is a density
+        # with the per-site matrix Q_a = i (H_aa^dagger M_a - M_a H_aa)
+        sites = where.reshape(-1)
+        bound = getattr(op, '_bound_hamiltonian', None) if not ours else None
+        if bound is not None:
+            H_aa = _blocks_from_bsm(bound)
+        else:
+            H_aa = _hop_blocks(op.syst, np.stack([sites, sites], axis=1),
+                               params)
+        _, norbs = _site_orbitals(site_ranges, sites)
+        Ms = _blocks_for(mats if isinstance(mats, list) else mats, norbs)
+        mats = []
+        for w in range(len(sites)):
+            n = int(norbs[w])
+            H = np.asarray(H_aa[w], complex).reshape(n, n)
+            M = Ms[w]
+            mats.append(1j * (H.conj().T @ M - M @ H))
     info = dict(kind=kind, where=where if kind == 'current'
                 else where.reshape(-1), site_ranges=site_ranges,
                 onsite=mats, sum=bool(op.sum),

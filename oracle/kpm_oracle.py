@@ -327,6 +327,46 @@ def current_matels(bra, ket, site_ranges, hoppings, hop_blocks,
     return np.sum(out) if sum_ else out
 
 
+def source_matels(bra, ket, site_ranges, where, ham_blocks, onsite_blocks,
+                  sum_=False, real=False):
+    """Source MAT_ELS, kwant/operator.pyx:1091-1104:
+    q_w = i sum_i conj(bra[a_s+i]) [(H_aa^dagger M_a - M_a H_aa) ket_a]_i
+    for site w = a, with H_aa the onsite block of the Hamiltonian."""
+    start, norbs = site_orbitals(site_ranges, where)
+    out = np.zeros(len(where), dtype=complex)
+    for w in range(len(where)):
+        M = onsite_blocks if not isinstance(onsite_blocks, list) \
+            else onsite_blocks[w]
+        M = np.asarray(M, dtype=complex)
+        n = norbs[w]
+        M = M[:n, :n] if M.shape[0] > n else M
+        H = np.asarray(ham_blocks[w], dtype=complex)
+        s = start[w]
+        k = ket[s:s + n]
+        out[w] = 1j * (np.conj(bra[s:s + n]) @ (H.conj().T @ M @ k
+                                                 - M @ H @ k))
+    if real:
+        out = out.real
+    return np.sum(out) if sum_ else out
+
+
+def source_act(ket, site_ranges, where, ham_blocks, onsite_blocks):
+    """Source ACT, kwant/operator.pyx:1105-1115:
+    out[a_s+i] += i [(H_aa^dagger M_a - M_a H_aa) ket_a]_i."""
+    start, norbs = site_orbitals(site_ranges, where)
+    out = np.zeros(len(ket), dtype=complex)
+    for w in range(len(where)):
+        M = onsite_blocks if not isinstance(onsite_blocks, list) \
+            else onsite_blocks[w]
+        M = np.asarray(M, dtype=complex)
+        n = norbs[w]
+        H = np.asarray(ham_blocks[w], dtype=complex)
+        s = start[w]
+        k = ket[s:s + n]
+        out[s:s + n] += 1j * (H.conj().T @ M @ k - M @ H @ k)
+    return out
+
+
 # --------------------------------------------------------------------------
 # Correlator / Kubo-Bastin conductivity
 # --------------------------------------------------------------------------

@@ -230,6 +230,31 @@ def make_rashba_ops():
           **_sd_state(sd_cur, 'cur_'))
 
 
+def make_source_ops():
+    """Source operator (kwant/operator.pyx:1003-1126) of sigma_x on the
+    two-orbital Rashba + exchange system: local and summed, __call__, act,
+    and as the operator of a SpectralDensity."""
+    fsyst, _ = _rashba_builder(6, 1.0, 0.3, 0.2, 1.0, 5)
+    sx = lattices.SIGMAX
+    where_sites = [i for i in range(0, 36, 4)]
+    src_loc = kwant.operator.Source(fsyst, onsite=sx, where=where_sites)
+    src_sum = kwant.operator.Source(fsyst, onsite=sx, sum=True)
+    kw = dict(rng=6, num_moments=30, num_vectors=3)
+    sd_loc = kwant.kpm.SpectralDensity(fsyst, operator=src_loc, **kw)
+    sd_sum = kwant.kpm.SpectralDensity(fsyst, operator=src_sum, **kw)
+    ham = fsyst.hamiltonian_submatrix(sparse=True).tocsr()
+    lmin, lmax = _raw_bounds(ham, 0.05, 6)
+    rs = np.random.RandomState(12)
+    bra = rs.randn(ham.shape[0]) + 1j * rs.randn(ham.shape[0])
+    ket = rs.randn(ham.shape[0]) + 1j * rs.randn(ham.shape[0])
+    _save('source_ops', lmin=lmin, lmax=lmax, seed=6, eps=0.05,
+          where_sites=np.asarray(where_sites, np.int32), **_csr(ham),
+          bra=bra, ket=ket, loc_call=src_loc(bra, ket),
+          sum_call=src_sum(bra, ket), sum_self=src_sum(bra),
+          loc_act=src_loc.act(ket), sum_act=src_sum.act(ket),
+          **_sd_state(sd_loc, 'loc_'), **_sd_state(sd_sum, 'sum_'))
+
+
 def make_conductivity():
     """Kubo-Bastin sigma_xy on a small Rashba + exchange system
     (kwant/kpm.py:763-847)."""
@@ -311,6 +336,6 @@ def make_lattice_twins():
 if __name__ == '__main__':
     which = sys.argv[1:] or ['rmt', 'square100', 'chain_current',
                              'honeycomb_ldos', 'rashba_ops', 'conductivity',
-                             'lattice_twins']
+                             'lattice_twins', 'source_ops']
     for name in which:
         globals()['make_' + name]()

@@ -185,6 +185,31 @@ def test_two_orbital_operators(kpm):
     assert _rel(cur.act(g['ket']), g['cur_act']) < TOL
 
 
+def test_source_operator(kpm):
+    """kwant.operator.Source (kwant/operator.pyx:1003-1126) lowered to a
+    density with per-site matrices i (H_aa^dagger M - M H_aa)."""
+    from kwant_gb300.system import LatticeSystem
+    from kwant_gb300.operator import Source
+    g = load('source_ops')
+    ham = csr(g)
+    n = ham.shape[0]
+    syst = LatticeSystem(ham, [(0, 2, 0), (n // 2, 0, n)], np.zeros((n // 2, 2)))
+    sx = np.array([[0, 1], [1, 0]], complex)
+    s_loc = Source(syst, onsite=sx, where=list(g['where_sites']))
+    s_sum = Source(syst, onsite=sx, sum=True)
+    kw = dict(num_moments=30, num_vectors=3)
+    for op, pre in ((s_loc, 'loc_'), (s_sum, 'sum_')):
+        sd = _sd(kpm, ham, g, operator=op, **kw)
+        assert _rel(np.array(sd._moments_list), g[pre + 'moments_list']) \
+            < TOL, pre
+        assert _rel(sd.densities, g[pre + 'densities']) < TOL, pre
+    assert _rel(s_loc(g['bra'], g['ket']), g['loc_call']) < TOL
+    assert abs(s_sum(g['bra'], g['ket']) - g['sum_call']) < 1e-10
+    assert abs(s_sum(g['bra']) - g['sum_self']) < 1e-10
+    assert _rel(s_loc.act(g['ket']), g['loc_act']) < TOL
+    assert _rel(s_sum.act(g['ket']), g['sum_act']) < TOL
+
+
 def test_mixed_operator_moments(kpm):
     from kwant_gb300.system import LatticeSystem
     from kwant_gb300.operator import Density

@@ -143,6 +143,30 @@ def test_two_orbital_operators():
     assert _rel(out['densities'], g['cur_densities']) < TOL
 
 
+def test_source_operator_matches_reference():
+    g = load('source_ops')
+    ham = csr(g)
+    n = ham.shape[0]
+    sr = [(0, 2, 0), (n // 2, 0, n)]
+    sx = np.array([[0, 1], [1, 0]], complex)
+    bra, ket = g['bra'], g['ket']
+    ws = g['where_sites']
+    blocks = [ham[2 * a:2 * a + 2, 2 * a:2 * a + 2].toarray() for a in ws]
+    assert _rel(ko.source_matels(bra, ket, sr, ws, blocks, sx),
+                g['loc_call']) < TOL
+    allsites = np.arange(n // 2)
+    ball = [ham[2 * a:2 * a + 2, 2 * a:2 * a + 2].toarray() for a in allsites]
+    assert abs(ko.source_matels(bra, ket, sr, allsites, ball, sx, sum_=True)
+               - g['sum_call']) < 1e-10
+    assert abs(ko.source_matels(bra, bra, sr, allsites, ball, sx, sum_=True,
+                                real=True) - g['sum_self']) < 1e-10
+    assert _rel(ko.source_act(ket, sr, ws, blocks, sx), g['loc_act']) < TOL
+    _, vecs = ref_vectors(g['seed'], n, 3)
+    op = lambda b_, k_: ko.source_matels(b_, k_, sr, ws, blocks, sx)
+    out = ko.spectral_density(ham, vecs, g['lmin'], g['lmax'], 30, op=op)
+    assert _rel(out['densities'], g['loc_densities']) < TOL
+
+
 def test_conductivity_matches_reference():
     g = load('conductivity')
     ham = csr(g)
