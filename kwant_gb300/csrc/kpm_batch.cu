@@ -102,6 +102,27 @@ __device__ __forceinline__ void stage_tile(const SysDev& S, int64_t base,
                    threadIdx.x);
 }
 
+// Per-warp variant: the two block rows [base, base + 2) of one warp's two
+// slots (2 x 1 KB of values: 4 chunks per lane; 2 x 32 B of indices: lanes
+// 0-3), so that warps advance without CTA-wide barriers.
+constexpr int WROWS = 2;                                 // slots per warp
+constexpr int WVAL = WROWS * KB * 16;                    // float2 per stage
+constexpr int WIDX = WROWS * KB;                         // int32 per stage
+__device__ __forceinline__ void stage_warp(const SysDev& S, int64_t base,
+                                           int lane, float2* sval,
+                                           int32_t* sidx) {
+  const float4* gv = reinterpret_cast<const float4*>(S.bval + base * KB * 16);
+  float4* dv = reinterpret_cast<float4*>(sval);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int c = lane + 32 * k;                 // 128 chunks, 64 per row
+    if (base + c / 64 < S.nb) cp_async16(dv + c, gv + c);
+  }
+  if (lane < 4 && base + lane / 2 < S.nb)
+    cp_async16(reinterpret_cast<int4*>(sidx) + lane,
+               reinterpret_cast<const int4*>(S.bidx + base * KB) + lane);
+}
+
 // PHASE 0: x = a0 -> b0 (first step); 1: x = b0, prev = a0 -> b1;
 // 2: x = b1, prev = b0 -> b0; 3: x = b0, prev = b1 -> b1.
 //
@@ -112,8 +133,8 @@ __device__ __forceinline__ void stage_tile(const SysDev& S, int64_t base,
 // double-buffered one block ahead in registers.  Padding blocks (column ==
 // the row itself after the diagonal block) skip their products: adding
 // 0 * x would not change the sums.
-template <int VPL, int PHASE>
-__global__ void __launch_bounds__(STEP_THREADS, VPL == 1 ? 4 : 3)
+template <int VPL, int PHASE, int OCC>
+__global__ void __launch_bounds__(STEP_THREADS, OCC)
 bsr_step_kernel(const SysDev* __restrict__ sys,
                 const int64_t* __restrict__ prefix, int nsys, int64_t total,
                 int64_t Rpad) {
@@ -123,10 +144,12 @@ bsr_step_kernel(const SysDev* __restrict__ sys,
   const int lane = threadIdx.x & 15;
   const int slot = threadIdx.x >> 4;
   __shared__ double red[SLOTS][G * 3];
-  __shared__ __align__(16) float2 sval[2][TILE * KB * 16];
-  __shared__ __align__(16) int32_t sidx[2][TILE * KB];
+  __shared__ __align__(16) float2 sval[STEP_THREADS / 32][2][WVAL];
+  __shared__ __align__(16) int32_t sidx[STEP_THREADS / 32][2][WIDX];
   const int64_t groups = Rpad / G;
   const int64_t rp = Rpad / VPL;
+  const int wid = threadIdx.x >> 5, wl = threadIdx.x & 31;
+  const int half = slot & 1;                     // this slot's row in the warp
 
   for (int64_t w = blockIdx.x; w < total; w += gridDim.x) {
     int lo = 0, hi = nsys;   // largest s with prefix[s] <= w
@@ -162,21 +185,24 @@ bsr_step_kernel(const SysDev* __restrict__ sys,
     const int64_t first = (int64_t)xi * SLOTS;
     const int64_t tiles = first < S.nb ? (S.nb - first + stride - 1) / stride
                                        : 0;
-    if (tiles > 0) stage_tile(S, first, sval[0], sidx[0]);
+    const int64_t wfirst = first + 2 * wid;      // this warp's rows
+    if (tiles > 0) stage_warp(S, wfirst, wl, sval[wid][0], sidx[wid][0]);
     cp_async_commit();
 
     for (int64_t t = 0; t < tiles; ++t) {
       const int buf = (int)(t & 1);
       if (t + 1 < tiles)
-        stage_tile(S, first + (t + 1) * stride, sval[buf ^ 1], sidx[buf ^ 1]);
+        stage_warp(S, wfirst + (t + 1) * stride, wl, sval[wid][buf ^ 1],
+                   sidx[wid][buf ^ 1]);
       cp_async_commit();
       cp_async_wait_prev();
-      __syncthreads();
+      __syncwarp();
       const int64_t i = first + t * stride + slot;
       if (i < S.nb) {
         const float4* bvs =
-            reinterpret_cast<const float4*>(sval[buf] + slot * KB * 16);
-        const int4* ip = reinterpret_cast<const int4*>(sidx[buf] + slot * KB);
+            reinterpret_cast<const float4*>(sval[wid][buf] + half * KB * 16);
+        const int4* ip =
+            reinterpret_cast<const int4*>(sidx[wid][buf] + half * KB);
         const int4 i0 = ip[0], i1 = ip[1];
         const int cidx[KB] = {i0.x, i0.y, i0.z, i0.w,
                               i1.x, i1.y, i1.z, i1.w};
@@ -277,7 +303,7 @@ bsr_step_kernel(const SysDev* __restrict__ sys,
           pending = 0;
         }
       }
-      __syncthreads();   // buffer buf is restaged at t + 2
+      __syncwarp();   // buffer buf is restaged at t + 2
     }
 #pragma unroll
     for (int k = 0; k < VPL; ++k) {
@@ -703,6 +729,7 @@ struct kpm_batch {
   double2* d_out = nullptr;
   int vpl = 0;
   int ell = 0;               // 1: every system runs the ELL kernel
+  int occ2 = 0;              // 1: BSR VPL-2 kernel budgeted for 2 blocks/SM
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int64_t nodes = 0;
@@ -747,10 +774,14 @@ int batch_free(kpm_batch* bt) {
 
 template <int VPL, int PHASE>
 int launch_bsr(kpm_batch* bt) {
-  static int occ[2] = {-1, -1};
-  auto kern = bt->ell ? ell_batch_step_kernel<VPL, PHASE>
-                      : bsr_step_kernel<VPL, PHASE>;
-  int& o = occ[bt->ell];
+  // kernel variants: ELL, or BSR with registers budgeted for 2 or 3 (VPL 2)
+  // / 4 (VPL 1) resident blocks per SM
+  static int occ[3] = {-1, -1, -1};
+  const int var = bt->ell ? 2 : (VPL == 2 && bt->occ2 ? 1 : 0);
+  auto kern = var == 2 ? ell_batch_step_kernel<VPL, PHASE>
+              : var == 1 ? bsr_step_kernel<VPL, PHASE, 2>
+                         : bsr_step_kernel<VPL, PHASE, VPL == 1 ? 4 : 3>;
+  int& o = occ[var];
   if (o < 0) {
     int blocks = 0;
     KPM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
@@ -910,13 +941,16 @@ int prepare(kpm_batch* bt) {
   // format the arithmetic is identical across VPL, and the two formats
   // differ only in the order of the dot-product partial sums
   float best = 1e30f;
-  int best_fmt = 0;
+  int best_fmt = 0, best_occ2 = 0;
   const char* force = getenv("KPM_BATCH_FORMAT");
   const int f_lo = (have_ell && force && strcmp(force, "ell") == 0) ? 1 : 0;
-  for (int f = f_lo; f < (have_ell ? 2 : 1); ++f) {
+  for (int f = f_lo; f < (have_ell ? 2 : 1); ++f)
+  for (int o2 = 0; o2 < (f ? 1 : 2); ++o2) {
     bt->ell = f;
+    bt->occ2 = o2;
     for (int vpl = 1; vpl <= 2; ++vpl) {
       if (bt->Rpad % (16 * vpl)) continue;
+      if (o2 && vpl == 1) continue;
       KPM_TRY(launch_step_phase(bt, vpl, 0));  // warm-up
       KPM_CUDA(cudaEventRecord(bt->e0, s));
       KPM_TRY(launch_step_phase(bt, vpl, 0));
@@ -931,10 +965,12 @@ int prepare(kpm_batch* bt) {
         best = ms;
         bt->vpl = vpl;
         best_fmt = f;
+        best_occ2 = o2;
       }
     }
   }
   bt->ell = best_fmt;
+  bt->occ2 = best_occ2;
   // keep only the chosen format's matrices
   for (auto& y : bt->sys) {
     if (bt->ell) {
