@@ -297,6 +297,12 @@ KPM_API int kpm_reconstruct(int64_t R, int64_t M, int64_t W, const double* momen
                             int mean, int is_real, double a, int kernel,
                             double lorentz_l, const double* nodes, double* gammas_out,
                             double* densities_out);
+/* Chebyshev series sum_n c[n][w] T_n(x_e) at E arbitrary points (the
+ * chebval of SpectralDensity.__call__, kwant/kpm.py:263-295): coefs M x W
+ * complex128, x E doubles in [-1, 1], out E x W complex128.  numpy's
+ * Clenshaw recursion with the same rounding (results equal numpy's). */
+KPM_API int kpm_chebval(int64_t M, int64_t W, const double* coefs, int64_t E,
+                        const double* x, double* out);
 /* Kernel weights g_m (M doubles) as applied by kpm_reconstruct. */
 KPM_API int kpm_kernel_weights(int64_t M, int kernel, double lorentz_l, double* g);
 

@@ -106,6 +106,7 @@ def _load():
         'kpm_dos': [P, D, D, I, P, I64, I64, I, P, P, P],
         'kpm_reconstruct': [I64, I64, I64, P, I, I, D, I, D, P, P, P],
         'kpm_kernel_weights': [I64, I, D, P],
+        'kpm_chebval': [I64, I64, P, I64, P, P],
         'kpm_bounds': [P, P, D, I, P, P, P],
         'kpm_handle_matvec': [P, P, P],
         'kpm_correlator_moments': [P, D, D, P, P, P, I64, I64, I, I, P],
@@ -406,6 +407,22 @@ def reconstruct(moments, mean, is_real, a, kernel, lorentz_l, nodes):
                               float(lorentz_l), ptr(nodes), ptr(gam),
                               ptr(rho)))
     return gam, rho
+
+
+def chebval(x, coefs):
+    """numpy.polynomial.chebyshev.chebval(x, coefs) (tensor form) on the
+    device: coefs (M, ...) complex, x any shape -> coefs.shape[1:] +
+    x.shape complex."""
+    c = np.asarray(coefs, dtype=np.complex128)
+    M = c.shape[0]
+    tail = c.shape[1:]
+    W = int(np.prod(tail)) if tail else 1
+    c2 = np.ascontiguousarray(c.reshape(M, W))
+    xs = np.asarray(x, dtype=np.float64)
+    xf = np.ascontiguousarray(xs.reshape(-1))
+    out = np.empty((xf.size, W), dtype=np.complex128)
+    check(lib.kpm_chebval(M, W, ptr(c2), xf.size, ptr(xf), ptr(out)))
+    return out.T.reshape(tail + xs.shape)
 
 
 def kernel_weights(M, kernel, lorentz_l=4.0):

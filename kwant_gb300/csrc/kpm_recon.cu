@@ -245,7 +245,80 @@ __global__ void integral_factor_kernel(int64_t M,
 
 using namespace kpm;
 
+// Chebyshev series at arbitrary points, one thread per (point, column):
+// numpy.polynomial.chebyshev.chebval's Clenshaw recursion (c0 = c[-2],
+// c1 = c[-1]; c0, c1 = c[-i] - c1, c0 + c1 * 2x; result c0 + c1 x) with
+// the same separately rounded products and sums, so results are those of
+// numpy bit for bit.
+__global__ void chebval_kernel(int64_t M, int64_t W,
+                               const double2* __restrict__ c, int64_t E,
+                               const double* __restrict__ x,
+                               double2* __restrict__ out) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= E * W) return;
+  const int64_t e = t / W, w = t % W;
+  const double xe = x[e];
+  double2 c0, c1;
+  if (M == 1) {
+    c0 = c[w];
+    c1 = make_double2(0.0, 0.0);
+  } else {
+    const double x2 = __dmul_rn(2.0, xe);
+    c0 = c[(M - 2) * W + w];
+    c1 = c[(M - 1) * W + w];
+    for (int64_t i = 3; i <= M; ++i) {
+      const double2 tmp = c0;
+      const double2 ci = c[(M - i) * W + w];
+      c0 = make_double2(__dsub_rn(ci.x, c1.x), __dsub_rn(ci.y, c1.y));
+      c1 = make_double2(__dadd_rn(tmp.x, __dmul_rn(c1.x, x2)),
+                        __dadd_rn(tmp.y, __dmul_rn(c1.y, x2)));
+    }
+  }
+  out[t] = make_double2(__dadd_rn(c0.x, __dmul_rn(c1.x, xe)),
+                        __dadd_rn(c0.y, __dmul_rn(c1.y, xe)));
+}
+
 extern "C" {
+
+int kpm_chebval(int64_t M, int64_t W, const double* coefs, int64_t E,
+                const double* x, double* out) {
+  KPM_REQUIRE(M > 0 && W > 0 && E >= 0 && coefs && (E == 0 || (x && out)),
+              "kpm_chebval: invalid argument");
+  if (E == 0) return KPM_OK;
+  int dev, sms;
+  KPM_TRY(init_device(&dev, &sms));
+  cudaStream_t s = 0;
+  double2 *dc = nullptr, *dout = nullptr;
+  double* dx = nullptr;
+  int st = dev_alloc((void**)&dc, (size_t)M * W * sizeof(double2), s);
+  if (st == KPM_OK) st = dev_alloc((void**)&dx, (size_t)E * sizeof(double), s);
+  if (st == KPM_OK)
+    st = dev_alloc((void**)&dout, (size_t)E * W * sizeof(double2), s);
+  cudaError_t e = cudaSuccess;
+  if (st == KPM_OK) {
+    e = cudaMemcpyAsync(dc, coefs, (size_t)M * W * sizeof(double2),
+                        cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dx, x, (size_t)E * sizeof(double),
+                          cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+      chebval_kernel<<<(unsigned)ceil_div(E * W, 256), 256, 0, s>>>(
+          M, W, dc, E, dx, dout);
+      count_launch(1);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(out, dout, (size_t)E * W * sizeof(double2),
+                          cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  }
+  dev_free(dc, s);
+  dev_free(dx, s);
+  dev_free(dout, s);
+  if (st != KPM_OK) return st;
+  KPM_CUDA(e);
+  return KPM_OK;
+}
 
 int kpm_kernel_weights(int64_t M, int kernel, double lorentz_l, double* g) {
   KPM_REQUIRE(M > 0 && g, "kpm_kernel_weights: invalid argument");

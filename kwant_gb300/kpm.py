@@ -33,7 +33,6 @@ import math
 from collections.abc import Iterable
 
 import numpy as np
-from numpy.polynomial.chebyshev import chebval
 from scipy.integrate import simpson
 from scipy.sparse import coo_matrix, csr_matrix
 from scipy.sparse.linalg import LinearOperator, eigsh
@@ -611,7 +610,11 @@ class SpectralDensity:
         g_e = (np.pi * np.sqrt(1 - e) * np.sqrt(1 + e))
         moments = self._moments()
         moments[1:] = 2 * moments[1:]
-        return np.transpose(chebval(e, moments) / g_e)
+        # the chebval sum runs on the device, with numpy's arithmetic
+        vals = _lib.chebval(e, moments)
+        if not np.iscomplexobj(moments):
+            vals = vals.real
+        return np.transpose(vals / g_e)
 
     def integrate(self, distribution_function=None):
         """kwant/kpm.py:297-316."""
@@ -928,6 +931,26 @@ class Correlator:
         integral = simpson(integrand, x=e_rescaled)
         prefactor = 2 * 4**2 / ((2 * self._a) ** 2)
         return prefactor * integral
+
+    def sweep(self, mu=0, temperature=0):
+        """``self(mu, temperature)`` over a grid: ``mu`` and
+        ``temperature`` broadcast against each other and the result has
+        their broadcast shape.  One vectorised Simpson integration over the
+        2M energies for all points (no reference counterpart: the reference
+        evaluates one (mu, temperature) per call, kwant/kpm.py:608-630)."""
+        mu, temperature = np.broadcast_arrays(np.asarray(mu, float),
+                                              np.asarray(temperature, float))
+        e = self.energies
+        e_rescaled = (e - self._b) / self._a
+        flat_mu, flat_t = mu.ravel(), temperature.ravel()
+        dist = np.empty((flat_mu.size, e.size))
+        for k in range(flat_mu.size):
+            dist[k] = fermi_distribution(e, flat_mu[k], flat_t[k])
+        integrand = dist / ((1 - e_rescaled ** 2) ** 2)
+        integrand = integrand * self._integral_factor
+        integral = simpson(integrand, x=e_rescaled, axis=-1)
+        prefactor = 2 * 4**2 / ((2 * self._a) ** 2)
+        return (prefactor * integral).reshape(mu.shape)
 
     def add_moments(self, num_moments=None, *, energy_resolution=None):
         """kwant/kpm.py:637-664 (recomputed on the device with the larger

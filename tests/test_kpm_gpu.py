@@ -314,6 +314,11 @@ def test_conductivity_fp64(kpm):
     vals = np.array([[cxx(mu=m, temperature=T) for m in g['mus']]
                      for T in g['temps']])
     assert _rel(vals, g['values_xx']) < 1e-9
+    # the vectorised (mu, temperature) sweep equals point-by-point calls
+    grid = cxx.sweep(mu=np.asarray(g['mus'])[None, :],
+                     temperature=np.asarray(g['temps'])[:, None])
+    assert grid.shape == vals.shape
+    assert _rel(grid, vals) < 1e-12
     cond.add_moments(16)
     vals = np.array([cond(mu=m, temperature=0.1) for m in g['mus']])
     assert _rel(vals, g['values_add']) < 1e-9
@@ -420,3 +425,32 @@ def test_repeatable(kpm):
     a = _sd(kpm, csr(g), g, num_moments=50, num_vectors=10, precision='mixed')
     b = _sd(kpm, csr(g), g, num_moments=50, num_vectors=10, precision='mixed')
     assert np.array_equal(a.densities, b.densities)
+
+
+def test_call_at_arbitrary_energies_on_device(kpm):
+    """SpectralDensity.__call__(energy) (kwant/kpm.py:263-295): the
+    Chebyshev sum runs on the device with numpy's Clenshaw arithmetic."""
+    from numpy.polynomial.chebyshev import chebval
+    from kwant_gb300.system import LatticeSystem
+    from kwant_gb300.operator import Density
+    g = load('rashba_ops')
+    ham = csr(g)
+    n = ham.shape[0]
+    syst = LatticeSystem(ham, [(0, 2, 0), (n // 2, 0, n)], g['positions'])
+    rng = np.random.RandomState(3)
+    for op in (None, Density(syst, onsite=np.diag([1.0, -1.0]),
+                             where=list(g['where_sites']))):
+        sd = _sd(kpm, ham, g, operator=op, num_moments=40, num_vectors=3)
+        lo, hi = sd.bounds
+        E = rng.uniform(lo + 0.1, hi - 0.1, size=(3, 7))
+        got = sd(E)
+        e = (E - sd._b) / sd._a
+        g_e = np.pi * np.sqrt(1 - e) * np.sqrt(1 + e)
+        mom = sd._moments()
+        mom[1:] = 2 * mom[1:]
+        ref = np.transpose(chebval(e, mom) / g_e)
+        assert got.shape == ref.shape
+        assert np.array_equal(got, ref)
+        # scalar energy
+        assert np.array_equal(sd(float(E[0, 0])),
+                              np.transpose(chebval(e[0, 0], mom) / g_e[0, 0]))
