@@ -438,8 +438,10 @@ def run_ours(args):
             'roofline': {'bound': 'hbm', 'achieved': achieved,
                          'peak': hbm_peak, 'unit': 'GB/s',
                          'frac': achieved / hbm_peak, 'traffic': traffic,
-                         'kernel': 'cheb_step_kernel (fused step + moment '
-                                   'dots)',
+                         'kernel': ('cheb_step_ell_kernel'
+                                    if args.precision == 'mixed' else
+                                    'cheb_step_kernel') +
+                                   ' (fused step + moment dots)',
                          'algorithmic_bytes_per_launch': B,
                          'avg_launch_ms': avg_step_ms,
                          'launches_timed': n_step,

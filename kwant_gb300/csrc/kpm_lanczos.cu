@@ -282,15 +282,29 @@ int kpm_bounds(const kpm_csr_desc* ham, const double* v0, double tol,
           d[j] = hc[2 * j];
           off[j] = hc[2 * j + 1];
         }
-        const double beta_k = off[k - 1];
-        th_lo = bisect_eig(d, off, k, 0);
-        th_hi = bisect_eig(d, off, k, k - 1);
-        r_lo = beta_k * last_component(d, off, k, th_lo);
-        r_hi = beta_k * last_component(d, off, k, th_hi);
+        // breakdown: beta_j ~ 0 (relative to the coefficients so far) means
+        // span(q_0..q_j) is invariant and its Ritz values are exact
+        // eigenvalues; the coefficients computed after it (from an
+        // unnormalised q) are discarded
+        int kk = k;
+        double mag = 0.0;
+        for (int j = 0; j < k; ++j) {
+          mag = std::max(mag, fabs(d[j]));
+          if (j > 0) mag = std::max(mag, fabs(off[j - 1]));
+          if (off[j] <= 1e-14 * (mag > 0 ? mag : 1.0)) {
+            kk = j + 1;
+            break;
+          }
+        }
+        const double beta_k = off[kk - 1];
+        th_lo = bisect_eig(d, off, kk, 0);
+        th_hi = bisect_eig(d, off, kk, kk - 1);
+        r_lo = beta_k * last_component(d, off, kk, th_lo);
+        r_hi = beta_k * last_component(d, off, kk, th_hi);
         const double sc = std::max(fabs(th_lo), fabs(th_hi));
         const double small = 1e-14 * (sc > 0 ? sc : 1.0);
-        if ((r_lo <= tol * sc && r_hi <= tol * sc) || beta_k <= small ||
-            k == N) {
+        if (kk < k || (r_lo <= tol * sc && r_hi <= tol * sc) ||
+            beta_k <= small || k == N) {
           converged = true;
           break;
         }
