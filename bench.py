@@ -283,9 +283,8 @@ def run_ours(args):
     clk = clocks.stop()
     t_ms = ev0.elapsed_time(ev1)
     if world > 1:
-        t = torch.tensor([t_ms], device='cuda')
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_ms = float(t.item())
+        from kwant_gb300 import replicas
+        t_ms = replicas.max_over_ranks(t_ms, device='cuda')
     ms_per_step = t_ms / args.steps
     value = world * nnz * R * M / (ms_per_step / 1e3)
 

@@ -14,7 +14,7 @@ system type they produce.
 
 __version__ = '0.1.0'
 
-from . import system, lattices  # noqa: F401  (host-only modules)
+from . import system, lattices, replicas  # noqa: F401  (host-only)
 
 
 def __getattr__(name):
