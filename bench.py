@@ -569,7 +569,7 @@ def run_batch(args):
         times.append(bd.stats()[0])
     ms = float(np.median(times))
     _, nodes, vpl = bd.stats()
-    ell_k = bd.ell_width()
+    fmt, ell_k = bd.step_format()
     # Kwant CSR nnz (exact zeros dropped): 4 per site onsite, 8 per
     # directed hopping block (Gamma_0 diagonal + tau_x (x) sigma_j)
     nnz = int(sum(4 * L ** 3 + 8 * 6 * L * L * (L - 1) for L in Ls))
@@ -578,8 +578,10 @@ def run_batch(args):
     # algorithmic bytes per step: the stored matrix once (orbital-row ELL:
     # K entries of 4 + 8 bytes per row; BSR: 8 blocks of 4 + 128 bytes per
     # block row), 3 vector passes (x, alpha_{n-1}, out)
-    if ell_k:
+    if fmt == 1:
         mat = orbs * ell_k * 12
+    elif fmt == 2:      # block columns + 16 entries (4 + 8 bytes) per row
+        mat = int(sum(int(L) ** 3 * 8 * 4 for L in Ls)) + orbs * 16 * 12
     else:
         mat = int(sum(int(L) ** 3 * 8 * (4 + 16 * 8) for L in Ls))
     B = int(mat + 3 * orbs * Rpad * 8)
@@ -601,17 +603,19 @@ def run_batch(args):
                                           R, M),
                    'L': [int(x) for x in Ls], 'orbitals': orbs, 'nnz': nnz,
                    'graph_nodes': nodes, 'vectors_per_lane': vpl,
-                   'step_format': ('orbital-row ELL, width %d' % ell_k)
-                   if ell_k else 'BSR 4x4',
+                   'step_format': ['BSR 4x4', 'orbital-row ELL, width %d'
+                                   % ell_k,
+                                   'sparse blocks (staged in shared memory)'
+                                   ][fmt],
                    'prepare_s': prep_s},
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm,
                      'unit': 'GB/s', 'frac': achieved / hbm,
                      # ncu dram bytes of one BSR launch on the 2-system
                      # (L = 37, 32) case: 2.443 GB against 2.138 GB
                      # algorithmic, scaled by algorithmic bytes
-                     'traffic': None if ell_k else B * (2.443 / 2.138),
-                     'kernel': ('ell_batch_step_kernel' if ell_k else
-                                'bsr_step_kernel') +
+                     'traffic': B * (2.443 / 2.138) if fmt == 0 else None,
+                     'kernel': ['bsr_step_kernel', 'ell_batch_step_kernel',
+                                'sb_step_kernel'][fmt] +
                                ' (+ finalize, per graph step)',
                      'algorithmic_bytes_per_step': B,
                      'avg_step_ms': ms / steps},

@@ -274,12 +274,13 @@ KPM_API int kpm_batch_run(kpm_batch* bt, double* out);
  * kernel nodes it contains; the chosen variant (vectors per lane). */
 KPM_API int kpm_batch_stats(kpm_batch* bt, double* ms, int64_t* nodes,
                             int* vectors_per_lane);
-/* Step format chosen at the first kpm_batch_run: when every row of every
- * system has at most 16 non-zero entries, the blocks are also converted on
- * the device to an orbital-row ELL (zeros dropped) and the autotuner times
- * both step kernels; ell_width is the ELL width (4..16) if ELL won, else 0
- * (dense 4 x 4 blocks). */
-KPM_API int kpm_batch_format(kpm_batch* bt, int* ell_width);
+/* Step format chosen at the first kpm_batch_run.  When every row of every
+ * system has at most 16 non-zero entries, two sparse forms are built on the
+ * device besides the dense 4 x 4 blocks (format 0): an orbital-row ELL
+ * (format 1, ell_width its width) and sparse blocks (format 2: the block
+ * rows' vector rows staged in shared memory, products over the non-zero
+ * entries only); the autotuner times all of them and keeps the fastest. */
+KPM_API int kpm_batch_format(kpm_batch* bt, int* format, int* ell_width);
 KPM_API int kpm_batch_destroy(kpm_batch* bt);
 
 /* ---- reconstruction (device) -------------------------------------------------

@@ -119,7 +119,7 @@ def _load():
         'kpm_batch_add_wilson_dirac': [P, I64, D, D, C.c_uint64, D, D],
         'kpm_batch_run': [P, P],
         'kpm_batch_stats': [P, P, P, P],
-        'kpm_batch_format': [P, P],
+        'kpm_batch_format': [P, P, P],
         'kpm_batch_destroy': [P],
         'kpm_profile': [P, I],
         'kpm_profile_read': [P, P, P],
@@ -521,10 +521,12 @@ class Batch:
                                   C.byref(vpl)))
         return ms.value, nodes.value, vpl.value
 
-    def ell_width(self):
-        k = C.c_int()
-        check(lib.kpm_batch_format(self._b, C.byref(k)))
-        return k.value
+    def step_format(self):
+        """(format, ell_width): 0 dense blocks, 1 orbital-row ELL, 2 sparse
+        blocks staged in shared memory."""
+        f, k = C.c_int(), C.c_int()
+        check(lib.kpm_batch_format(self._b, C.byref(f), C.byref(k)))
+        return f.value, k.value
 
     def close(self):
         if getattr(self, '_b', None):

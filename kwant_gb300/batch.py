@@ -127,7 +127,9 @@ class BatchedDOS:
         lane chosen by the autotuner)."""
         return self._b.stats()
 
-    def ell_width(self):
-        """Orbital-row ELL width of the step kernel (0: dense 4 x 4 blocks);
-        chosen at the first run."""
-        return self._b.ell_width()
+    def step_format(self):
+        """Step kernel chosen by the autotuner at the first run:
+        ``(format, ell_width)`` with format 0 = dense 4 x 4 blocks, 1 =
+        orbital-row ELL of width ell_width, 2 = sparse blocks staged in
+        shared memory."""
+        return self._b.step_format()

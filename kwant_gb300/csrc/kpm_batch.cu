@@ -49,6 +49,8 @@ struct SysDev {
   int ell_k;             // ELL width (0: BSR kernel)
   const int32_t* eidx;   // [4 nb][ell_k]
   const float2* eval;    // [4 nb][ell_k]
+  const int32_t* spidx;  // [4 nb][16]: panel slot q * 4 + cc of each entry
+  const float2* spval;   // [4 nb][16]: its value (sparse-block kernel)
   void* v[3];            // a0, b0, b1: [4 nb][Rpad] complex64
   double* partials;      // [Rpad * 3][xitems]
   double2* mu01;         // [Rpad][2]
@@ -577,6 +579,232 @@ ell_batch_step_kernel(const SysDev* __restrict__ sys,
   }
 }
 
+// Sparse-block entries of orbital row r: the non-zero entries of its block
+// row in (block, column) order as (panel slot q * 4 + cc, value); padding
+// (slot rr of the diagonal block, value 0) up to EK.
+__global__ void sb_fill_kernel(int64_t nb, const int32_t* __restrict__ bidx,
+                               const float2* __restrict__ bval,
+                               int32_t* __restrict__ spidx,
+                               float2* __restrict__ spval) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nb * BS) return;
+  const int64_t i = r / BS;
+  const int rr = (int)(r % BS);
+  int e = 0;
+  for (int q = 0; q < KB; ++q) {
+    if (q > 0 && bidx[i * KB + q] == (int32_t)i) continue;
+    for (int cc = 0; cc < BS; ++cc) {
+      const float2 v = bval[(i * KB + q) * 16 + rr * BS + cc];
+      if ((v.x != 0.f || v.y != 0.f) && e < EK) {
+        spidx[r * EK + e] = q * BS + cc;
+        spval[r * EK + e] = v;
+        ++e;
+      }
+    }
+  }
+  for (; e < EK; ++e) {
+    spidx[r * EK + e] = rr;
+    spval[r * EK + e] = make_float2(0.f, 0.f);
+  }
+}
+
+// Sparse-block step.  A warp owns two consecutive block rows (one per
+// 16-lane half) for a group of 16 vectors (one complex64 per lane).  The
+// vector rows of every non-padding block of the next row pair (4 rows x 16
+// vectors per block), its alpha_{n-1} rows and its entries are copied into
+// shared memory with cp.async while the current pair computes, so every
+// gather is asynchronous; the products then run over the non-zero entries
+// only (zeros of the 4 x 4 blocks skipped), reading the staged rows by
+// panel slot.  No CTA-wide barrier inside the row loop.
+constexpr int SB_WARPS = 4;
+constexpr int SB_THREADS = SB_WARPS * 32;
+constexpr int SB_SLOTS = SB_WARPS * 2;
+struct SbStage {
+  float2 x[2][KB * BS][16];    // 2 rows x 8 blocks x 4 rows x 16 vectors
+  float2 p[2][BS][16];         // alpha_{n-1}
+  float2 val[2][BS][EK];
+  int32_t pidx[2][BS][EK];
+};
+struct SbWarp {
+  SbStage st[2];
+  int32_t bidx[3][2][KB];      // block columns, staged two pairs ahead
+};
+constexpr size_t SB_SMEM = SB_WARPS * sizeof(SbWarp) +
+                           SB_SLOTS * 16 * 3 * sizeof(double);
+
+template <int PHASE>
+__device__ __forceinline__ void sb_stage_idx(const SysDev& S, int64_t base,
+                                             int lane, int32_t (*dst)[KB]) {
+  // 2 rows x 8 int32 = 4 chunks of 16 bytes
+  if (lane < 4 && base + lane / 2 < S.nb)
+    cp_async16(&dst[lane / 2][(lane % 2) * 4],
+               S.bidx + (base + lane / 2) * KB + (lane % 2) * 4);
+}
+
+template <int PHASE>
+__device__ __forceinline__ void sb_stage_data(const SysDev& S, int64_t base,
+                                              int lane, int64_t gcol,
+                                              int64_t Rpad,
+                                              const float2* X, const float2* P,
+                                              const int32_t (*bidx)[KB],
+                                              SbStage& st) {
+  // vector rows of the blocks: chunk lane of each (row, block): 4 rows x
+  // 128 bytes = 32 chunks
+  const int cc = lane >> 3, part = lane & 7;
+#pragma unroll
+  for (int s2 = 0; s2 < 2; ++s2) {
+    const int64_t i = base + s2;
+    if (i >= S.nb) continue;
+#pragma unroll
+    for (int q = 0; q < KB; ++q) {
+      const int32_t c = bidx[s2][q];
+      if (q > 0 && c == (int32_t)i) continue;     // padding block
+      cp_async16(&st.x[s2][q * BS + cc][part * 2],
+                 X + ((int64_t)c * BS + cc) * Rpad + gcol + part * 2);
+    }
+    if constexpr (PHASE != 0)
+      cp_async16(&st.p[s2][cc][part * 2],
+                 P + (i * BS + cc) * Rpad + gcol + part * 2);
+    // entries: 4 rows x 16 x 8 bytes = 32 chunks; indices 16 chunks
+    cp_async16(reinterpret_cast<float4*>(&st.val[s2][0][0]) + lane,
+               reinterpret_cast<const float4*>(S.spval + i * BS * EK) + lane);
+    if (lane < 16)
+      cp_async16(reinterpret_cast<int4*>(&st.pidx[s2][0][0]) + lane,
+                 reinterpret_cast<const int4*>(S.spidx + i * BS * EK) + lane);
+  }
+}
+
+template <int PHASE>
+__global__ void __launch_bounds__(SB_THREADS)
+sb_step_kernel(const SysDev* __restrict__ sys,
+               const int64_t* __restrict__ prefix, int nsys, int64_t total,
+               int64_t Rpad) {
+  extern __shared__ __align__(16) uint8_t sb_smem[];
+  SbWarp* wsm = reinterpret_cast<SbWarp*>(sb_smem);
+  double (*red)[16 * 3] = reinterpret_cast<double (*)[16 * 3]>(
+      sb_smem + SB_WARPS * sizeof(SbWarp));
+  constexpr int G = 16;
+  constexpr int FLUSH = 32;                  // orbital rows
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int half = lane >> 4, v = lane & 15;
+  const int slot = wid * 2 + half;
+  SbWarp& W = wsm[wid];
+  const int64_t groups = Rpad / G;
+
+  for (int64_t w = blockIdx.x; w < total; w += gridDim.x) {
+    int lo = 0, hi = nsys;   // largest s with prefix[s] <= w
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (prefix[mid] <= w) lo = mid; else hi = mid;
+    }
+    const SysDev& S = sys[lo];
+    const int64_t local = w - prefix[lo];
+    const int xi = (int)(local / groups);
+    const int g = (int)(local - (int64_t)xi * groups);
+    const int64_t gcol = (int64_t)g * G;
+    const float2* X;
+    const float2* P = nullptr;
+    float2* O;
+    if constexpr (PHASE == 0) {
+      X = (const float2*)S.v[0]; O = (float2*)S.v[1];
+    } else if constexpr (PHASE == 1) {
+      X = (const float2*)S.v[1]; P = (const float2*)S.v[0];
+      O = (float2*)S.v[2];
+    } else if constexpr (PHASE == 2) {
+      X = (const float2*)S.v[2]; P = (const float2*)S.v[1];
+      O = (float2*)S.v[1];
+    } else {
+      X = (const float2*)S.v[1]; P = (const float2*)S.v[2];
+      O = (float2*)S.v[2];
+    }
+    double dn = 0.0, dr = 0.0, di = 0.0;
+    float fn = 0.f, fr = 0.f, fi = 0.f;
+    int pending = 0;
+    const int64_t stride = (int64_t)S.xitems * SB_SLOTS;
+    const int64_t wfirst = (int64_t)xi * SB_SLOTS + 2 * wid;
+    const int64_t pairs = wfirst < S.nb ? (S.nb - wfirst + stride - 1) / stride
+                                        : 0;
+    // prologue: indices of pairs 0 and 1, then the data of pair 0
+    if (pairs > 0) sb_stage_idx<PHASE>(S, wfirst, lane, W.bidx[0]);
+    if (pairs > 1) sb_stage_idx<PHASE>(S, wfirst + stride, lane, W.bidx[1]);
+    cp_async_commit();
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncwarp();
+    if (pairs > 0)
+      sb_stage_data<PHASE>(S, wfirst, lane, gcol, Rpad, X, P, W.bidx[0],
+                           W.st[0]);
+    cp_async_commit();
+
+    for (int64_t t = 0; t < pairs; ++t) {
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+      __syncwarp();
+      const int64_t base = wfirst + t * stride;
+      if (t + 2 < pairs)
+        sb_stage_idx<PHASE>(S, base + 2 * stride, lane,
+                            W.bidx[(int)((t + 2) % 3)]);
+      if (t + 1 < pairs)
+        sb_stage_data<PHASE>(S, base + stride, lane, gcol, Rpad, X, P,
+                             W.bidx[(int)((t + 1) % 3)], W.st[(t + 1) & 1]);
+      cp_async_commit();
+      const SbStage& st = W.st[t & 1];
+      const int64_t i = base + half;
+      if (i < S.nb) {
+#pragma unroll
+        for (int rr = 0; rr < BS; ++rr) {
+          float ar = 0.f, ai = 0.f;
+#pragma unroll
+          for (int e4 = 0; e4 < EK / 4; ++e4) {
+            const int4 p4 = reinterpret_cast<const int4*>(st.pidx[half][rr])[e4];
+            const float4 v01 = reinterpret_cast<const float4*>(st.val[half][rr])[2 * e4];
+            const float4 v23 = reinterpret_cast<const float4*>(st.val[half][rr])[2 * e4 + 1];
+            const float2 x0 = st.x[half][p4.x][v], x1 = st.x[half][p4.y][v];
+            const float2 x2 = st.x[half][p4.z][v], x3 = st.x[half][p4.w][v];
+            cmac(ar, ai, v01.x, v01.y, x0.x, x0.y);
+            cmac(ar, ai, v01.z, v01.w, x1.x, x1.y);
+            cmac(ar, ai, v23.x, v23.y, x2.x, x2.y);
+            cmac(ar, ai, v23.z, v23.w, x3.x, x3.y);
+          }
+          float2 o;
+          if constexpr (PHASE == 0) {
+            o = make_float2(0.5f * ar, 0.5f * ai);
+          } else {
+            const float2 pv = st.p[half][rr][v];
+            o = make_float2(ar - pv.x, ai - pv.y);
+          }
+          O[(i * BS + rr) * Rpad + gcol + v] = o;
+          const float2 xo = st.x[half][rr][v];     // diagonal block, row rr
+          fn = fmaf(xo.x, xo.x, fmaf(xo.y, xo.y, fn));
+          fr = fmaf(o.x, xo.x, fmaf(o.y, xo.y, fr));
+          fi = fmaf(o.x, xo.y, fmaf(-o.y, xo.x, fi));
+          if (++pending == FLUSH) {
+            dn += (double)fn;
+            dr += (double)fr;
+            di += (double)fi;
+            fn = fr = fi = 0.f;
+            pending = 0;
+          }
+        }
+      }
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    dn += (double)fn;
+    dr += (double)fr;
+    di += (double)fi;
+    red[slot][v * 3 + 0] = dn;
+    red[slot][v * 3 + 1] = dr;
+    red[slot][v * 3 + 2] = di;
+    __syncthreads();
+    double* dst = S.partials + (int64_t)g * G * 3 * S.xitems + xi;
+    for (int e = threadIdx.x; e < G * 3; e += blockDim.x) {
+      double sum = 0.0;
+#pragma unroll
+      for (int q = 0; q < SB_SLOTS; ++q) sum += red[q][e];
+      dst[(int64_t)e * S.xitems] = sum;
+    }
+    __syncthreads();
+  }
+}
+
 // grid (Rpad, nsys): fixed-order sums of the partials into DOS moments
 __global__ void bsr_finalize_kernel(const SysDev* __restrict__ sys,
                                     int64_t Rpad, int mode, int64_t m_even,
@@ -715,6 +943,8 @@ struct kpm_batch {
     int ell_k = 0;
     int32_t* eidx = nullptr;
     float2* eval = nullptr;
+    int32_t* spidx = nullptr;
+    float2* spval = nullptr;
     void* v[3] = {nullptr, nullptr, nullptr};
     double* partials = nullptr;
     double2* mu01 = nullptr;
@@ -728,7 +958,8 @@ struct kpm_batch {
   int64_t total[2][2] = {{0, 0}, {0, 0}};
   double2* d_out = nullptr;
   int vpl = 0;
-  int ell = 0;               // 1: every system runs the ELL kernel
+  int ell = 0;               // step format: 0 BSR, 1 orbital-row ELL,
+                             // 2 sparse-block (staged BSR, zeros skipped)
   int occ2 = 0;              // 1: BSR VPL-2 kernel budgeted for 2 blocks/SM
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -750,6 +981,8 @@ int batch_free(kpm_batch* bt) {
     dev_free(y.bval, s);
     dev_free(y.eidx, s);
     dev_free(y.eval, s);
+    dev_free(y.spidx, s);
+    dev_free(y.spval, s);
     for (int k = 0; k < 3; ++k) dev_free(y.v[k], s);
     dev_free(y.partials, s);
     dev_free(y.mu01, s);
@@ -772,8 +1005,32 @@ int batch_free(kpm_batch* bt) {
   return KPM_OK;
 }
 
+template <int PHASE>
+int launch_sb(kpm_batch* bt) {
+  static int occ = -1;
+  if (occ < 0) {
+    KPM_CUDA(cudaFuncSetAttribute(sb_step_kernel<PHASE>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)SB_SMEM));
+    int blocks = 0;
+    KPM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &blocks, sb_step_kernel<PHASE>, SB_THREADS, SB_SMEM));
+    occ = blocks > 0 ? blocks : 1;
+  }
+  const int64_t total = bt->total[0][0];          // BSR partitions, VPL 1
+  int64_t grid = (int64_t)occ * bt->num_sms;
+  if (grid > total) grid = total;
+  sb_step_kernel<PHASE><<<(unsigned)grid, SB_THREADS, SB_SMEM, bt->stream>>>(
+      bt->d_sys[0], bt->d_prefix[0][0], (int)bt->sys.size(), total,
+      bt->Rpad);
+  count_launch(1);
+  KPM_CHECK_LAUNCH();
+  return KPM_OK;
+}
+
 template <int VPL, int PHASE>
 int launch_bsr(kpm_batch* bt) {
+  if (bt->ell == 2) return launch_sb<PHASE>(bt);
   // kernel variants: ELL, or BSR with registers budgeted for 2 or 3 (VPL 2)
   // / 4 (VPL 1) resident blocks per SM
   static int occ[3] = {-1, -1, -1};
@@ -835,6 +1092,13 @@ int choose_format(kpm_batch* bt) {
     count_launch(1);
     KPM_CHECK_LAUNCH();
     y.ell_k = K;
+    const size_t ns = (size_t)y.nb * BS * EK;
+    KPM_TRY(dev_alloc((void**)&y.spidx, ns * sizeof(int32_t), s));
+    KPM_TRY(dev_alloc((void**)&y.spval, ns * sizeof(float2), s));
+    sb_fill_kernel<<<(unsigned)ceil_div(y.nb * BS, 256), 256, 0, s>>>(
+        y.nb, y.bidx, y.bval, y.spidx, y.spval);
+    count_launch(1);
+    KPM_CHECK_LAUNCH();
   }
   KPM_CUDA(cudaStreamSynchronize(s));
   return KPM_OK;
@@ -856,7 +1120,7 @@ int launch_step_phase(kpm_batch* bt, int vpl, int phase) {
 
 int finalize_all(kpm_batch* bt, int mode, int64_t me, int64_t mo) {
   dim3 grid((unsigned)bt->Rpad, (unsigned)bt->sys.size());
-  bsr_finalize_kernel<<<grid, 128, 0, bt->stream>>>(bt->d_sys[bt->ell],
+  bsr_finalize_kernel<<<grid, 128, 0, bt->stream>>>(bt->d_sys[bt->ell == 1],
                                                     bt->Rpad, mode,
                                                     me, mo);
   count_launch(1);
@@ -874,7 +1138,7 @@ int enqueue_run(kpm_batch* bt, int vpl) {
     KPM_TRY(finalize_all(bt, 1, 2 * n, 2 * n + 1));
   }
   dim3 grid((unsigned)bt->M, (unsigned)bt->sys.size());
-  bsr_mean_kernel<<<grid, 128, 0, bt->stream>>>(bt->d_sys[bt->ell], bt->R,
+  bsr_mean_kernel<<<grid, 128, 0, bt->stream>>>(bt->d_sys[bt->ell == 1], bt->R,
                                                 bt->Rpad,
                                                 bt->M, bt->d_out);
   count_launch(1);
@@ -911,9 +1175,10 @@ int prepare(kpm_batch* bt) {
     count_launch(1);
     KPM_CHECK_LAUNCH();
     for (int f = 0; f < 2; ++f) {
-      hs[f][i] = SysDev{y.nb,      xit[f], y.bidx, y.bval, f ? y.ell_k : 0,
-                        y.eidx,    y.eval, {y.v[0], y.v[1], y.v[2]},
-                        y.partials, y.mu01, y.mom};
+      hs[f][i] = SysDev{y.nb,     xit[f],  y.bidx,  y.bval, f ? y.ell_k : 0,
+                        y.eidx,   y.eval,  y.spidx, y.spval,
+                        {y.v[0], y.v[1], y.v[2]}, y.partials, y.mu01,
+                        y.mom};
       for (int v = 0; v < 2; ++v)
         pre[f][v][i + 1] =
             pre[f][v][i] + (int64_t)xit[f] * (bt->Rpad / (16 * (v + 1)));
@@ -943,14 +1208,17 @@ int prepare(kpm_batch* bt) {
   float best = 1e30f;
   int best_fmt = 0, best_occ2 = 0;
   const char* force = getenv("KPM_BATCH_FORMAT");
-  const int f_lo = (have_ell && force && strcmp(force, "ell") == 0) ? 1 : 0;
-  for (int f = f_lo; f < (have_ell ? 2 : 1); ++f)
+  int f_lo = 0, f_hi = have_ell ? 2 : 0;
+  if (have_ell && force && strcmp(force, "ell") == 0) f_lo = f_hi = 1;
+  if (have_ell && force && strcmp(force, "sparse") == 0) f_lo = f_hi = 2;
+  for (int f = f_lo; f <= f_hi; ++f)
   for (int o2 = 0; o2 < (f ? 1 : 2); ++o2) {
     bt->ell = f;
     bt->occ2 = o2;
     for (int vpl = 1; vpl <= 2; ++vpl) {
       if (bt->Rpad % (16 * vpl)) continue;
       if (o2 && vpl == 1) continue;
+      if (f == 2 && vpl == 2) continue;          // sparse-block: 16 vectors
       KPM_TRY(launch_step_phase(bt, vpl, 0));  // warm-up
       KPM_CUDA(cudaEventRecord(bt->e0, s));
       KPM_TRY(launch_step_phase(bt, vpl, 0));
@@ -971,18 +1239,26 @@ int prepare(kpm_batch* bt) {
   }
   bt->ell = best_fmt;
   bt->occ2 = best_occ2;
-  // keep only the chosen format's matrices
+  // keep only the chosen format's matrices (the sparse-block kernel reads
+  // the BSR block columns and its own entries)
   for (auto& y : bt->sys) {
-    if (bt->ell) {
+    if (bt->ell == 1) {
       dev_free(y.bidx, s);
       dev_free(y.bval, s);
       y.bidx = nullptr;
       y.bval = nullptr;
-    } else {
+    }
+    if (bt->ell != 1) {
       dev_free(y.eidx, s);
       dev_free(y.eval, s);
       y.eidx = nullptr;
       y.eval = nullptr;
+    }
+    if (bt->ell != 2) {
+      dev_free(y.spidx, s);
+      dev_free(y.spval, s);
+      y.spidx = nullptr;
+      y.spval = nullptr;
     }
   }
   // capture the whole run in a CUDA graph
@@ -1189,10 +1465,11 @@ int kpm_batch_stats(kpm_batch* bt, double* ms, int64_t* nodes,
   return KPM_OK;
 }
 
-int kpm_batch_format(kpm_batch* bt, int* ell_width) {
-  KPM_REQUIRE(bt && ell_width, "kpm_batch_format: null argument");
+int kpm_batch_format(kpm_batch* bt, int* format, int* ell_width) {
+  KPM_REQUIRE(bt && format && ell_width, "kpm_batch_format: null argument");
+  *format = bt->ell;
   *ell_width = 0;
-  if (bt->ell)
+  if (bt->ell == 1)
     for (auto& y : bt->sys) *ell_width = std::max(*ell_width, y.ell_k);
   return KPM_OK;
 }

@@ -97,16 +97,21 @@ def test_sparse_blocks_run_as_orbital_ell(monkeypatch):
 
     monkeypatch.setenv('KPM_BATCH_FORMAT', 'ell')
     bd_ell, m_ell = run()
-    assert bd_ell.ell_width() == 16
+    assert bd_ell.step_format() == (1, 16)
+    monkeypatch.setenv('KPM_BATCH_FORMAT', 'sparse')
+    bd_sb, m_sb = run()
+    assert bd_sb.step_format()[0] == 2
     monkeypatch.setenv('KPM_BATCH_FORMAT', 'bsr')
     bd_bsr, m_bsr = run()
-    assert bd_bsr.ell_width() == 0
+    assert bd_bsr.step_format() == (0, 0)
     assert np.max(np.abs(m_ell - m_bsr)) <= 1e-6 * np.max(np.abs(m_bsr))
+    assert np.max(np.abs(m_sb - m_bsr)) <= 1e-6 * np.max(np.abs(m_bsr))
     for s, H in enumerate(mats):
         a, b = bd_ell.scales[s]
         vecs = batch.random_phase_vectors(seed, s, R, H.shape[0])
         ref = _oracle_mean(H, a, b, vecs, M)
         assert np.max(np.abs(m_ell[s] - ref)) / np.max(np.abs(ref)) < 1e-5
+        assert np.max(np.abs(m_sb[s] - ref)) / np.max(np.abs(ref)) < 1e-5
 
 
 def test_dense_blocks_stay_bsr():
@@ -123,7 +128,7 @@ def test_dense_blocks_stay_bsr():
     bd = batch.BatchedDOS(R, M, seed=1)
     bd.add_matrix(H, _gershgorin(H))
     mom = bd.moments()
-    assert bd.ell_width() == 0
+    assert bd.step_format()[0] == 0
     a, b = bd.scales[0]
     vecs = batch.random_phase_vectors(1, 0, R, n)
     ref = _oracle_mean(H, a, b, vecs, M)
