@@ -304,7 +304,7 @@ def run_ours(args):
     # MB against 794.0 MB algorithmic; the workload here is too large for a
     # multi-pass capture), scaled to this launch by its algorithmic bytes
     traffic = None
-    if args.precision == 'mixed' and args.reorder:
+    if args.precision == 'mixed' and args.reorder and R == 64:
         traffic = B * (788.0 / 794.0)
 
     # ---- accuracy vs the FP64 path (untimed) -------------------------------

@@ -61,6 +61,13 @@ constexpr int MAX_XITEMS = 2048;
 inline int group_size(int precision) {
   return precision == KPM_PREC_MIXED ? GROUP_FP32 : GROUP_FP64;
 }
+// Vector group of a block of R vectors: complex64 blocks of at most 16
+// vectors use 16-vector groups (one complex64 per lane), so that R <= 16
+// (Kwant's default is 10) does not move padding vectors.
+inline int group_size(int precision, int64_t R) {
+  return precision == KPM_PREC_MIXED && R > GROUP_FP64 ? GROUP_FP32
+                                                       : GROUP_FP64;
+}
 __host__ __device__ inline int64_t round_up(int64_t x, int64_t m) {
   return (x + m - 1) / m * m;
 }
@@ -141,6 +148,7 @@ struct kpm_block {
   kpm_handle* h = nullptr;
   int64_t R = 0;        // real vectors
   int64_t Rpad = 0;     // padded to the group size
+  int G = 0;            // vectors per group (16, or 32 for complex64 R > 16)
   int groups = 0;
   int64_t N = 0;
   bool keep_a0 = false;

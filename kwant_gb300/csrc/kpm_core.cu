@@ -318,18 +318,45 @@ int download_vectors(kpm_handle* h, const void* src, int64_t R, int64_t N,
 }
 
 // ------------------------------------------------------------ step kernel
-template <bool MIXED> struct Traits;
-template <> struct Traits<false> {
+template <bool MIXED, int VPL> struct Traits;
+template <> struct Traits<false, 1> {
   using PT = double2;
   using VT = double2;
   static constexpr int VPL = 1;
   static constexpr int G = GROUP_FP64;
 };
-template <> struct Traits<true> {
+template <> struct Traits<true, 2> {
   using PT = float4;
   using VT = float2;
   static constexpr int VPL = 2;
   static constexpr int G = GROUP_FP32;
+};
+template <> struct Traits<true, 1> {
+  using PT = float2;
+  using VT = float2;
+  static constexpr int VPL = 1;
+  static constexpr int G = GROUP_FP64;
+};
+
+// complex64 payload access: vector k (0 or 1) of a lane's payload
+__device__ __forceinline__ float c64_re(const float4& v, int k) {
+  return k ? v.z : v.x;
+}
+__device__ __forceinline__ float c64_im(const float4& v, int k) {
+  return k ? v.w : v.y;
+}
+__device__ __forceinline__ float c64_re(const float2& v, int) { return v.x; }
+__device__ __forceinline__ float c64_im(const float2& v, int) { return v.y; }
+template <int VPL> struct C64Pay;
+template <> struct C64Pay<2> {
+  __device__ static float4 make(const float (&r)[2], const float (&i)[2]) {
+    return make_float4(r[0], i[0], r[1], i[1]);
+  }
+};
+template <> struct C64Pay<1> {
+  __device__ static float2 make(const float (&r)[1], const float (&i)[1]) {
+    return make_float2(r[0], i[0]);
+  }
 };
 
 __device__ __forceinline__ void cmul_acc_exact(double& ar, double& ai,
@@ -342,10 +369,10 @@ __device__ __forceinline__ void cmul_acc_exact(double& ar, double& ai,
   ai = __dadd_rn(ai, pi);
 }
 
-template <bool MIXED, int MODE, bool DOTS>
+template <bool MIXED, int MODE, bool DOTS, int VPL_ = (MIXED ? 2 : 1)>
 __global__ void __launch_bounds__(STEP_THREADS)
 cheb_step_kernel(StepArgs p) {
-  using T = Traits<MIXED>;
+  using T = Traits<MIXED, VPL_>;
   using PT = typename T::PT;
   using VT = typename T::VT;
   constexpr int VPL = T::VPL;
@@ -396,8 +423,10 @@ cheb_step_kernel(StepArgs p) {
       const PT xv = x[i * p.rp + col];
       if constexpr (MODE == STEP_NORM) {
         if constexpr (MIXED) {
-          fn[0] = fmaf(xv.x, xv.x, fmaf(xv.y, xv.y, fn[0]));
-          fn[1] = fmaf(xv.z, xv.z, fmaf(xv.w, xv.w, fn[1]));
+#pragma unroll
+          for (int k = 0; k < VPL; ++k)
+            fn[k] = fmaf(c64_re(xv, k), c64_re(xv, k),
+                         fmaf(c64_im(xv, k), c64_im(xv, k), fn[k]));
           if (++pending == FLUSH) flush();
         } else {
           nrm[0] = fma(xv.x, xv.x, fma(xv.y, xv.y, nrm[0]));
@@ -439,14 +468,28 @@ cheb_step_kernel(StepArgs p) {
                            __dsub_rn(__dmul_rn(2.0, ti), pv.y));
         }
       } else {
-        // complex64: values are 2H/a, shift = -2b/a; FMA everywhere.
-        float a0r = p.shift * xv.x, a0i = p.shift * xv.y;
-        float a1r = p.shift * xv.z, a1i = p.shift * xv.w;
+        // complex64: values are 2H/a, shift = -2b/a; FMA everywhere (the
+        // same sequence for every vector whatever the vectors per lane).
+        float ar[VPL], ai[VPL];
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) {
+          ar[k] = p.shift * c64_re(xv, k);
+          ai[k] = p.shift * c64_im(xv, k);
+        }
+        auto mac = [&](const float2 h, const PT xx) {
+#pragma unroll
+          for (int k = 0; k < VPL; ++k) {
+            ar[k] = fmaf(h.x, c64_re(xx, k), ar[k]);
+            ar[k] = fmaf(-h.y, c64_im(xx, k), ar[k]);
+            ai[k] = fmaf(h.x, c64_im(xx, k), ai[k]);
+            ai[k] = fmaf(h.y, c64_re(xx, k), ai[k]);
+          }
+        };
         int jj = beg;
         for (; jj + 4 <= end; jj += 4) {
           int c[4];
           float2 h[4];
-          float4 xx[4];
+          PT xx[4];
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
             c[u] = __ldg(indices + jj + u);
@@ -455,47 +498,41 @@ cheb_step_kernel(StepArgs p) {
 #pragma unroll
           for (int u = 0; u < 4; ++u) xx[u] = x[(int64_t)c[u] * p.rp + col];
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            a0r = fmaf(h[u].x, xx[u].x, a0r);
-            a0r = fmaf(-h[u].y, xx[u].y, a0r);
-            a0i = fmaf(h[u].x, xx[u].y, a0i);
-            a0i = fmaf(h[u].y, xx[u].x, a0i);
-            a1r = fmaf(h[u].x, xx[u].z, a1r);
-            a1r = fmaf(-h[u].y, xx[u].w, a1r);
-            a1i = fmaf(h[u].x, xx[u].w, a1i);
-            a1i = fmaf(h[u].y, xx[u].z, a1i);
-          }
+          for (int u = 0; u < 4; ++u) mac(h[u], xx[u]);
         }
         for (; jj < end; ++jj) {
           int c = __ldg(indices + jj);
-          float2 h = vals[jj];
-          float4 xx = x[(int64_t)c * p.rp + col];
-          a0r = fmaf(h.x, xx.x, a0r);
-          a0r = fmaf(-h.y, xx.y, a0r);
-          a0i = fmaf(h.x, xx.y, a0i);
-          a0i = fmaf(h.y, xx.x, a0i);
-          a1r = fmaf(h.x, xx.z, a1r);
-          a1r = fmaf(-h.y, xx.w, a1r);
-          a1i = fmaf(h.x, xx.w, a1i);
-          a1i = fmaf(h.y, xx.z, a1i);
+          mac(vals[jj], x[(int64_t)c * p.rp + col]);
         }
+        float orr[VPL], oii[VPL];
         if constexpr (MODE == STEP_FIRST) {
-          o = make_float4(0.5f * a0r, 0.5f * a0i, 0.5f * a1r, 0.5f * a1i);
+#pragma unroll
+          for (int k = 0; k < VPL; ++k) {
+            orr[k] = 0.5f * ar[k];
+            oii[k] = 0.5f * ai[k];
+          }
         } else {
-          const float4 pv = prev[i * p.rp + col];
-          o = make_float4(a0r - pv.x, a0i - pv.y, a1r - pv.z, a1i - pv.w);
+          const PT pv = prev[i * p.rp + col];
+#pragma unroll
+          for (int k = 0; k < VPL; ++k) {
+            orr[k] = ar[k] - c64_re(pv, k);
+            oii[k] = ai[k] - c64_im(pv, k);
+          }
         }
+        o = C64Pay<VPL>::make(orr, oii);
       }
       out[i * p.rp + col] = o;
       if constexpr (DOTS) {
         // <x|x> and <o|x> = sum conj(o) x
         if constexpr (MIXED) {
-          fn[0] = fmaf(xv.x, xv.x, fmaf(xv.y, xv.y, fn[0]));
-          fn[1] = fmaf(xv.z, xv.z, fmaf(xv.w, xv.w, fn[1]));
-          fcr[0] = fmaf(o.x, xv.x, fmaf(o.y, xv.y, fcr[0]));
-          fcr[1] = fmaf(o.z, xv.z, fmaf(o.w, xv.w, fcr[1]));
-          fci[0] = fmaf(o.x, xv.y, fmaf(-o.y, xv.x, fci[0]));
-          fci[1] = fmaf(o.z, xv.w, fmaf(-o.w, xv.z, fci[1]));
+#pragma unroll
+          for (int k = 0; k < VPL; ++k) {
+            const float xr = c64_re(xv, k), xi = c64_im(xv, k);
+            const float or_ = c64_re(o, k), oi = c64_im(o, k);
+            fn[k] = fmaf(xr, xr, fmaf(xi, xi, fn[k]));
+            fcr[k] = fmaf(or_, xr, fmaf(oi, xi, fcr[k]));
+            fci[k] = fmaf(or_, xi, fmaf(-oi, xr, fci[k]));
+          }
           if (++pending == FLUSH) flush();
         } else {
           nrm[0] = fma(xv.x, xv.x, fma(xv.y, xv.y, nrm[0]));
@@ -591,13 +628,13 @@ __global__ void moments_to_host_order_kernel(const double2* __restrict__ in,
 }
 
 // --------------------------------------------------------------- dispatch
-template <bool MIXED, int MODE, bool DOTS>
+template <bool MIXED, int MODE, bool DOTS, int VPL = (MIXED ? 2 : 1)>
 static int launch_step_t(kpm_handle* h, const StepArgs& a) {
   static int occ = -1;
   if (occ < 0) {
     int blocks = 0;
     KPM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &blocks, cheb_step_kernel<MIXED, MODE, DOTS>, STEP_THREADS, 0));
+        &blocks, cheb_step_kernel<MIXED, MODE, DOTS, VPL>, STEP_THREADS, 0));
     occ = blocks > 0 ? blocks : 1;
   }
   int64_t work = (int64_t)a.xitems * a.groups;
@@ -615,7 +652,7 @@ static int launch_step_t(kpm_handle* h, const StepArgs& a) {
     h->prof_used += 2;
     KPM_CUDA(cudaEventRecord(e0, h->stream));
   }
-  cheb_step_kernel<MIXED, MODE, DOTS>
+  cheb_step_kernel<MIXED, MODE, DOTS, VPL>
       <<<(unsigned)grid, STEP_THREADS, 0, h->stream>>>(a);
   count_launch(1);
   KPM_CHECK_LAUNCH();
@@ -627,6 +664,15 @@ int launch_step(kpm_handle* h, int mode, bool dots, const StepArgs& a) {
   const bool mixed = h->precision == KPM_PREC_MIXED;
   if (mixed && h->H.ell_k > 0 && mode != STEP_NORM && a.vals == h->H.data)
     return launch_step_ell(h, mode, dots, a);
+  if (mixed && a.vpl == 1) {
+    if (mode == STEP_FIRST)
+      return dots ? launch_step_t<true, STEP_FIRST, true, 1>(h, a)
+                  : launch_step_t<true, STEP_FIRST, false, 1>(h, a);
+    if (mode == STEP_RECUR)
+      return dots ? launch_step_t<true, STEP_RECUR, true, 1>(h, a)
+                  : launch_step_t<true, STEP_RECUR, false, 1>(h, a);
+    return launch_step_t<true, STEP_NORM, false, 1>(h, a);
+  }
   if (mixed) {
     if (mode == STEP_FIRST)
       return dots ? launch_step_t<true, STEP_FIRST, true>(h, a)
@@ -669,7 +715,8 @@ StepArgs step_args(kpm_block* b, const void* x, const void* prev, void* out) {
   a.x = x;
   a.prev = prev;
   a.out = out;
-  a.rp = b->Rpad / (h->precision == KPM_PREC_MIXED ? 2 : 1);
+  a.vpl = h->precision == KPM_PREC_MIXED ? b->G / GROUP_FP64 : 1;
+  a.rp = b->Rpad / a.vpl;
   a.groups = b->groups;
   a.xitems = xitems_for_rows(b->N);
   a.partials = h->partials;
@@ -710,7 +757,7 @@ int finalize(kpm_block* b, int mode, double2* mom, int64_t slot_even,
              int64_t slot_odd) {
   kpm_handle* h = b->h;
   dos_finalize_kernel<<<(unsigned)b->Rpad, 128, 0, h->stream>>>(
-      h->partials, group_size(h->precision), xitems_for_rows(b->N), b->Rpad,
+      h->partials, b->G, xitems_for_rows(b->N), b->Rpad,
       mode, (double2*)b->mu01, mom, b->Rpad, slot_even, slot_odd);
   count_launch(1);
   KPM_CHECK_LAUNCH();
@@ -957,7 +1004,8 @@ int kpm_block_create(kpm_handle* h, const double* vecs, int64_t R,
   b->h = h;
   b->R = R;
   b->N = h->H.rows;
-  const int G = group_size(h->precision);
+  const int G = group_size(h->precision, R);
+  b->G = G;
   b->Rpad = round_up(R, G);
   b->groups = (int)(b->Rpad / G);
   b->keep_a0 = keep_a0 != 0;

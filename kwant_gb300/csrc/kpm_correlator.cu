@@ -129,7 +129,8 @@ static int block_from_device(kpm_handle* h, int64_t R, void* a0_owned,
   b->h = h;
   b->R = R;
   b->N = h->H.rows;
-  const int G = group_size(h->precision);
+  const int G = group_size(h->precision, R);
+  b->G = G;
   b->Rpad = round_up(R, G);
   b->groups = (int)(b->Rpad / G);
   b->keep_a0 = true;

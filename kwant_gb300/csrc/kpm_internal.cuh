@@ -17,7 +17,8 @@ struct StepArgs {
   const void* x;    // alpha_n        [rows][Rpad]
   const void* prev; // alpha_{n-1}    (may alias out)
   void* out;        // alpha_{n+1}
-  int64_t rp;       // 16-byte payloads per row
+  int64_t rp;       // payloads per row (16 bytes, or 8 when vpl == 1)
+  int vpl;          // complex64 vectors per lane: 2 (groups of 32) or 1
   int groups;
   int xitems;
   double* partials; // [groups][xitems][group][3]

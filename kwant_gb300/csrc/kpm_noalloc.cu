@@ -123,6 +123,7 @@ int kpm_dos_moments_noalloc(const kpm_device_csr* ham, double a, double b,
   blk.h = &h;
   blk.R = R;
   blk.Rpad = Rpad;
+  blk.G = G;
   blk.groups = groups;
   blk.N = N;
   blk.keep_a0 = true;  // the caller's vectors are only read

@@ -27,20 +27,43 @@ constexpr int ell_min_blocks() {
   return (K <= 4 && RPI == 1) ? KPM_ELL_MIN_BLOCKS : 1;
 }
 
-template <int K, int MODE, bool DOTS, int RPI>
+template <int VPL> struct EllPay;
+template <> struct EllPay<2> {
+  using T = float4;
+  __device__ static float re(const float4& v, int k) { return k ? v.z : v.x; }
+  __device__ static float im(const float4& v, int k) { return k ? v.w : v.y; }
+  __device__ static float4 make(const float (&r)[2], const float (&i)[2]) {
+    return make_float4(r[0], i[0], r[1], i[1]);
+  }
+};
+template <> struct EllPay<1> {
+  using T = float2;
+  __device__ static float re(const float2& v, int) { return v.x; }
+  __device__ static float im(const float2& v, int) { return v.y; }
+  __device__ static float2 make(const float (&r)[1], const float (&i)[1]) {
+    return make_float2(r[0], i[0]);
+  }
+};
+
+// VPL complex64 vectors per lane: 2 (groups of 32 vectors) or 1 (groups of
+// 16, for blocks of at most 16 vectors); every vector gets the same FMA
+// sequence either way.
+template <int K, int MODE, bool DOTS, int RPI, int VPL>
 __global__ void __launch_bounds__(STEP_THREADS, ell_min_blocks<K, RPI>())
 cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
                      const float2* __restrict__ eval) {
-  constexpr int G = GROUP_FP32;
+  using Pay = EllPay<VPL>;
+  using PT = typename Pay::T;
+  constexpr int G = LANES * VPL;
   constexpr int KQ = K / 4;
   const int lane = threadIdx.x & (LANES - 1);
   const int slot = threadIdx.x / LANES;
   // FP64 accumulators of this slot's lanes, then the in-block reduction
   __shared__ double red[DOTS ? SLOTS : 1][DOTS ? G * 3 : 1];
 
-  const float4* __restrict__ x = reinterpret_cast<const float4*>(p.x);
-  const float4* prev = reinterpret_cast<const float4*>(p.prev);
-  float4* out = reinterpret_cast<float4*>(p.out);
+  const PT* __restrict__ x = reinterpret_cast<const PT*>(p.x);
+  const PT* prev = reinterpret_cast<const PT*>(p.prev);
+  PT* out = reinterpret_cast<PT*>(p.out);
   const int64_t work = (int64_t)p.xitems * p.groups;
   const int64_t stride = (int64_t)p.xitems * SLOTS;
   const float shift = p.shift;
@@ -50,12 +73,14 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
     const int xi = (int)(w / p.groups);
     const int g = (int)(w - (int64_t)xi * p.groups);
     const int64_t col = (int64_t)g * LANES + lane;
-    double* my = DOTS ? &red[slot][lane * 2 * 3] : nullptr;
+    double* my = DOTS ? &red[slot][lane * VPL * 3] : nullptr;
     if constexpr (DOTS) {
 #pragma unroll
-      for (int e = 0; e < 6; ++e) my[e] = 0.0;
+      for (int e = 0; e < VPL * 3; ++e) my[e] = 0.0;
     }
-    float fn0 = 0.f, fn1 = 0.f, fr0 = 0.f, fr1 = 0.f, fi0 = 0.f, fi1 = 0.f;
+    float fn[VPL], fr[VPL], fi[VPL];
+#pragma unroll
+    for (int k = 0; k < VPL; ++k) fn[k] = fr[k] = fi[k] = 0.f;
     int pending = 0;
 
     for (int64_t i0 = (int64_t)xi * SLOTS + slot; i0 < p.rows;
@@ -67,7 +92,7 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
         row[u] = i0 + u * stride;
         ok[u] = row[u] < p.rows;
       }
-      float4 xv[RPI], pv[RPI];
+      PT xv[RPI], pv[RPI];
       int4 c4[RPI][KQ];
       float4 hv[RPI][2 * KQ];
 #pragma unroll
@@ -88,12 +113,16 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
 #pragma unroll
       for (int u = 0; u < RPI; ++u) {
         if (!ok[u]) continue;
-        float a0r = shift * xv[u].x, a0i = shift * xv[u].y;
-        float a1r = shift * xv[u].z, a1i = shift * xv[u].w;
+        float ar[VPL], ai[VPL];
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) {
+          ar[k] = shift * Pay::re(xv[u], k);
+          ai[k] = shift * Pay::im(xv[u], k);
+        }
 #pragma unroll
         for (int q = 0; q < KQ; ++q) {
           const int cc[4] = {c4[u][q].x, c4[u][q].y, c4[u][q].z, c4[u][q].w};
-          float4 xx[4];
+          PT xx[4];
 #pragma unroll
           for (int t = 0; t < 4; ++t) xx[t] = x[(int64_t)cc[t] * p.rp + col];
           const float hr[4] = {hv[u][2 * q].x, hv[u][2 * q].z,
@@ -102,52 +131,55 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
                                hv[u][2 * q + 1].y, hv[u][2 * q + 1].w};
 #pragma unroll
           for (int t = 0; t < 4; ++t) {
-            a0r = fmaf(hr[t], xx[t].x, a0r);
-            a0r = fmaf(-hi[t], xx[t].y, a0r);
-            a0i = fmaf(hr[t], xx[t].y, a0i);
-            a0i = fmaf(hi[t], xx[t].x, a0i);
-            a1r = fmaf(hr[t], xx[t].z, a1r);
-            a1r = fmaf(-hi[t], xx[t].w, a1r);
-            a1i = fmaf(hr[t], xx[t].w, a1i);
-            a1i = fmaf(hi[t], xx[t].z, a1i);
+#pragma unroll
+            for (int k = 0; k < VPL; ++k) {
+              ar[k] = fmaf(hr[t], Pay::re(xx[t], k), ar[k]);
+              ar[k] = fmaf(-hi[t], Pay::im(xx[t], k), ar[k]);
+              ai[k] = fmaf(hr[t], Pay::im(xx[t], k), ai[k]);
+              ai[k] = fmaf(hi[t], Pay::re(xx[t], k), ai[k]);
+            }
           }
         }
-        float4 o;
-        if constexpr (MODE == STEP_FIRST) {
-          o = make_float4(0.5f * a0r, 0.5f * a0i, 0.5f * a1r, 0.5f * a1i);
-        } else {
-          o = make_float4(a0r - pv[u].x, a0i - pv[u].y, a1r - pv[u].z,
-                          a1i - pv[u].w);
+        float orr[VPL], oii[VPL];
+#pragma unroll
+        for (int k = 0; k < VPL; ++k) {
+          if constexpr (MODE == STEP_FIRST) {
+            orr[k] = 0.5f * ar[k];
+            oii[k] = 0.5f * ai[k];
+          } else {
+            orr[k] = ar[k] - Pay::re(pv[u], k);
+            oii[k] = ai[k] - Pay::im(pv[u], k);
+          }
         }
-        out[row[u] * p.rp + col] = o;
+        out[row[u] * p.rp + col] = Pay::make(orr, oii);
         if constexpr (DOTS) {
-          const float4 v = xv[u];
-          fn0 = fmaf(v.x, v.x, fmaf(v.y, v.y, fn0));
-          fn1 = fmaf(v.z, v.z, fmaf(v.w, v.w, fn1));
-          fr0 = fmaf(o.x, v.x, fmaf(o.y, v.y, fr0));
-          fr1 = fmaf(o.z, v.z, fmaf(o.w, v.w, fr1));
-          fi0 = fmaf(o.x, v.y, fmaf(-o.y, v.x, fi0));
-          fi1 = fmaf(o.z, v.w, fmaf(-o.w, v.z, fi1));
+#pragma unroll
+          for (int k = 0; k < VPL; ++k) {
+            const float vr = Pay::re(xv[u], k), vi = Pay::im(xv[u], k);
+            fn[k] = fmaf(vr, vr, fmaf(vi, vi, fn[k]));
+            fr[k] = fmaf(orr[k], vr, fmaf(oii[k], vi, fr[k]));
+            fi[k] = fmaf(orr[k], vi, fmaf(-oii[k], vr, fi[k]));
+          }
           if (++pending == FLUSH) {
-            my[0] += (double)fn0;
-            my[1] += (double)fr0;
-            my[2] += (double)fi0;
-            my[3] += (double)fn1;
-            my[4] += (double)fr1;
-            my[5] += (double)fi1;
-            fn0 = fn1 = fr0 = fr1 = fi0 = fi1 = 0.f;
+#pragma unroll
+            for (int k = 0; k < VPL; ++k) {
+              my[k * 3 + 0] += (double)fn[k];
+              my[k * 3 + 1] += (double)fr[k];
+              my[k * 3 + 2] += (double)fi[k];
+              fn[k] = fr[k] = fi[k] = 0.f;
+            }
             pending = 0;
           }
         }
       }
     }
     if constexpr (DOTS) {
-      my[0] += (double)fn0;
-      my[1] += (double)fr0;
-      my[2] += (double)fi0;
-      my[3] += (double)fn1;
-      my[4] += (double)fr1;
-      my[5] += (double)fi1;
+#pragma unroll
+      for (int k = 0; k < VPL; ++k) {
+        my[k * 3 + 0] += (double)fn[k];
+        my[k * 3 + 1] += (double)fr[k];
+        my[k * 3 + 2] += (double)fi[k];
+      }
       __syncthreads();
       // layout [group][vector*3 + component][partition]: the finalize
       // kernel reads each vector's partitions contiguously
@@ -163,13 +195,14 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
   }
 }
 
-template <int K, int MODE, bool DOTS, int RPI>
+template <int K, int MODE, bool DOTS, int RPI, int VPL>
 static int launch_ell_t(kpm_handle* h, const StepArgs& a) {
   static int occ = -1;
   if (occ < 0) {
     int blocks = 0;
     KPM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &blocks, cheb_step_ell_kernel<K, MODE, DOTS, RPI>, STEP_THREADS, 0));
+        &blocks, cheb_step_ell_kernel<K, MODE, DOTS, RPI, VPL>, STEP_THREADS,
+        0));
     occ = blocks > 0 ? blocks : 1;
   }
   const int64_t work = (int64_t)a.xitems * a.groups;
@@ -187,7 +220,7 @@ static int launch_ell_t(kpm_handle* h, const StepArgs& a) {
     h->prof_used += 2;
     KPM_CUDA(cudaEventRecord(e0, h->stream));
   }
-  cheb_step_ell_kernel<K, MODE, DOTS, RPI>
+  cheb_step_ell_kernel<K, MODE, DOTS, RPI, VPL>
       <<<(unsigned)grid, STEP_THREADS, 0, h->stream>>>(a, h->H.ell_idx,
                                                         h->H.ell_val);
   count_launch(1);
@@ -196,31 +229,32 @@ static int launch_ell_t(kpm_handle* h, const StepArgs& a) {
   return KPM_OK;
 }
 
-template <int K, int RPI>
+template <int K, int RPI, int VPL>
 static int dispatch_mode(kpm_handle* h, int mode, bool dots,
                          const StepArgs& a) {
   if (mode == STEP_FIRST)
-    return dots ? launch_ell_t<K, STEP_FIRST, true, RPI>(h, a)
-                : launch_ell_t<K, STEP_FIRST, false, RPI>(h, a);
-  return dots ? launch_ell_t<K, STEP_RECUR, true, RPI>(h, a)
-              : launch_ell_t<K, STEP_RECUR, false, RPI>(h, a);
+    return dots ? launch_ell_t<K, STEP_FIRST, true, RPI, VPL>(h, a)
+                : launch_ell_t<K, STEP_FIRST, false, RPI, VPL>(h, a);
+  return dots ? launch_ell_t<K, STEP_RECUR, true, RPI, VPL>(h, a)
+              : launch_ell_t<K, STEP_RECUR, false, RPI, VPL>(h, a);
 }
 
-template <int RPI>
+template <int RPI, int VPL>
 static int dispatch_k(kpm_handle* h, int mode, bool dots, const StepArgs& a) {
   switch (h->H.ell_k) {
-    case 4: return dispatch_mode<4, RPI>(h, mode, dots, a);
-    case 8: return dispatch_mode<8, RPI>(h, mode, dots, a);
-    case 12: return dispatch_mode<12, RPI>(h, mode, dots, a);
-    case 16: return dispatch_mode<16, RPI>(h, mode, dots, a);
+    case 4: return dispatch_mode<4, RPI, VPL>(h, mode, dots, a);
+    case 8: return dispatch_mode<8, RPI, VPL>(h, mode, dots, a);
+    case 12: return dispatch_mode<12, RPI, VPL>(h, mode, dots, a);
+    case 16: return dispatch_mode<16, RPI, VPL>(h, mode, dots, a);
   }
   set_error("ELL width %d not supported", h->H.ell_k);
   return KPM_EUNSUPPORTED;
 }
 
 int launch_step_ell(kpm_handle* h, int mode, bool dots, const StepArgs& a) {
-  if (h->step_rpi == 2) return dispatch_k<2>(h, mode, dots, a);
-  return dispatch_k<1>(h, mode, dots, a);
+  if (a.vpl == 1) return dispatch_k<1, 1>(h, mode, dots, a);
+  if (h->step_rpi == 2) return dispatch_k<2, 2>(h, mode, dots, a);
+  return dispatch_k<1, 2>(h, mode, dots, a);
 }
 
 }  // namespace kpm
