@@ -293,12 +293,16 @@ __global__ void strip_kernel(const float* __restrict__ src, int N, int K,
   dst[t] = src[(int64_t)n * Kp + k];
 }
 
+// Adam step t = *step + 1 (the counter is advanced by adam_count_kernel
+// afterwards, so that a captured epoch replays with the right t)
 __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g,
                             float* __restrict__ m, float* __restrict__ v,
                             int64_t n, float lr, float b1, float b2,
-                            float eps, float c1, float c2) {
+                            float eps, const int64_t* __restrict__ step) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const float t = (float)(*step + 1);
+  const float c1 = 1.f - powf(b1, t), c2 = 1.f - powf(b2, t);
   const float gi = g[i];
   const float mi = b1 * m[i] + (1.f - b1) * gi;
   const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
@@ -306,6 +310,8 @@ __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g,
   v[i] = vi;
   p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
 }
+
+__global__ void adam_count_kernel(int64_t* step) { *step += 1; }
 
 }  // namespace mlp
 }  // namespace kpm
@@ -327,6 +333,7 @@ struct kpm_mlp {
   float *dH = nullptr, *tmp = nullptr;
   double* part = nullptr;
   double* loss_acc = nullptr;  // sum of batch losses since the last reset
+  int64_t* dstep = nullptr;    // Adam step counter on the device
   int* err = nullptr;
   int num_sms = 0, device = 0;
   cudaStream_t stream = nullptr;
@@ -337,6 +344,11 @@ namespace {
 template <typename T>
 int alloc(T** p, size_t count, cudaStream_t s) {
   return dev_alloc((void**)p, count * sizeof(T), s);
+}
+
+size_t gemm_smem(int nt) {
+  return 1024 + STAGES * (tc::TM * KC * 2 + (size_t)nt * KC * 2) +
+         (2 * STAGES + 1) * 8 + 16;
 }
 
 // C[M][N] = A[M][K] B[N][K]^T  (A, B bf16 row-major, K multiple of 32)
@@ -351,15 +363,7 @@ int gemm_tn(kpm_mlp* net, const bf16* A, int64_t M, const bf16* B,
   CUtensorMap ma, mb;
   KPM_TRY(make_map2d(&ma, A, M, K, tc::TM));
   KPM_TRY(make_map2d(&mb, B, N, K, nt));
-  const size_t smem = 1024 + STAGES * (tc::TM * KC * 2 + (size_t)nt * KC * 2) +
-                      (2 * STAGES + 1) * 8 + 16;
-  static size_t configured = 0;
-  if (smem > configured) {
-    KPM_CUDA(cudaFuncSetAttribute(bf16_tn_kernel,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem));
-    configured = smem;
-  }
+  const size_t smem = gemm_smem(nt);   // attribute set at create
   TnArgs args{M, N, K, nt, ntiles_n, tmem_cols, C, ldc, net->err};
   const int grid = (int)(ceil_div(M, tc::TM) * ntiles_n);
   bf16_tn_kernel<<<grid, tc::THREADS, smem, net->stream>>>(ma, mb, args);
@@ -493,6 +497,18 @@ int kpm_mlp_create(int num_layers, const int32_t* widths, int max_batch,
     delete net;
     return st;
   }
+  // the largest GEMM tile (256 columns) needs this much dynamic shared
+  // memory; set it (and resolve the tensor-map encoder) before any stream
+  // capture of a training epoch
+  tc::encode_fn();
+  if (cudaFuncSetAttribute(bf16_tn_kernel,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)gemm_smem(256)) != cudaSuccess) {
+    set_error("kpm_mlp_create: shared memory attribute failed");
+    cudaStreamDestroy(net->stream);
+    delete net;
+    return KPM_ECUDA;
+  }
   net->w.assign(widths, widths + num_layers + 1);
   net->wp.resize(num_layers + 1);
   for (int l = 0; l <= num_layers; ++l)
@@ -550,11 +566,13 @@ int kpm_mlp_create(int num_layers, const int32_t* widths, int max_batch,
   if (st == KPM_OK) st = alloc(&net->part, (size_t)ceil_div(B * maxw, 256), s);
   if (st == KPM_OK) st = alloc(&net->err, 1, s);
   if (st == KPM_OK) st = alloc(&net->loss_acc, 1, s);
+  if (st == KPM_OK) st = alloc(&net->dstep, 1, s);
   if (st == KPM_OK) {
     cudaMemsetAsync(net->m, 0, off * sizeof(float), s);
     cudaMemsetAsync(net->v, 0, off * sizeof(float), s);
     cudaMemsetAsync(net->err, 0, sizeof(int), s);
     cudaMemsetAsync(net->loss_acc, 0, sizeof(double), s);
+    cudaMemsetAsync(net->dstep, 0, sizeof(int64_t), s);
     // zero activations (padding columns must stay zero)
     for (int l = 0; l <= num_layers; ++l) {
       cudaMemsetAsync(net->Hb[l], 0, (size_t)B * net->wp[l] * 2, s);
@@ -595,6 +613,7 @@ int kpm_mlp_set_params(kpm_mlp* net, const float* in) {
                            cudaMemcpyHostToDevice, net->stream));
   KPM_CUDA(cudaStreamSynchronize(net->stream));
   net->step = 0;
+  KPM_CUDA(cudaMemsetAsync(net->dstep, 0, sizeof(int64_t), net->stream));
   KPM_CUDA(cudaMemsetAsync(net->m, 0, net->nparams * sizeof(float),
                            net->stream));
   KPM_CUDA(cudaMemsetAsync(net->v, 0, net->nparams * sizeof(float),
@@ -688,6 +707,53 @@ int kpm_mlp_train(kpm_mlp* net, const float* x, const float* y, int64_t n,
   std::mt19937_64 gen(seed);
   std::vector<int32_t> perm(n);
   const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  // One epoch (per_epoch forward / backward / Adam steps over the shuffled
+  // index buffer) is captured once as a CUDA graph and replayed; only the
+  // shuffled indices change between epochs.
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  size_t nodes = 0;
+  int64_t counted0 = 0, counted1 = 0;
+  kpm_launch_count(&counted0);
+  if (st == KPM_OK) {
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) !=
+        cudaSuccess) {
+      set_error("kpm_mlp_train: stream capture failed");
+      st = KPM_ECUDA;
+    } else {
+      int cst = KPM_OK;
+      for (int64_t it = 0; cst == KPM_OK && it < per_epoch; ++it) {
+        const int32_t* idx = didx + it * batch;
+        cst = forward(net, dx, idx, batch, true);
+        if (cst == KPM_OK) cst = backward(net, dy, idx, batch);
+        if (cst != KPM_OK) break;
+        adam_kernel<<<blocks(net->nparams), 256, 0, s>>>(
+            net->params, net->grads, net->m, net->v, net->nparams,
+            (float)lr, b1, b2, eps, net->dstep);
+        adam_count_kernel<<<1, 1, 0, s>>>(net->dstep);
+        if (cudaGetLastError() != cudaSuccess) {
+          set_error("kpm_mlp_train: Adam launch failed");
+          cst = KPM_ECUDA;
+        }
+      }
+      const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+      st = cst;
+      if (st == KPM_OK && ce != cudaSuccess) {
+        set_error("kpm_mlp_train: stream capture failed: %s",
+                  cudaGetErrorString(ce));
+        st = KPM_ECUDA;
+      }
+      if (st == KPM_OK &&
+          (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess ||
+           cudaGraphGetNodes(graph, nullptr, &nodes) != cudaSuccess)) {
+        set_error("kpm_mlp_train: graph instantiation failed");
+        st = KPM_ECUDA;
+      }
+    }
+  }
+  // launches are counted when the graph replays, not when it is captured
+  kpm_launch_count(&counted1);
+  count_launch(-(int)(counted1 - counted0));
   for (int64_t ep = 0; st == KPM_OK && ep < epochs; ++ep) {
     for (int64_t i = 0; i < n; ++i) perm[i] = (int32_t)i;
     std::shuffle(perm.begin(), perm.end(), gen);
@@ -698,24 +764,15 @@ int kpm_mlp_train(kpm_mlp* net, const float* x, const float* y, int64_t n,
       break;
     }
     if (ep + 1 == epochs && st == KPM_OK) st = read_loss(net, nullptr, true);
-    for (int64_t it = 0; st == KPM_OK && it < per_epoch; ++it) {
-      const int32_t* idx = didx + it * batch;
-      st = forward(net, dx, idx, batch, true);
-      if (st == KPM_OK) st = backward(net, dy, idx, batch);
-      if (st != KPM_OK) break;
-      net->step += 1;
-      const float c1 = 1.f - std::pow(b1, (float)net->step);
-      const float c2 = 1.f - std::pow(b2, (float)net->step);
-      adam_kernel<<<blocks(net->nparams), 256, 0, s>>>(
-          net->params, net->grads, net->m, net->v, net->nparams, (float)lr,
-          b1, b2, eps, c1, c2);
-      count_launch(1);
-      if (cudaGetLastError() != cudaSuccess) {
-        set_error("kpm_mlp_train: Adam launch failed");
-        st = KPM_ECUDA;
-      }
+    if (st == KPM_OK && cudaGraphLaunch(exec, s) != cudaSuccess) {
+      set_error("kpm_mlp_train: graph launch failed");
+      st = KPM_ECUDA;
     }
+    count_launch((int)nodes);
+    net->step += per_epoch;
   }
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
   double last = 0.0;
   if (st == KPM_OK) st = read_loss(net, &last, true);
   if (st == KPM_OK) st = check_err(net);
@@ -743,6 +800,7 @@ int kpm_mlp_destroy(kpm_mlp* net) {
   dev_free(net->part, s);
   dev_free(net->err, s);
   dev_free(net->loss_acc, s);
+  dev_free(net->dstep, s);
   dev_free(net->params, s);
   dev_free(net->grads, s);
   dev_free(net->m, s);
