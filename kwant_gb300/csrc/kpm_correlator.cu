@@ -150,23 +150,43 @@ static int block_from_device(kpm_handle* h, int64_t R, void* a0_owned,
   return KPM_OK;
 }
 
+// One order n of a stored recursion: alpha_n (advancing from alpha_{n-1}
+// for n > 0) and its store row, launched on `stream` with the scale (a, b)
+// of this recursion (the correlator's second recursion uses (a2, b2)).
 template <int STORE>
-static int run_recursion(kpm_block* b, const Matrix* V, int64_t M,
-                         Store* store, double a, double bshift) {
+static int recursion_order(kpm_block* b, const Matrix* V, int64_t n,
+                           Store* store, double a, double bshift,
+                           cudaStream_t stream) {
   kpm_handle* h = b->h;
-  // per-call scale (the correlator's second recursion uses (a2, b2))
   const double a_save = h->a, b_save = h->b;
+  const cudaStream_t s_save = h->stream;
   h->a = a;
   h->b = bshift;
+  h->stream = stream;
   int st = KPM_OK;
-  for (int64_t n = 0; st == KPM_OK && n < M; ++n) {
-    if (n > 0) st = block_advance(b, false);
-    if (st == KPM_OK)
-      st = put_row<STORE>(h, V, b->p_cur, b->N, b->R, b->Rpad,
-                          store->row(n));
-  }
+  if (n > 0) st = block_advance(b, false);
+  if (st == KPM_OK)
+    st = put_row<STORE>(h, V, b->p_cur, b->N, b->R, b->Rpad, store->row(n));
   h->a = a_save;
   h->b = b_save;
+  h->stream = s_save;
+  return st;
+}
+
+// Both recursions of the correlator, interleaved order by order on two
+// streams: each is a chain of small dependent launches (latency-bound at
+// the sizes of the Kubo workload), and they are independent of each other.
+template <int STORE>
+static int run_recursions(kpm_block* bR, const Matrix* Vb, Store* psi,
+                          double a, double b, kpm_block* bL, Store* omega,
+                          double a2, double b2, int64_t M,
+                          cudaStream_t s2) {
+  int st = KPM_OK;
+  for (int64_t n = 0; st == KPM_OK && n < M; ++n) {
+    st = recursion_order<STORE>(bR, Vb, n, psi, a, b, bR->h->stream);
+    if (st == KPM_OK)
+      st = recursion_order<STORE>(bL, nullptr, n, omega, a2, b2, s2);
+  }
   return st;
 }
 
@@ -208,12 +228,7 @@ int kpm_correlator_moments(kpm_handle* h, double a2, double b2,
   if (st == KPM_OK) st = store_alloc(&omega, kind, M, K, s);
   if (st == KPM_OK) st = kpm_block_create(h, vecs, R, 1, &bR);
   if (st == KPM_OK) st = timed_begin(h);
-  // Psi_n = v_beta T_n(H~)|r>
-  if (st == KPM_OK)
-    st = kind == STORE_C128
-             ? run_recursion<STORE_C128>(bR, &Vb, M, &psi, h->a, h->b)
-             : run_recursion<STORE_BF16X3>(bR, &Vb, M, &psi, h->a, h->b);
-  // Omega_m = T_m(H~') v_alpha|r>
+  // Omega's starting vectors v_alpha|r>
   if (st == KPM_OK) {
     const size_t csz = h->precision == KPM_PREC_MIXED ? 8 : 16;
     void* a0L = nullptr;
@@ -235,26 +250,53 @@ int kpm_correlator_moments(kpm_handle* h, double a2, double b2,
     if (st == KPM_OK) st = block_from_device(h, R, a0L, &bL);
     else dev_free(a0L, s);
   }
+  // Psi_n = v_beta T_n(H~)|r> on the handle's stream and Omega_m =
+  // T_m(H~') v_alpha|r> on a second stream, interleaved
+  cudaStream_t s2 = nullptr;
+  cudaEvent_t ready = nullptr, done = nullptr;
+  if (st == KPM_OK &&
+      (cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking) != cudaSuccess ||
+       cudaEventCreateWithFlags(&ready, cudaEventDisableTiming) !=
+           cudaSuccess ||
+       cudaEventCreateWithFlags(&done, cudaEventDisableTiming) !=
+           cudaSuccess)) {
+    set_error("kpm_correlator_moments: stream creation failed");
+    st = KPM_ECUDA;
+  }
+  if (st == KPM_OK && (cudaEventRecord(ready, s) != cudaSuccess ||
+                       cudaStreamWaitEvent(s2, ready, 0) != cudaSuccess)) {
+    set_error("kpm_correlator_moments: stream ordering failed");
+    st = KPM_ECUDA;
+  }
   if (st == KPM_OK) {
-    // release the first recursion's vectors before the second one
-    kpm_block_destroy(bR);
-    bR = nullptr;
-    if (h->precision == KPM_PREC_MIXED) {
-      // complex64 values are pre-scaled by 2/a; a2 equals a up to rounding
-      // (kwant/kpm.py:576-579), so only the diagonal shift is re-derived.
-      st = kind == STORE_C128
-               ? run_recursion<STORE_C128>(bL, nullptr, M, &omega, h->a, b2)
-               : run_recursion<STORE_BF16X3>(bL, nullptr, M, &omega, h->a,
-                                             b2);
-    } else {
-      st = kind == STORE_C128
-               ? run_recursion<STORE_C128>(bL, nullptr, M, &omega, a2, b2)
-               : run_recursion<STORE_BF16X3>(bL, nullptr, M, &omega, a2, b2);
+    // complex64 values are pre-scaled by 2/a; a2 equals a up to rounding
+    // (kwant/kpm.py:576-579), so in mixed mode only the diagonal shift of
+    // the second recursion is re-derived.
+    const double aL = h->precision == KPM_PREC_MIXED ? h->a : a2;
+    st = kind == STORE_C128
+             ? run_recursions<STORE_C128>(bR, &Vb, &psi, h->a, h->b, bL,
+                                          &omega, aL, b2, M, s2)
+             : run_recursions<STORE_BF16X3>(bR, &Vb, &psi, h->a, h->b, bL,
+                                            &omega, aL, b2, M, s2);
+  }
+  if (s2) {
+    // the contraction (on the handle's stream) needs both stores
+    if (cudaEventRecord(done, s2) != cudaSuccess ||
+        cudaStreamWaitEvent(s, done, 0) != cudaSuccess) {
+      if (st == KPM_OK) {
+        set_error("kpm_correlator_moments: stream ordering failed");
+        st = KPM_ECUDA;
+      }
+      cudaStreamSynchronize(s2);
     }
   }
   if (bL) {
-    kpm_block_destroy(bL);
+    kpm_block_destroy(bL);   // frees on its handle's stream (after s2's work)
     bL = nullptr;
+  }
+  if (bR) {
+    kpm_block_destroy(bR);
+    bR = nullptr;
   }
   if (st == KPM_OK) {
     if (gemm == 0)
@@ -271,6 +313,12 @@ int kpm_correlator_moments(kpm_handle* h, double a2, double b2,
   free_matrix(&Va, s);
   free_matrix(&Vb, s);
   cudaStreamSynchronize(s);
+  if (s2) {
+    cudaStreamSynchronize(s2);
+    cudaStreamDestroy(s2);
+  }
+  if (ready) cudaEventDestroy(ready);
+  if (done) cudaEventDestroy(done);
   return st;
 }
 

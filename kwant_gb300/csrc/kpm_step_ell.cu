@@ -252,7 +252,9 @@ static int dispatch_k(kpm_handle* h, int mode, bool dots, const StepArgs& a) {
 }
 
 int launch_step_ell(kpm_handle* h, int mode, bool dots, const StepArgs& a) {
-  if (a.vpl == 1) return dispatch_k<1, 1>(h, mode, dots, a);
+  if (a.vpl == 1)
+    return h->step_rpi == 2 ? dispatch_k<2, 1>(h, mode, dots, a)
+                            : dispatch_k<1, 1>(h, mode, dots, a);
   if (h->step_rpi == 2) return dispatch_k<2, 2>(h, mode, dots, a);
   return dispatch_k<1, 2>(h, mode, dots, a);
 }
