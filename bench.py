@@ -456,6 +456,103 @@ def run_ours(args):
     return 0
 
 
+def run_ldos(args):
+    """Local DOS workload (not the headline line): the graphene system of
+    the DOS workload with kwant.operator.Density on the 1000 sites nearest
+    the flake's centre as the operator (one output per site), R vectors, M
+    moments by the operator path (M - 1 matvecs, kwant/kpm.py:478-484).
+    Metric as the DOS line: nnz * R * M / time of one moment run."""
+    import torch
+    from kwant_gb300 import _lib, kpm, lattices, operator
+    syst = lattices.honeycomb(args.cells, t=1.0, flux=1.0 / 1000, W=0.5,
+                              seed=0)
+    ham = syst.hamiltonian_submatrix(sparse=True).tocsr()
+    n, nnz = ham.shape[0], ham.nnz
+    centre = syst.positions.mean(axis=0)
+    d = np.linalg.norm(syst.positions - centre, axis=1)
+    where = np.sort(np.argsort(d)[:1000])
+    dens = operator.Density(syst, where=list(where))
+    R, M = args.vectors, args.moments
+    _, v0, vecs = make_workload(args.cells, R)
+    lo, hi = kpm.spectral_bounds(ham, 0.05, v0, 'lanczos')
+    a, b = kpm._rescale_ab(lo, hi, 0.05)
+    handle = _lib.Handle(_lib.Csr(ham), a, b, _lib.PREC_MIXED, reorder=True)
+    op = _lib.Op(handle, operator.lower(dens))
+    block = _lib.Block(handle, vecs, keep_a0=True)
+    stream = torch.cuda.ExternalStream(handle.stream())
+
+    def one_step():
+        block.rewind()
+        return block.op_moments(op, 0, M)
+
+    for _ in range(args.warmup):
+        one_step()
+    handle.profile(True)
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        mom = one_step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    n_step, step_ms = handle.profile_read()
+    handle.profile(False)
+    ms = ev0.elapsed_time(ev1) / args.steps
+    accuracy = None
+    if args.accuracy:
+        # FP64 GPU path on the first 8 vectors (parity-tested at 1e-12)
+        k = min(8, R)
+        h64 = _lib.Handle(_lib.Csr(ham), a, b, _lib.PREC_FP64)
+        op64 = _lib.Op(h64, operator.lower(dens))
+        b64 = _lib.Block(h64, vecs[:k], keep_a0=True)
+        ref = b64.op_moments(op64, 0, M)
+        nodes = kpm._chebyshev_nodes(2 * M)
+        _, rho = _lib.reconstruct(mom[:k], True, True, a,
+                                  _lib.KERNEL_JACKSON, 4.0, nodes)
+        _, rho64 = _lib.reconstruct(ref, True, True, a,
+                                    _lib.KERNEL_JACKSON, 4.0, nodes)
+        inside = np.abs(nodes) <= (hi - lo) / (2 * a) * 0.999
+        err = np.abs(rho.real - rho64.real)
+        accuracy = {'ldos_linf_vs_fp64_inside_bounds':
+                    float(err[inside].max()),
+                    'ldos_max': float(np.abs(rho64.real).max()),
+                    'vectors_compared': k}
+        b64.close()
+        op64.close()
+        h64.close()
+    peaks = {}
+    pk = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    hbm = float(peaks.get('hbm_gbs', 6800.0))
+    B = step_bytes(nnz, n, R, 'mixed')
+    avg = step_ms / max(n_step, 1)
+    achieved = B / (avg / 1e3) / 1e9
+    line = {
+        'metric': METRIC, 'value': nnz * R * M / (ms / 1e3), 'unit': UNIT,
+        'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'c64+f64acc', 'data': 'synthetic',
+        'config': {'workload': 'LDOS: honeycomb %dx%d cells, Density on the '
+                               '1000 central sites, R=%d, M=%d'
+                               % (args.cells, args.cells, R, M),
+                   'nnz': int(nnz), 'orbitals': int(n), 'outputs': 1000},
+        'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm,
+                     'unit': 'GB/s', 'frac': achieved / hbm, 'traffic': None,
+                     'kernel': 'cheb_step_ell_kernel (operator path, no '
+                               'fused dots)',
+                     'algorithmic_bytes_per_launch': B, 'avg_launch_ms': avg,
+                     'launches_timed': n_step},
+        'accuracy': accuracy,
+    }
+    print(json.dumps(line))
+    block.close()
+    op.close()
+    handle.close()
+    return 0
+
+
 def run_kubo(args):
     """Kubo-Bastin workload (not the headline line): square 200 x 200, two
     orbitals, t = 1, Rashba 0.3, exchange 0.2, W = 1 (seed 0), R = 16
@@ -725,7 +822,8 @@ def main():
     p = argparse.ArgumentParser()
     p.add_argument('--workload', default='dos', choices=['dos', 'kubo',
                                                          'batch',
-                                                         'surrogate'])
+                                                         'surrogate',
+                                                         'ldos'])
     p.add_argument('--sur-cells', type=int, default=500)
     p.add_argument('--sur-moments', type=int, default=512)
     p.add_argument('--sur-vectors', type=int, default=32)
@@ -768,6 +866,8 @@ def main():
         return run_batch(args)
     if args.workload == 'surrogate':
         return run_surrogate(args)
+    if args.workload == 'ldos':
+        return run_ldos(args)
     return run_ours(args)
 
 
