@@ -226,6 +226,8 @@ class MomentSurrogate:
         ``scale`` times the largest (over energies) standard deviation of the
         members' DOS."""
         mem = self.predict_members(points)
+        if len(self.nets) < 2:                        # no spread: no estimate
+            return mem[0], np.full(mem.shape[1], np.inf)
         dos = mem @ dos_op.T                          # E x P x K
         spread = dos.std(axis=0, ddof=1).max(axis=1)
         return mem.mean(axis=0), self.scale * spread
@@ -235,8 +237,11 @@ class MomentSurrogate:
         (against the given KPM moments) on ``quantile`` of the points."""
         mem = self.predict_members(points)
         dos = mem @ dos_op.T
-        spread = dos.std(axis=0, ddof=1).max(axis=1)
         err = np.abs(dos.mean(axis=0) - moments @ dos_op.T).max(axis=1)
+        if len(self.nets) < 2:
+            self.scale = np.inf
+            return err, np.full(err.shape, np.inf)
+        spread = dos.std(axis=0, ddof=1).max(axis=1)
         self.scale = float(np.quantile(err / np.maximum(spread, 1e-300),
                                        quantile))
         return err, spread
