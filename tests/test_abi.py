@@ -54,3 +54,31 @@ def test_device_count_without_gpu_is_graceful():
     from kwant_gb300 import _lib
     n = _lib.device_count()
     assert n >= 0
+
+
+def test_argument_checks_and_missing_device_fail_cleanly():
+    """Invalid arguments are rejected before any device work, and without a
+    usable device every computing entry point returns KPM_ECUDA with a
+    message (there is no CPU fallback); nothing crashes."""
+    import numpy as np
+    from kwant_gb300 import _lib
+    lib = _lib.lib
+    P = ctypes.c_void_p
+    out = P()
+    # null / invalid arguments: KPM_EINVAL
+    assert lib.kpm_create(None, 1.0, 0.0, 0, ctypes.byref(out)) == -1
+    assert lib.kpm_family_point(None, 0.0, 0.0, 0.0) == -1
+    assert lib.kpm_chebval(0, 1, None, 0, None, None) == -1
+    w = np.array([3, 100, 32], np.int32)            # hidden width % 32 != 0
+    assert lib.kpm_mlp_create(2, w.ctypes.data_as(P), 64, 0,
+                              ctypes.byref(out)) == -1
+    assert lib.kpm_batch_create(4, 25, 0, ctypes.byref(out)) == -1  # odd M
+    assert lib.kpm_block_restore(None, 0, 0, None, None, None) == -1
+    if _lib.device_count() == 0:
+        m = np.eye(3, dtype=complex)
+        import scipy.sparse as sp
+        csr = _lib.Csr(sp.csr_matrix(m + np.diag([0, 1, 2])))
+        st = lib.kpm_create(csr.ref(), 2.0, 0.0, 0, ctypes.byref(out))
+        assert st == -2                                  # KPM_ECUDA
+        assert 'CUDA' in _lib.last_error()
+        assert lib.kpm_batch_create(4, 24, 0, ctypes.byref(out)) == -2
