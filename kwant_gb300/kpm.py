@@ -279,15 +279,48 @@ def _normalize_orbs_where(syst, where):
     return tot_norbs, orbs
 
 
+_PHASE_POOL = None
+
+
+def _phases(u):
+    """exp(2j * pi * u) elementwise, bit-identical to numpy's expression
+    (the same ufuncs on each element), computed in chunks on the host's
+    cores for long vectors (numpy's complex exp is single-threaded)."""
+    n = u.shape[0]
+    chunk = 1 << 18
+    if n < 4 * chunk:
+        return np.exp(2j * np.pi * u)
+    global _PHASE_POOL
+    if _PHASE_POOL is None:
+        import concurrent.futures
+        import os
+        _PHASE_POOL = concurrent.futures.ThreadPoolExecutor(
+            max_workers=max(1, min(32, os.cpu_count() or 1)))
+    out = np.empty(n, dtype=complex)
+
+    def work(i):
+        out[i:i + chunk] = np.exp(2j * np.pi * u[i:i + chunk])
+
+    list(_PHASE_POOL.map(work, range(0, n, chunk)))
+    return out
+
+
 def RandomVectors(syst, where=None, rng=None):
     """Random-phase vectors exp(2 pi i u) on the orbitals of ``where``
-    (kwant/kpm.py:932-951)."""
+    (kwant/kpm.py:932-951): the same stream and values as the reference."""
     rng = ensure_rng(rng)
     tot_norbs, orbs = _normalize_orbs_where(syst, where)
+    idx = np.asarray(orbs, dtype=np.intp)
+    full = idx.shape[0] == tot_norbs and np.array_equal(
+        idx, np.arange(tot_norbs))
     while True:
-        vector = np.zeros(tot_norbs, dtype=complex)
-        vector[orbs] = np.exp(2j * np.pi * rng.random_sample(len(orbs)))
-        yield vector
+        phases = _phases(rng.random_sample(idx.shape[0]))
+        if full:
+            yield phases
+        else:
+            vector = np.zeros(tot_norbs, dtype=complex)
+            vector[idx] = phases
+            yield vector
 
 
 class LocalVectors:
