@@ -17,14 +17,16 @@
 
 namespace kpm {
 
-// Blocks per SM the register budget is sized for (narrow rows need few
-// registers; 6 x 256 threads leaves 40 registers per thread).
+// Blocks per SM the register budget is sized for (5 x 256 threads leaves
+// 48 registers per thread: enough for rows of up to 12 entries without
+// spilling; 16-entry rows get 64).  Occupancy is what hides the gather
+// latency of these kernels.
 #ifndef KPM_ELL_MIN_BLOCKS
 #define KPM_ELL_MIN_BLOCKS 5
 #endif
 template <int K, int RPI>
 constexpr int ell_min_blocks() {
-  return (K <= 4 && RPI == 1) ? KPM_ELL_MIN_BLOCKS : 1;
+  return RPI != 1 ? 1 : (K <= 12 ? KPM_ELL_MIN_BLOCKS : 4);
 }
 
 template <int VPL> struct EllPay;
