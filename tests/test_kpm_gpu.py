@@ -454,3 +454,29 @@ def test_call_at_arbitrary_energies_on_device(kpm):
         # scalar energy
         assert np.array_equal(sd(float(E[0, 0])),
                               np.transpose(chebval(e[0, 0], mom) / g_e[0, 0]))
+
+
+def test_correlator_with_local_operators(kpm):
+    """Correlator(operator1=Density, operator2=Current) (kwant/kpm.py:557-
+    606): the operators act on the vectors through their ACT maps
+    (kwant/operator.pyx:561-606); moments matrix against the oracle with the
+    same matrices."""
+    from kwant_gb300.system import LatticeSystem
+    from kwant_gb300.operator import Density, Current, act_matrix
+    g = load('rashba_ops')
+    ham = csr(g)
+    n = ham.shape[0]
+    syst = LatticeSystem(ham, [(0, 2, 0), (n // 2, 0, n)], g['positions'])
+    sz = np.diag([1.0, -1.0])
+    dens = Density(syst, onsite=sz)
+    cur = Current(syst, onsite=sz, where=[tuple(w) for w in g['hop_where']])
+    R, M = 3, 24
+    rng = np.random.RandomState(9)
+    vecs = np.exp(2j * np.pi * rng.random_sample((R, n)))
+    corr = kpm.Correlator(ham, operator1=dens, operator2=cur,
+                          vector_factory=list(vecs), num_vectors=R,
+                          num_moments=M, bounds=(g['lmin'], g['lmax']))
+    ref, _, _ = ko.correlator_moments_matrix(
+        ham, vecs, g['lmin'], g['lmax'], M, act_matrix(dens, n),
+        act_matrix(cur, n))
+    assert _rel(corr.moments_matrix, ref) < 1e-11
