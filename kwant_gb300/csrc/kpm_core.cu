@@ -748,6 +748,37 @@ int block_advance(kpm_block* b, bool dots) {
   return KPM_OK;
 }
 
+int block_advance_store(kpm_block* b, int smode, const float2* vell,
+                        const StoreRow& row, int64_t R) {
+  kpm_handle* h = b->h;
+  if (h->precision != KPM_PREC_MIXED || h->H.ell_k == 0) {
+    set_error("fused store needs a complex64 ELL handle");
+    return KPM_EUNSUPPORTED;
+  }
+  void* x = b->p_cur;
+  void* out;
+  const void* prev = nullptr;
+  int mode;
+  if (b->steps_done == 0) {
+    out = b->buf[0];
+    mode = STEP_FIRST;
+  } else {
+    if (b->p_prev == b->a0 && b->keep_a0)
+      out = (b->p_cur == b->buf[0]) ? b->buf[1] : b->buf[0];
+    else
+      out = b->p_prev;
+    prev = b->p_prev;
+    mode = STEP_RECUR;
+  }
+  StepArgs a = step_args(b, x, prev, out);
+  StoreArgs sa{smode, vell, row, R};
+  KPM_TRY(launch_step_ell(h, mode, false, a, &sa));
+  b->p_prev = b->p_cur;
+  b->p_cur = out;
+  b->steps_done += 1;
+  return KPM_OK;
+}
+
 int block_norm(kpm_block* b) {
   StepArgs a = step_args(b, b->p_cur, nullptr, nullptr);
   return launch_step(b->h, STEP_NORM, false, a);

@@ -173,21 +173,94 @@ static int recursion_order(kpm_block* b, const Matrix* V, int64_t n,
   return st;
 }
 
+// Order n of a recursion with the store row of alpha_n written by the step
+// that computes alpha_{n+1} (complex64 ELL handles, BF16x3 stores): V's
+// product shares H's gathered rows, and no separate store launch is needed.
+static int fused_order(kpm_block* b, const Matrix* V, int64_t n, Store* store,
+                       double a, double bshift, cudaStream_t stream) {
+  kpm_handle* h = b->h;
+  const double a_save = h->a, b_save = h->b;
+  const cudaStream_t s_save = h->stream;
+  h->a = a;
+  h->b = bshift;
+  h->stream = stream;
+  int st = block_advance_store(b, V ? 2 : 1, V ? V->ell_val : nullptr,
+                               store->row(n), b->R);
+  h->a = a_save;
+  h->b = b_save;
+  h->stream = s_save;
+  return st;
+}
+
 // Both recursions of the correlator, interleaved order by order on two
 // streams: each is a chain of small dependent launches (latency-bound at
 // the sizes of the Kubo workload), and they are independent of each other.
+// With `fused`, orders 0 .. M-2 store from inside the step kernels and only
+// the last order uses the separate store kernel.
 template <int STORE>
 static int run_recursions(kpm_block* bR, const Matrix* Vb, Store* psi,
                           double a, double b, kpm_block* bL, Store* omega,
                           double a2, double b2, int64_t M,
-                          cudaStream_t s2) {
+                          cudaStream_t s2, bool fused) {
   int st = KPM_OK;
+  if (fused) {
+    for (int64_t n = 0; st == KPM_OK && n + 1 < M; ++n) {
+      st = fused_order(bR, Vb, n, psi, a, b, bR->h->stream);
+      if (st == KPM_OK) st = fused_order(bL, nullptr, n, omega, a2, b2, s2);
+    }
+    // last order: alpha_{M-1} is already computed; store it separately
+    if (st == KPM_OK) {
+      kpm_handle* h = bR->h;
+      st = put_row<STORE>(h, Vb, bR->p_cur, bR->N, bR->R, bR->Rpad,
+                          psi->row(M - 1));
+      const cudaStream_t s_save = h->stream;
+      h->stream = s2;
+      if (st == KPM_OK)
+        st = put_row<STORE>(h, nullptr, bL->p_cur, bL->N, bL->R, bL->Rpad,
+                            omega->row(M - 1));
+      h->stream = s_save;
+    }
+    return st;
+  }
   for (int64_t n = 0; st == KPM_OK && n < M; ++n) {
     st = recursion_order<STORE>(bR, Vb, n, psi, a, b, bR->h->stream);
     if (st == KPM_OK)
       st = recursion_order<STORE>(bL, nullptr, n, omega, a2, b2, s2);
   }
   return st;
+}
+
+__global__ void ell_index_diff_kernel(const int32_t* __restrict__ a,
+                                      const int32_t* __restrict__ b,
+                                      int64_t n, int* __restrict__ diff) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && a[i] != b[i]) atomicExch(diff, 1);
+}
+
+// Does V's ELL copy line up entry for entry with H's (same widths, same
+// column indices)?  Then V can share H's gathers.
+static int ell_aligned(kpm_handle* h, const Matrix* V, bool* aligned) {
+  *aligned = false;
+  if (h->H.ell_k == 0 || V->ell_k != h->H.ell_k || !V->ell_val) return KPM_OK;
+  int* diff = nullptr;
+  KPM_TRY(dev_alloc((void**)&diff, sizeof(int), h->stream));
+  const int64_t n = h->H.rows * (int64_t)h->H.ell_k;
+  int hd = 1;
+  cudaError_t e = cudaMemsetAsync(diff, 0, sizeof(int), h->stream);
+  if (e == cudaSuccess) {
+    ell_index_diff_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, h->stream>>>(
+        h->H.ell_idx, V->ell_idx, n, diff);
+    count_launch(1);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&hd, diff, sizeof(int), cudaMemcpyDeviceToHost,
+                        h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  dev_free(diff, h->stream);
+  KPM_CUDA(e);
+  *aligned = hd == 0;
+  return KPM_OK;
 }
 
 }  // namespace kpm
@@ -222,8 +295,15 @@ int kpm_correlator_moments(kpm_handle* h, double a2, double b2,
   // operators in the recursion's precision (complex64 values in mixed mode)
   const double vscale = h->precision == KPM_PREC_MIXED ? 1.0 : 0.0;
   int st = upload_matrix_for(h, v_alpha, vscale, &Va, false);
-  if (st == KPM_OK) st = upload_matrix_for(h, v_beta, vscale, &Vb, false);
   const int kind = gemm == 0 ? STORE_C128 : STORE_BF16X3;
+  // complex64 + BF16x3: V_beta also as ELL, to share the step's gathers
+  const bool want_fuse = h->precision == KPM_PREC_MIXED &&
+                         kind == STORE_BF16X3 && h->H.ell_k > 0 &&
+                         getenv("KPM_CORRELATOR_UNFUSED") == nullptr;
+  if (st == KPM_OK)
+    st = upload_matrix_for(h, v_beta, vscale, &Vb, want_fuse);
+  bool fused = false;
+  if (st == KPM_OK && want_fuse) st = ell_aligned(h, &Vb, &fused);
   if (st == KPM_OK) st = store_alloc(&psi, kind, M, K, s);
   if (st == KPM_OK) st = store_alloc(&omega, kind, M, K, s);
   if (st == KPM_OK) st = kpm_block_create(h, vecs, R, 1, &bR);
@@ -275,9 +355,9 @@ int kpm_correlator_moments(kpm_handle* h, double a2, double b2,
     const double aL = h->precision == KPM_PREC_MIXED ? h->a : a2;
     st = kind == STORE_C128
              ? run_recursions<STORE_C128>(bR, &Vb, &psi, h->a, h->b, bL,
-                                          &omega, aL, b2, M, s2)
+                                          &omega, aL, b2, M, s2, false)
              : run_recursions<STORE_BF16X3>(bR, &Vb, &psi, h->a, h->b, bL,
-                                            &omega, aL, b2, M, s2);
+                                            &omega, aL, b2, M, s2, fused);
   }
   if (s2) {
     // the contraction (on the handle's stream) needs both stores

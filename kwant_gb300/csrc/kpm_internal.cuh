@@ -2,6 +2,7 @@
 #pragma once
 
 #include "kpm_common.cuh"
+#include "kpm_gemm.cuh"
 
 namespace kpm {
 
@@ -22,6 +23,17 @@ struct StepArgs {
   int groups;
   int xitems;
   double* partials; // [groups][xitems][group][3]
+};
+
+// Fused store of alpha_n's row (the correlator's recursions, ELL step,
+// BF16x3 store): smode 0 none, 1 alpha_n itself, 2 V alpha_n with V's values
+// in an ELL copy aligned entry for entry with H's (vell).  A separate
+// kernel argument: inside StepArgs it made the plain step kernel spill.
+struct StoreArgs {
+  int smode;
+  const float2* vell;
+  StoreRow store;
+  int64_t R;
 };
 
 void count_launch(int n);
@@ -57,9 +69,15 @@ int launch_step(kpm_handle* h, int mode, bool dots, const StepArgs& a);
 constexpr int ELL_MAX = 16;
 int build_ell(kpm_handle* h, const kpm_csr_desc* m, double scale,
               Matrix* out);
-int launch_step_ell(kpm_handle* h, int mode, bool dots, const StepArgs& a);
+int launch_step_ell(kpm_handle* h, int mode, bool dots, const StepArgs& a,
+                    const StoreArgs* sa = nullptr);
 StepArgs step_args(kpm_block* b, const void* x, const void* prev, void* out);
 int block_advance(kpm_block* b, bool dots);
+// block_advance without dot products that also writes the store row of the
+// current vector (StepArgs::smode); KPM_EUNSUPPORTED when the handle has no
+// complex64 ELL copy (the caller then stores with a separate kernel)
+int block_advance_store(kpm_block* b, int smode, const float2* vell,
+                        const StoreRow& row, int64_t R);
 int block_norm(kpm_block* b);
 // sum the dot-product partials and write DOS moments (slots < 0 skipped)
 int finalize(kpm_block* b, int mode, double2* mom, int64_t slot_even,

@@ -50,10 +50,15 @@ template <> struct EllPay<1> {
 // VPL complex64 vectors per lane: 2 (groups of 32 vectors) or 1 (groups of
 // 16, for blocks of at most 16 vectors); every vector gets the same FMA
 // sequence either way.
-template <int K, int MODE, bool DOTS, int RPI, int VPL>
+// SM (store mode, the correlator's recursions): 1 also writes alpha_n (the
+// input x) into the BF16x3 store row, 2 writes V alpha_n, with V's entries
+// in an ELL copy aligned with H's, so that V shares H's gathered rows; the
+// products follow the separate store kernel's operation order.
+template <int K, int MODE, bool DOTS, int RPI, int VPL, int SM = 0>
 __global__ void __launch_bounds__(STEP_THREADS, ell_min_blocks<K, RPI>())
 cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
-                     const float2* __restrict__ eval) {
+                     const float2* __restrict__ eval, StoreArgs sa) {
+  static_assert(SM == 0 || (!DOTS && RPI == 1), "store fusion: no dots");
   using Pay = EllPay<VPL>;
   using PT = typename Pay::T;
   constexpr int G = LANES * VPL;
@@ -116,11 +121,15 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
       for (int u = 0; u < RPI; ++u) {
         if (!ok[u]) continue;
         float ar[VPL], ai[VPL];
+        float sr[VPL], si[VPL];        // store values (SM == 2: V alpha_n)
 #pragma unroll
         for (int k = 0; k < VPL; ++k) {
           ar[k] = shift * Pay::re(xv[u], k);
           ai[k] = shift * Pay::im(xv[u], k);
+          sr[k] = si[k] = 0.f;
         }
+        const float4* vv = SM == 2
+            ? reinterpret_cast<const float4*>(sa.vell + row[u] * K) : nullptr;
 #pragma unroll
         for (int q = 0; q < KQ; ++q) {
           const int cc[4] = {c4[u][q].x, c4[u][q].y, c4[u][q].z, c4[u][q].w};
@@ -139,6 +148,32 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
               ar[k] = fmaf(-hi[t], Pay::im(xx[t], k), ar[k]);
               ai[k] = fmaf(hr[t], Pay::im(xx[t], k), ai[k]);
               ai[k] = fmaf(hi[t], Pay::re(xx[t], k), ai[k]);
+            }
+          }
+          if constexpr (SM == 2) {
+            const float4 v01 = __ldg(vv + 2 * q), v23 = __ldg(vv + 2 * q + 1);
+            const float wr[4] = {v01.x, v01.z, v23.x, v23.z};
+            const float wi[4] = {v01.y, v01.w, v23.y, v23.w};
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+#pragma unroll
+              for (int k = 0; k < VPL; ++k) {
+                const float xr = Pay::re(xx[t], k), xi = Pay::im(xx[t], k);
+                sr[k] = fmaf(wr[t], xr, fmaf(-wi[t], xi, sr[k]));
+                si[k] = fmaf(wr[t], xi, fmaf(wi[t], xr, si[k]));
+              }
+            }
+          }
+        }
+        if constexpr (SM != 0) {
+          // store row of alpha_n: K index row * R + vector, real vectors only
+#pragma unroll
+          for (int k = 0; k < VPL; ++k) {
+            const int64_t vec = (int64_t)g * G + (int64_t)lane * VPL + k;
+            if (vec < sa.R) {
+              const float re = SM == 2 ? sr[k] : Pay::re(xv[u], k);
+              const float im = SM == 2 ? si[k] : Pay::im(xv[u], k);
+              store_put<STORE_BF16X3>(sa.store, row[u] * sa.R + vec, re, im);
             }
           }
         }
@@ -197,14 +232,15 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
   }
 }
 
-template <int K, int MODE, bool DOTS, int RPI, int VPL>
-static int launch_ell_t(kpm_handle* h, const StepArgs& a) {
+template <int K, int MODE, bool DOTS, int RPI, int VPL, int SM = 0>
+static int launch_ell_t(kpm_handle* h, const StepArgs& a,
+                        const StoreArgs& sa = StoreArgs{}) {
   static int occ = -1;
   if (occ < 0) {
     int blocks = 0;
     KPM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &blocks, cheb_step_ell_kernel<K, MODE, DOTS, RPI, VPL>, STEP_THREADS,
-        0));
+        &blocks, cheb_step_ell_kernel<K, MODE, DOTS, RPI, VPL, SM>,
+        STEP_THREADS, 0));
     occ = blocks > 0 ? blocks : 1;
   }
   const int64_t work = (int64_t)a.xitems * a.groups;
@@ -222,18 +258,35 @@ static int launch_ell_t(kpm_handle* h, const StepArgs& a) {
     h->prof_used += 2;
     KPM_CUDA(cudaEventRecord(e0, h->stream));
   }
-  cheb_step_ell_kernel<K, MODE, DOTS, RPI, VPL>
+  cheb_step_ell_kernel<K, MODE, DOTS, RPI, VPL, SM>
       <<<(unsigned)grid, STEP_THREADS, 0, h->stream>>>(a, h->H.ell_idx,
-                                                        h->H.ell_val);
+                                                        h->H.ell_val, sa);
   count_launch(1);
   KPM_CHECK_LAUNCH();
   if (e1) KPM_CUDA(cudaEventRecord(e1, h->stream));
   return KPM_OK;
 }
 
+template <int K, int VPL, int SM>
+static int dispatch_store_mode(kpm_handle* h, int mode, const StepArgs& a,
+                               const StoreArgs& sa) {
+  return mode == STEP_FIRST
+             ? launch_ell_t<K, STEP_FIRST, false, 1, VPL, SM>(h, a, sa)
+             : launch_ell_t<K, STEP_RECUR, false, 1, VPL, SM>(h, a, sa);
+}
+
+template <int K, int VPL>
+static int dispatch_store(kpm_handle* h, int mode, const StepArgs& a,
+                          const StoreArgs& sa) {
+  return sa.smode == 2 ? dispatch_store_mode<K, VPL, 2>(h, mode, a, sa)
+                       : dispatch_store_mode<K, VPL, 1>(h, mode, a, sa);
+}
+
 template <int K, int RPI, int VPL>
 static int dispatch_mode(kpm_handle* h, int mode, bool dots,
-                         const StepArgs& a) {
+                         const StepArgs& a, const StoreArgs* sa) {
+  if constexpr (RPI == 1)
+    if (sa && sa->smode) return dispatch_store<K, VPL>(h, mode, a, *sa);
   if (mode == STEP_FIRST)
     return dots ? launch_ell_t<K, STEP_FIRST, true, RPI, VPL>(h, a)
                 : launch_ell_t<K, STEP_FIRST, false, RPI, VPL>(h, a);
@@ -242,23 +295,28 @@ static int dispatch_mode(kpm_handle* h, int mode, bool dots,
 }
 
 template <int RPI, int VPL>
-static int dispatch_k(kpm_handle* h, int mode, bool dots, const StepArgs& a) {
+static int dispatch_k(kpm_handle* h, int mode, bool dots, const StepArgs& a,
+                      const StoreArgs* sa) {
   switch (h->H.ell_k) {
-    case 4: return dispatch_mode<4, RPI, VPL>(h, mode, dots, a);
-    case 8: return dispatch_mode<8, RPI, VPL>(h, mode, dots, a);
-    case 12: return dispatch_mode<12, RPI, VPL>(h, mode, dots, a);
-    case 16: return dispatch_mode<16, RPI, VPL>(h, mode, dots, a);
+    case 4: return dispatch_mode<4, RPI, VPL>(h, mode, dots, a, sa);
+    case 8: return dispatch_mode<8, RPI, VPL>(h, mode, dots, a, sa);
+    case 12: return dispatch_mode<12, RPI, VPL>(h, mode, dots, a, sa);
+    case 16: return dispatch_mode<16, RPI, VPL>(h, mode, dots, a, sa);
   }
   set_error("ELL width %d not supported", h->H.ell_k);
   return KPM_EUNSUPPORTED;
 }
 
-int launch_step_ell(kpm_handle* h, int mode, bool dots, const StepArgs& a) {
+int launch_step_ell(kpm_handle* h, int mode, bool dots, const StepArgs& a,
+                    const StoreArgs* sa) {
+  const bool store = sa && sa->smode;
   if (a.vpl == 1)
-    return h->step_rpi == 2 ? dispatch_k<2, 1>(h, mode, dots, a)
-                            : dispatch_k<1, 1>(h, mode, dots, a);
-  if (h->step_rpi == 2) return dispatch_k<2, 2>(h, mode, dots, a);
-  return dispatch_k<1, 2>(h, mode, dots, a);
+    return h->step_rpi == 2 && !store
+               ? dispatch_k<2, 1>(h, mode, dots, a, nullptr)
+               : dispatch_k<1, 1>(h, mode, dots, a, sa);
+  if (h->step_rpi == 2 && !store)
+    return dispatch_k<2, 2>(h, mode, dots, a, nullptr);
+  return dispatch_k<1, 2>(h, mode, dots, a, sa);
 }
 
 }  // namespace kpm
