@@ -70,20 +70,6 @@ __device__ __forceinline__ void cmac(float& ar, float& ai, float hr, float hi,
   ai = fmaf(hi, xr, ai);
 }
 
-// 16-byte asynchronous global -> shared copy (L2 only), grouped per thread
-__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
-                   static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
-               "l"(src)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() {
-  asm volatile("cp.async.commit_group;" ::: "memory");
-}
-__device__ __forceinline__ void cp_async_wait_prev() {
-  asm volatile("cp.async.wait_group 1;" ::: "memory");
-}
-
 // Block rows per CTA tile: one per 16-lane slot.
 constexpr int TILE = SLOTS;
 // 16-byte chunks of one tile's block values and indices

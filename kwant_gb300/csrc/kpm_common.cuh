@@ -84,6 +84,21 @@ __host__ __device__ inline uint64_t mix64(uint64_t z) {
   return z ^ (z >> 31);
 }
 
+// 16-byte asynchronous global -> shared copy (L2 only), grouped per thread
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                   static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+// wait until at most the most recent group is still in flight
+__device__ __forceinline__ void cp_async_wait_prev() {
+  asm volatile("cp.async.wait_group 1;" ::: "memory");
+}
+
 inline int xitems_for_rows(int64_t rows) {
   int64_t x = ceil_div(rows, (int64_t)SLOTS);
   if (x > MAX_XITEMS) x = MAX_XITEMS;

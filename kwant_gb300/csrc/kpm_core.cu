@@ -902,7 +902,9 @@ int kpm_create_ex(const kpm_csr_desc* ham, double a, double b, int precision,
   KPM_REQUIRE(ham->rows > 0 && ham->nnz >= 0 && ham->indptr && ham->indices &&
                   (ham->nnz == 0 || ham->data),
               "kpm_create: invalid CSR descriptor");
-  KPM_REQUIRE(ham->rows < INT32_MAX && ham->nnz < INT32_MAX,
+  // (the step kernels walk rows in 32-bit counters that run up to 2^17
+  // past the last row)
+  KPM_REQUIRE(ham->rows < INT32_MAX - (1 << 17) && ham->nnz < INT32_MAX,
               "kpm_create: CSR exceeds int32 indexing (rows=%lld nnz=%lld)",
               (long long)ham->rows, (long long)ham->nnz);
   KPM_REQUIRE(precision == KPM_PREC_FP64 || precision == KPM_PREC_MIXED,

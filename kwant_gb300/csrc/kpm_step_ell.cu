@@ -4,13 +4,13 @@
 // entry for entry and in the same order (ELL padding adds 0 * x exactly, and
 // the FP32 -> FP64 flush points and the reduction order are unchanged), so
 // results are bit-identical; it differs only in how it feeds the memory
-// system.  A row's column indices and values are fetched with 16-byte loads
-// that do not depend on a row-pointer load, and the row's own vector entry
-// and its alpha_{n-1} entry are requested together with them: every row
-// costs two dependent memory round trips instead of four.  RPI rows per
-// iteration overlap those round trips across rows; the FP64 dot-product
-// accumulators live in shared memory to keep registers (and so occupancy)
-// low.
+// system.  The two slots of a warp walk adjacent rows; the column indices
+// and values of the warp's next row pair are copied into shared memory
+// with cp.async (16-byte chunks, no row-pointer load) while the current
+// pair computes, so a row's gathers go out together with its own vector
+// entry and its alpha_{n-1} entry: one dependent memory round trip per row
+// (a CSR row costs four).  The FP64 dot-product accumulators live in shared
+// memory to keep registers (and so occupancy) low.
 
 #include "kpm_common.cuh"
 #include "kpm_internal.cuh"
@@ -65,21 +65,48 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
   constexpr int KQ = K / 4;
   const int lane = threadIdx.x & (LANES - 1);
   const int slot = threadIdx.x / LANES;
+  const int wq = slot >> 1, half = slot & 1, wl = threadIdx.x & 31;
   // FP64 accumulators of this slot's lanes, then the in-block reduction
   __shared__ double red[DOTS ? SLOTS : 1][DOTS ? G * 3 : 1];
+  // ELL entries of each warp's next two rows (per row-per-iteration u),
+  // double-buffered
+  __shared__ __align__(16) int32_t sidx[STEP_THREADS / 32][2][RPI][2 * K];
+  __shared__ __align__(16) float2 sval[STEP_THREADS / 32][2][RPI][2 * K];
 
   const PT* __restrict__ x = reinterpret_cast<const PT*>(p.x);
   const PT* prev = reinterpret_cast<const PT*>(p.prev);
   PT* out = reinterpret_cast<PT*>(p.out);
-  const int64_t work = (int64_t)p.xitems * p.groups;
-  const int64_t stride = (int64_t)p.xitems * SLOTS;
+  const int work = p.xitems * p.groups;
+  // row counters in 32 bits (CSR indices are int32); addresses in 64
+  const int rows = (int)p.rows;
+  const int stride = p.xitems * SLOTS;
   const float shift = p.shift;
   constexpr int FLUSH = 32;
 
-  for (int64_t w = blockIdx.x; w < work; w += gridDim.x) {
-    const int xi = (int)(w / p.groups);
-    const int g = (int)(w - (int64_t)xi * p.groups);
-    const int64_t col = (int64_t)g * LANES + lane;
+  // Copy the entries of rows r0 + h + u * stride (h < 2, u < RPI) into
+  // stage buffer b: 16-byte chunks, two rows' indices then their values.
+  auto stage = [&](int r0, int b) {
+    constexpr int IC = K / 2, VC = K;
+    for (int c = wl; c < RPI * (IC + VC); c += 32) {
+      const int u = c / (IC + VC), d = c % (IC + VC);
+      const int base = r0 + u * stride;
+      if (d < IC) {
+        if (base + (4 * d) / K < rows)
+          cp_async16(&sidx[wq][b][u][4 * d],
+                     eidx + (int64_t)base * K + 4 * d);
+      } else {
+        const int e = d - IC;
+        if (base + (2 * e) / K < rows)
+          cp_async16(&sval[wq][b][u][2 * e],
+                     eval + (int64_t)base * K + 2 * e);
+      }
+    }
+  };
+
+  for (int w = blockIdx.x; w < work; w += gridDim.x) {
+    const int xi = w / p.groups;
+    const int g = w - xi * p.groups;
+    const int col = g * LANES + lane;
     double* my = DOTS ? &red[slot][lane * VPL * 3] : nullptr;
     if constexpr (DOTS) {
 #pragma unroll
@@ -90,14 +117,25 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
     for (int k = 0; k < VPL; ++k) fn[k] = fr[k] = fi[k] = 0.f;
     int pending = 0;
 
-    for (int64_t i0 = (int64_t)xi * SLOTS + slot; i0 < p.rows;
-         i0 += RPI * stride) {
+    // the warp's two slots walk adjacent rows; the entries of its next
+    // row pair are in flight while the current pair computes, so a row's
+    // gathers go out together with its own vector loads
+    const int wb0 = xi * SLOTS + 2 * wq;
+    if (wb0 < rows) stage(wb0, 0);
+    cp_async_commit();
+    int sb = 0;
+    for (int wb = wb0; wb < rows; wb += RPI * stride) {
+      if (wb + RPI * stride < rows) stage(wb + RPI * stride, sb ^ 1);
+      cp_async_commit();
+      cp_async_wait_prev();
+      __syncwarp();
+      const int i0 = wb + half;
       int64_t row[RPI];
       bool ok[RPI];
 #pragma unroll
       for (int u = 0; u < RPI; ++u) {
         row[u] = i0 + u * stride;
-        ok[u] = row[u] < p.rows;
+        ok[u] = row[u] < rows;
       }
       PT xv[RPI], pv[RPI];
       int4 c4[RPI][KQ];
@@ -108,13 +146,14 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
         const int64_t r = row[u];
         xv[u] = x[r * p.rp + col];
         if constexpr (MODE == STEP_RECUR) pv[u] = prev[r * p.rp + col];
-        const int4* ri = reinterpret_cast<const int4*>(eidx + r * K);
-        const float4* rv = reinterpret_cast<const float4*>(eval + r * K);
+        const int4* ri = reinterpret_cast<const int4*>(&sidx[wq][sb][u][half * K]);
+        const float4* rv =
+            reinterpret_cast<const float4*>(&sval[wq][sb][u][half * K]);
 #pragma unroll
         for (int q = 0; q < KQ; ++q) {
-          c4[u][q] = __ldg(ri + q);
-          hv[u][2 * q] = __ldg(rv + 2 * q);
-          hv[u][2 * q + 1] = __ldg(rv + 2 * q + 1);
+          c4[u][q] = ri[q];
+          hv[u][2 * q] = rv[2 * q];
+          hv[u][2 * q + 1] = rv[2 * q + 1];
         }
       }
 #pragma unroll
@@ -129,7 +168,8 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
           sr[k] = si[k] = 0.f;
         }
         const float4* vv = SM == 2
-            ? reinterpret_cast<const float4*>(sa.vell + row[u] * K) : nullptr;
+            ? reinterpret_cast<const float4*>(sa.vell + (int64_t)row[u] * K)
+            : nullptr;
 #pragma unroll
         for (int q = 0; q < KQ; ++q) {
           const int cc[4] = {c4[u][q].x, c4[u][q].y, c4[u][q].z, c4[u][q].w};
@@ -173,7 +213,8 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
             if (vec < sa.R) {
               const float re = SM == 2 ? sr[k] : Pay::re(xv[u], k);
               const float im = SM == 2 ? si[k] : Pay::im(xv[u], k);
-              store_put<STORE_BF16X3>(sa.store, row[u] * sa.R + vec, re, im);
+              store_put<STORE_BF16X3>(sa.store, (int64_t)row[u] * sa.R + vec,
+                                      re, im);
             }
           }
         }
@@ -188,7 +229,7 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
             oii[k] = ai[k] - Pay::im(pv[u], k);
           }
         }
-        out[row[u] * p.rp + col] = Pay::make(orr, oii);
+        out[(int64_t)row[u] * p.rp + col] = Pay::make(orr, oii);
         if constexpr (DOTS) {
 #pragma unroll
           for (int k = 0; k < VPL; ++k) {
@@ -209,6 +250,8 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
           }
         }
       }
+      __syncwarp();   // stage buffer sb is refilled two iterations on
+      sb ^= 1;
     }
     if constexpr (DOTS) {
 #pragma unroll
