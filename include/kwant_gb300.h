@@ -217,7 +217,7 @@ KPM_API int kpm_dos(const kpm_csr_desc* ham, double a, double b, int precision,
  * make that first call before any stream capture.  Calls whose GPU work
  * overlaps in time share the scratch array and race; the array keeps the
  * last call's contents, and every call writes what it reads.  Sizes whose
- * scratch would exceed KPM_NOALLOC_SCRATCH_BYTES (more than about 160
+ * scratch would exceed KPM_NOALLOC_SCRATCH_BYTES (more than about 500
  * vectors at the largest row-partition count) are rejected with KPM_EINVAL. */
 typedef struct kpm_device_csr {
   int64_t rows;

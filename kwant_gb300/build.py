@@ -53,6 +53,14 @@ def build(verbose=False, extra_flags=()):
     os.makedirs(BUILD, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, '*.cu')))
     dep_t = _deps_mtime()
+    # objects built with other flags are stale too
+    stamp = os.path.join(BUILD, 'flags.txt')
+    flags = ' '.join(ARCH + NVCC_FLAGS + list(extra_flags))
+    if not os.path.exists(stamp) or open(stamp).read() != flags:
+        for o in glob.glob(os.path.join(BUILD, '*.o')):
+            os.remove(o)
+        with open(stamp, 'w') as f:
+            f.write(flags)
     jobs = []
     objs = []
     for src in srcs:

@@ -1148,7 +1148,8 @@ int prepare(kpm_batch* bt) {
     const size_t vb = (size_t)N * bt->Rpad * sizeof(float2);
     for (int k = 0; k < 3; ++k) KPM_TRY(dev_alloc(&y.v[k], vb, s));
     // row partitions: of block rows (BSR) or orbital rows (ELL)
-    const int xit[2] = {xitems_for_rows(y.nb), xitems_for_rows(N)};
+    const int xit[2] = {xitems_for_rows(y.nb, bt->num_sms),
+                          xitems_for_rows(N, bt->num_sms)};
     const int xmax = std::max(xit[0], have_ell ? xit[1] : 0);
     KPM_TRY(dev_alloc((void**)&y.partials,
                       (size_t)bt->Rpad * 3 * xmax * sizeof(double), s));

@@ -53,10 +53,15 @@ constexpr int SLOTS = STEP_THREADS / LANES;
 // Vectors per group: 16 (complex128) or 32 (complex64).
 constexpr int GROUP_FP64 = LANES;
 constexpr int GROUP_FP32 = 2 * LANES;
-// Upper bound on the number of row partitions ("x items") of a step: fixed,
-// so the reduction order of every dot product depends only on the number of
-// rows, never on the number of vectors or on the launch shape.
-constexpr int MAX_XITEMS = 2048;
+// Upper bound on the number of row partitions ("x items") of a step, per
+// SM.  The partition count depends only on the number of rows and the
+// device's SM count, never on the number of vectors or on the launch
+// shape, so the reduction order of every dot product is fixed for a given
+// GPU model.  4 is the resident blocks per SM of the complex64 ELL step
+// kernel: its persistent grid then gets exactly one long run of rows per
+// vector group and block (the per-item pipeline start and block reduction
+// are amortised over many rows, and no block idles in a last round).
+constexpr int XITEMS_PER_SM = 4;
 
 inline int group_size(int precision) {
   return precision == KPM_PREC_MIXED ? GROUP_FP32 : GROUP_FP64;
@@ -99,9 +104,10 @@ __device__ __forceinline__ void cp_async_wait_prev() {
   asm volatile("cp.async.wait_group 1;" ::: "memory");
 }
 
-inline int xitems_for_rows(int64_t rows) {
+inline int xitems_for_rows(int64_t rows, int num_sms) {
   int64_t x = ceil_div(rows, (int64_t)SLOTS);
-  if (x > MAX_XITEMS) x = MAX_XITEMS;
+  const int64_t cap = (int64_t)XITEMS_PER_SM * (num_sms > 0 ? num_sms : 1);
+  if (x > cap) x = cap;
   if (x < 1) x = 1;
   return (int)x;
 }

@@ -718,7 +718,7 @@ StepArgs step_args(kpm_block* b, const void* x, const void* prev, void* out) {
   a.vpl = h->precision == KPM_PREC_MIXED ? b->G / GROUP_FP64 : 1;
   a.rp = b->Rpad / a.vpl;
   a.groups = b->groups;
-  a.xitems = xitems_for_rows(b->N);
+  a.xitems = xitems_for_rows(b->N, h->num_sms);
   a.partials = h->partials;
   return a;
 }
@@ -788,7 +788,7 @@ int finalize(kpm_block* b, int mode, double2* mom, int64_t slot_even,
              int64_t slot_odd) {
   kpm_handle* h = b->h;
   dos_finalize_kernel<<<(unsigned)b->Rpad, 128, 0, h->stream>>>(
-      h->partials, b->G, xitems_for_rows(b->N), b->Rpad,
+      h->partials, b->G, xitems_for_rows(b->N, h->num_sms), b->Rpad,
       mode, (double2*)b->mu01, mom, b->Rpad, slot_even, slot_odd);
   count_launch(1);
   KPM_CHECK_LAUNCH();
@@ -1203,7 +1203,7 @@ int kpm_block_dos_moments(kpm_block* b, int64_t m_start, int64_t m_end,
   b->mode = 0;
   const int64_t count = m_end - m_start;
   const int G = group_size(h->precision);
-  KPM_TRY(ensure_partials(h, b->groups, xitems_for_rows(b->N)));
+  KPM_TRY(ensure_partials(h, b->groups, xitems_for_rows(b->N, h->num_sms)));
   double2* mom = nullptr;
   KPM_TRY(dev_alloc((void**)&mom, (size_t)count * b->Rpad * sizeof(double2),
                     h->stream));

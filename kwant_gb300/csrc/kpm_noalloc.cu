@@ -83,11 +83,15 @@ int kpm_dos_moments_noalloc(const kpm_device_csr* ham, double a, double b,
               "kpm_dos_moments_noalloc: need num_vectors > 0 and "
               "num_moments >= 2");
 
+  double* scratch = nullptr;
+  int sms = 0;
+  KPM_TRY(noalloc_scratch(&scratch, &sms));
+
   const int G = group_size(precision);
   const int64_t N = ham->rows;
   const int64_t Rpad = round_up(R, G);
   const int groups = (int)(Rpad / G);
-  const int xitems = xitems_for_rows(N);
+  const int xitems = xitems_for_rows(N, sms);
   const size_t partials = (size_t)groups * xitems * G * 3;  // doubles
   const size_t need = partials + (size_t)Rpad * 4;          // + mu0, mu1
   const size_t cap = KPM_NOALLOC_SCRATCH_BYTES / sizeof(double);
@@ -97,10 +101,6 @@ int kpm_dos_moments_noalloc(const kpm_device_csr* ham, double a, double b,
               "holds; use fewer vectors per call", (long long)R,
               (long long)N, need * sizeof(double),
               (size_t)KPM_NOALLOC_SCRATCH_BYTES);
-
-  double* scratch = nullptr;
-  int sms = 0;
-  KPM_TRY(noalloc_scratch(&scratch, &sms));
 
   // Stack descriptors over the caller's buffers: nothing is allocated.
   kpm_handle h;

@@ -17,16 +17,15 @@
 
 namespace kpm {
 
-// Blocks per SM the register budget is sized for (5 x 256 threads leaves
-// 48 registers per thread: enough for rows of up to 12 entries without
-// spilling; 16-entry rows get 64).  Occupancy is what hides the gather
-// latency of these kernels.
+// Blocks per SM the register budget is sized for: 4 x 256 threads leaves
+// 64 registers per thread, which every variant fits without spilling (at 5
+// blocks, 48 registers, the fused-dots step spills and runs 1.6x slower).
 #ifndef KPM_ELL_MIN_BLOCKS
-#define KPM_ELL_MIN_BLOCKS 5
+#define KPM_ELL_MIN_BLOCKS 4
 #endif
 template <int K, int RPI>
 constexpr int ell_min_blocks() {
-  return RPI != 1 ? 1 : (K <= 12 ? KPM_ELL_MIN_BLOCKS : 4);
+  return RPI != 1 ? 1 : KPM_ELL_MIN_BLOCKS;
 }
 
 template <int VPL> struct EllPay;
