@@ -112,85 +112,173 @@ int validate_csr(const kpm_csr_desc* m) {
   return KPM_OK;
 }
 
+namespace {
+
+// device staging buffer released on every exit path
+struct Staging {
+  void* p = nullptr;
+  cudaStream_t s;
+  explicit Staging(cudaStream_t st) : s(st) {}
+  ~Staging() { dev_free(p, s); }
+  int alloc(size_t bytes) { return dev_alloc(&p, bytes, s); }
+};
+
+}  // namespace
+
+// new row p = old row perm[p], columns renumbered by iperm, entry order
+// within each row kept; values complex128 (C64 false) or complex64 * scale
+template <bool C64>
+__global__ void permute_rows_kernel(int64_t n, const int32_t* __restrict__ perm,
+                                    const int32_t* __restrict__ iperm,
+                                    const int32_t* __restrict__ oip,
+                                    const int32_t* __restrict__ oix,
+                                    const double2* __restrict__ oval,
+                                    const int32_t* __restrict__ nip,
+                                    int32_t* __restrict__ nix,
+                                    void* __restrict__ nval, double scale) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const int32_t o = perm[p];
+  int32_t dst = nip[p];
+  for (int32_t k = oip[o]; k < oip[o + 1]; ++k, ++dst) {
+    nix[dst] = iperm[oix[k]];
+    const double2 v = oval[k];
+    if constexpr (C64)
+      static_cast<float2*>(nval)[dst] =
+          make_float2((float)(v.x * scale), (float)(v.y * scale));
+    else
+      static_cast<double2*>(nval)[dst] = v;
+  }
+}
+
+// ELL rows of width K from a device CSR with complex64 values; padding
+// entries point at the row itself with value 0
+__global__ void ell_from_csr_kernel(int64_t n, int K,
+                                    const int32_t* __restrict__ ip,
+                                    const int32_t* __restrict__ ix,
+                                    const float2* __restrict__ val,
+                                    int32_t* __restrict__ eidx,
+                                    float2* __restrict__ eval) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  int q = 0;
+  for (int32_t k = ip[p]; k < ip[p + 1]; ++k, ++q) {
+    eidx[p * K + q] = ix[k];
+    eval[p * K + q] = val[k];
+  }
+  for (; q < K; ++q) {
+    eidx[p * K + q] = (int32_t)p;
+    eval[p * K + q] = make_float2(0.f, 0.f);
+  }
+}
+
 int upload_matrix(kpm_handle* h, const kpm_csr_desc* m, double scale,
                   Matrix* out, bool with_ell) {
-  KPM_TRY(validate_csr(m));
-  out->rows = m->rows;
-  out->nnz = m->nnz;
-  KPM_TRY(dev_alloc((void**)&out->indptr, (m->rows + 1) * sizeof(int32_t),
-                    h->stream));
-  KPM_TRY(dev_alloc((void**)&out->indices,
-                    (m->nnz > 0 ? m->nnz : 1) * sizeof(int32_t), h->stream));
-  KPM_CUDA(cudaMemcpyAsync(out->indptr, m->indptr,
-                           (m->rows + 1) * sizeof(int32_t),
-                           cudaMemcpyHostToDevice, h->stream));
-  if (m->nnz > 0)
-    KPM_CUDA(cudaMemcpyAsync(out->indices, m->indices,
-                             m->nnz * sizeof(int32_t), cudaMemcpyHostToDevice,
-                             h->stream));
+  return upload_matrix_perm(h, m, scale, out, with_ell, nullptr, nullptr,
+                            true);
+}
+
+int upload_matrix_perm(kpm_handle* h, const kpm_csr_desc* m, double scale,
+                       Matrix* out, bool with_ell, const int32_t* perm,
+                       const int32_t* iperm, bool validate) {
+  if (validate) KPM_TRY(validate_csr(m));
+  cudaStream_t s = h->stream;
+  const int64_t n = m->rows;
   const int64_t nz = m->nnz > 0 ? m->nnz : 1;
-  if (scale == 0.0) {
-    KPM_TRY(dev_alloc(&out->data, nz * sizeof(double2), h->stream));
+  const bool c64 = scale != 0.0;
+  out->rows = n;
+  out->nnz = m->nnz;
+  KPM_TRY(dev_alloc((void**)&out->indptr, (n + 1) * sizeof(int32_t), s));
+  KPM_TRY(dev_alloc((void**)&out->indices, nz * sizeof(int32_t), s));
+  KPM_TRY(dev_alloc(&out->data, nz * (c64 ? sizeof(float2) : sizeof(double2)),
+                    s));
+  Staging vals(s);
+  if (!perm) {
+    KPM_CUDA(cudaMemcpyAsync(out->indptr, m->indptr, (n + 1) * sizeof(int32_t),
+                             cudaMemcpyHostToDevice, s));
     if (m->nnz > 0)
-      KPM_CUDA(cudaMemcpyAsync(out->data, m->data, m->nnz * sizeof(double2),
-                               cudaMemcpyHostToDevice, h->stream));
-  } else {
-    KPM_TRY(dev_alloc(&out->data, nz * sizeof(float2), h->stream));
-    if (m->nnz > 0) {
-      void* staging = nullptr;
-      KPM_TRY(dev_alloc(&staging, m->nnz * sizeof(double2), h->stream));
-      cudaError_t e = cudaMemcpyAsync(staging, m->data,
-                                      m->nnz * sizeof(double2),
-                                      cudaMemcpyHostToDevice, h->stream);
-      if (e == cudaSuccess) {
-        scale_to_c64_kernel<<<(unsigned)ceil_div(m->nnz, 256), 256, 0,
-                              h->stream>>>((const double2*)staging,
-                                           (float2*)out->data, m->nnz, scale);
-        count_launch(1);
-        e = cudaGetLastError();
-      }
-      dev_free(staging, h->stream);
-      KPM_CUDA(e);
+      KPM_CUDA(cudaMemcpyAsync(out->indices, m->indices,
+                               m->nnz * sizeof(int32_t),
+                               cudaMemcpyHostToDevice, s));
+    if (!c64) {
+      if (m->nnz > 0)
+        KPM_CUDA(cudaMemcpyAsync(out->data, m->data, m->nnz * sizeof(double2),
+                                 cudaMemcpyHostToDevice, s));
+    } else if (m->nnz > 0) {
+      KPM_TRY(vals.alloc(m->nnz * sizeof(double2)));
+      KPM_CUDA(cudaMemcpyAsync(vals.p, m->data, m->nnz * sizeof(double2),
+                               cudaMemcpyHostToDevice, s));
+      scale_to_c64_kernel<<<(unsigned)ceil_div(m->nnz, 256), 256, 0, s>>>(
+          (const double2*)vals.p, (float2*)out->data, m->nnz, scale);
+      count_launch(1);
+      KPM_CHECK_LAUNCH();
     }
-    if (with_ell) KPM_TRY(build_ell(h, m, scale, out));
+  } else {
+    // row pointers of the permuted matrix (host, O(rows)); the entries are
+    // moved on the device
+    std::vector<int32_t> nip(n + 1);
+    nip[0] = 0;
+    for (int64_t p = 0; p < n; ++p)
+      nip[p + 1] = nip[p] + (m->indptr[perm[p] + 1] - m->indptr[perm[p]]);
+    KPM_CUDA(cudaMemcpyAsync(out->indptr, nip.data(),
+                             (n + 1) * sizeof(int32_t),
+                             cudaMemcpyHostToDevice, s));
+    Staging oip(s), oix(s), dperm(s), diperm(s);
+    KPM_TRY(oip.alloc((n + 1) * sizeof(int32_t)));
+    KPM_TRY(oix.alloc(nz * sizeof(int32_t)));
+    KPM_TRY(vals.alloc(nz * sizeof(double2)));
+    KPM_TRY(dperm.alloc(n * sizeof(int32_t)));
+    KPM_TRY(diperm.alloc(n * sizeof(int32_t)));
+    KPM_CUDA(cudaMemcpyAsync(oip.p, m->indptr, (n + 1) * sizeof(int32_t),
+                             cudaMemcpyHostToDevice, s));
+    if (m->nnz > 0) {
+      KPM_CUDA(cudaMemcpyAsync(oix.p, m->indices, m->nnz * sizeof(int32_t),
+                               cudaMemcpyHostToDevice, s));
+      KPM_CUDA(cudaMemcpyAsync(vals.p, m->data, m->nnz * sizeof(double2),
+                               cudaMemcpyHostToDevice, s));
+    }
+    KPM_CUDA(cudaMemcpyAsync(dperm.p, perm, n * sizeof(int32_t),
+                             cudaMemcpyHostToDevice, s));
+    KPM_CUDA(cudaMemcpyAsync(diperm.p, iperm, n * sizeof(int32_t),
+                             cudaMemcpyHostToDevice, s));
+    const unsigned blocks = (unsigned)ceil_div(n, 256);
+    if (c64)
+      permute_rows_kernel<true><<<blocks, 256, 0, s>>>(
+          n, (const int32_t*)dperm.p, (const int32_t*)diperm.p,
+          (const int32_t*)oip.p, (const int32_t*)oix.p,
+          (const double2*)vals.p, out->indptr, out->indices, out->data, scale);
+    else
+      permute_rows_kernel<false><<<blocks, 256, 0, s>>>(
+          n, (const int32_t*)dperm.p, (const int32_t*)diperm.p,
+          (const int32_t*)oip.p, (const int32_t*)oix.p,
+          (const double2*)vals.p, out->indptr, out->indices, out->data, 0.0);
+    count_launch(1);
+    KPM_CHECK_LAUNCH();
+    // the staging buffers are released (stream-ordered) when this scope
+    // ends, after the kernel that reads them
   }
-  KPM_CUDA(cudaStreamSynchronize(h->stream));
+  if (c64 && with_ell) KPM_TRY(build_ell(h, m, out));
+  KPM_CUDA(cudaStreamSynchronize(s));
   return KPM_OK;
 }
 
-// ELL copy (complex64, values * scale) for rows of at most ELL_MAX entries.
-int build_ell(kpm_handle* h, const kpm_csr_desc* m, double scale,
-              Matrix* out) {
+// ELL copy (complex64) of a device CSR whose rows have at most ELL_MAX
+// entries; the width comes from the host row pointers.
+int build_ell(kpm_handle* h, const kpm_csr_desc* m, Matrix* out) {
   int64_t maxnnz = 0;
   for (int64_t i = 0; i < m->rows; ++i)
     maxnnz = std::max<int64_t>(maxnnz, m->indptr[i + 1] - m->indptr[i]);
   const int64_t K = round_up(maxnnz > 0 ? maxnnz : 1, 4);
   if (K > ELL_MAX) return KPM_OK;  // the CSR kernel handles wide rows
-  std::vector<int32_t> idx((size_t)m->rows * K);
-  std::vector<float2> val((size_t)m->rows * K);
-  for (int64_t i = 0; i < m->rows; ++i) {
-    int64_t q = 0;
-    for (int32_t k = m->indptr[i]; k < m->indptr[i + 1]; ++k, ++q) {
-      idx[i * K + q] = m->indices[k];
-      val[i * K + q] = make_float2((float)(m->data[2 * k] * scale),
-                                   (float)(m->data[2 * k + 1] * scale));
-    }
-    for (; q < K; ++q) {
-      idx[i * K + q] = (int32_t)i;
-      val[i * K + q] = make_float2(0.f, 0.f);
-    }
-  }
-  KPM_TRY(dev_alloc((void**)&out->ell_idx, idx.size() * sizeof(int32_t),
-                    h->stream));
-  KPM_TRY(dev_alloc((void**)&out->ell_val, val.size() * sizeof(float2),
-                    h->stream));
-  KPM_CUDA(cudaMemcpyAsync(out->ell_idx, idx.data(),
-                           idx.size() * sizeof(int32_t),
-                           cudaMemcpyHostToDevice, h->stream));
-  KPM_CUDA(cudaMemcpyAsync(out->ell_val, val.data(),
-                           val.size() * sizeof(float2),
-                           cudaMemcpyHostToDevice, h->stream));
-  KPM_CUDA(cudaStreamSynchronize(h->stream));
+  const size_t cnt = (size_t)m->rows * K;
+  KPM_TRY(dev_alloc((void**)&out->ell_idx, cnt * sizeof(int32_t), h->stream));
+  KPM_TRY(dev_alloc((void**)&out->ell_val, cnt * sizeof(float2), h->stream));
+  ell_from_csr_kernel<<<(unsigned)ceil_div(m->rows, 256), 256, 0,
+                        h->stream>>>(m->rows, (int)K, out->indptr, out->indices,
+                                     (const float2*)out->data, out->ell_idx,
+                                     out->ell_val);
+  count_launch(1);
+  KPM_CHECK_LAUNCH();
   out->ell_k = (int)K;
   return KPM_OK;
 }
@@ -933,11 +1021,11 @@ int kpm_create_ex(const kpm_csr_desc* ham, double a, double b, int precision,
   const double scale = h->precision == KPM_PREC_MIXED ? 2.0 / a : 0.0;
   if (flags & KPM_FLAG_REORDER) {
     st = validate_csr(ham);
-    std::vector<int32_t> ip, ix;
-    std::vector<double> data;
-    if (st == KPM_OK) st = setup_reorder(h, ham, ip, ix, data);
-    kpm_csr_desc pd{ham->rows, ham->nnz, ip.data(), ix.data(), data.data()};
-    if (st == KPM_OK) st = upload_matrix(h, &pd, scale, &h->H);
+    std::vector<int32_t> perm;
+    if (st == KPM_OK) st = setup_reorder(h, ham, perm);
+    if (st == KPM_OK)
+      st = upload_matrix_perm(h, ham, scale, &h->H, true, perm.data(),
+                              h->h_iperm.data(), false);
   } else {
     st = upload_matrix(h, ham, scale, &h->H);
   }

@@ -46,16 +46,20 @@ int validate_csr(const kpm_csr_desc* m);
 // stored as complex64 multiplied by scale.
 int upload_matrix(kpm_handle* h, const kpm_csr_desc* m, double scale,
                   Matrix* out, bool with_ell = true);
+// upload_matrix in a row order: new row p = old row perm[p] (host arrays
+// perm / iperm, or both null for the caller's order); the rows are moved
+// on the device.  validate false: m was validated by the caller.
+int upload_matrix_perm(kpm_handle* h, const kpm_csr_desc* m, double scale,
+                       Matrix* out, bool with_ell, const int32_t* perm,
+                       const int32_t* iperm, bool validate);
 void free_matrix(Matrix* m, cudaStream_t s);
 // upload_matrix in the handle's row order (reordered handles permute rows
 // and columns)
 int upload_matrix_for(kpm_handle* h, const kpm_csr_desc* m, double scale,
                       Matrix* out, bool with_ell = true);
-// compute the RCM order of m, set h->perm / h->h_iperm, and return the
-// permuted CSR arrays
+// compute the RCM order of m (perm[new] = old), set h->perm / h->h_iperm
 int setup_reorder(kpm_handle* h, const kpm_csr_desc* m,
-                  std::vector<int32_t>& ip, std::vector<int32_t>& ix,
-                  std::vector<double>& data);
+                  std::vector<int32_t>& perm);
 
 void free_family(kpm_handle* h);
 
@@ -67,8 +71,8 @@ int download_vectors(kpm_handle* h, const void* src, int64_t R, int64_t N,
 int launch_step(kpm_handle* h, int mode, bool dots, const StepArgs& a);
 // widest ELL row (entries) the complex64 ELL step kernel is built for
 constexpr int ELL_MAX = 16;
-int build_ell(kpm_handle* h, const kpm_csr_desc* m, double scale,
-              Matrix* out);
+// ELL copy of out's device CSR (complex64 values already in out)
+int build_ell(kpm_handle* h, const kpm_csr_desc* m, Matrix* out);
 int launch_step_ell(kpm_handle* h, int mode, bool dots, const StepArgs& a,
                     const StoreArgs* sa = nullptr);
 StepArgs step_args(kpm_block* b, const void* x, const void* prev, void* out);

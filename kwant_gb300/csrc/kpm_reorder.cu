@@ -8,9 +8,10 @@
 // keeps the neighbours of a row within a band of about the lattice width,
 // which a step's working window holds in L2.
 //
-// The permutation is applied on the device when vectors are uploaded or
-// downloaded; the entry order inside each row is kept, so every row sum is
-// evaluated in the caller's order.
+// Only the order itself is computed on the host.  The matrix rows are
+// moved and the vectors permuted on the device (at upload and download);
+// the entry order inside each row is kept, so every row sum is evaluated in
+// the caller's order.
 
 #include <algorithm>
 #include <numeric>
@@ -65,59 +66,23 @@ void rcm_order(int64_t n, const int32_t* indptr, const int32_t* indices,
   std::reverse(perm.begin(), perm.end());
 }
 
-// Row/column permutation of a CSR matrix; entry order within rows kept.
-void permute_csr(const kpm_csr_desc* m, const std::vector<int32_t>& perm,
-                 const std::vector<int32_t>& iperm, std::vector<int32_t>& ip,
-                 std::vector<int32_t>& ix, std::vector<double>& data) {
-  const int64_t n = m->rows;
-  ip.assign(n + 1, 0);
-  for (int64_t p = 0; p < n; ++p) {
-    const int32_t o = perm[p];
-    ip[p + 1] = ip[p] + (m->indptr[o + 1] - m->indptr[o]);
-  }
-  ix.resize(m->nnz);
-  data.resize(2 * m->nnz);
-  for (int64_t p = 0; p < n; ++p) {
-    const int32_t o = perm[p];
-    int32_t dst = ip[p];
-    for (int32_t k = m->indptr[o]; k < m->indptr[o + 1]; ++k, ++dst) {
-      ix[dst] = iperm[m->indices[k]];
-      data[2 * dst] = m->data[2 * k];
-      data[2 * dst + 1] = m->data[2 * k + 1];
-    }
-  }
-}
-
 int upload_matrix_for(kpm_handle* h, const kpm_csr_desc* m, double scale,
                       Matrix* out, bool with_ell) {
   if (!h->perm) return upload_matrix(h, m, scale, out, with_ell);
   KPM_REQUIRE(m->rows == (int64_t)h->h_iperm.size(),
               "matrix size does not match the handle");
-  // validate before permuting (the permutation indexes with the columns)
-  KPM_REQUIRE(m->indptr[0] == 0 && m->indptr[m->rows] == m->nnz,
-              "CSR indptr must start at 0 and end at nnz");
-  for (int64_t i = 0; i < m->rows; ++i)
-    KPM_REQUIRE(m->indptr[i] <= m->indptr[i + 1], "CSR indptr not monotone");
-  for (int64_t k = 0; k < m->nnz; ++k)
-    KPM_REQUIRE(m->indices[k] >= 0 && m->indices[k] < m->rows,
-                "CSR column index out of range");
+  KPM_TRY(validate_csr(m));
   std::vector<int32_t> perm(m->rows);
   for (int64_t o = 0; o < m->rows; ++o) perm[h->h_iperm[o]] = (int32_t)o;
-  std::vector<int32_t> ip, ix;
-  std::vector<double> data;
-  permute_csr(m, perm, h->h_iperm, ip, ix, data);
-  kpm_csr_desc pd{m->rows, m->nnz, ip.data(), ix.data(), data.data()};
-  return upload_matrix(h, &pd, scale, out, with_ell);
+  return upload_matrix_perm(h, m, scale, out, with_ell, perm.data(),
+                            h->h_iperm.data(), false);
 }
 
 int setup_reorder(kpm_handle* h, const kpm_csr_desc* m,
-                  std::vector<int32_t>& ip, std::vector<int32_t>& ix,
-                  std::vector<double>& data) {
-  std::vector<int32_t> perm;
+                  std::vector<int32_t>& perm) {
   rcm_order(m->rows, m->indptr, m->indices, perm);
   h->h_iperm.assign(m->rows, 0);
   for (int64_t p = 0; p < m->rows; ++p) h->h_iperm[perm[p]] = (int32_t)p;
-  permute_csr(m, perm, h->h_iperm, ip, ix, data);
   KPM_TRY(dev_alloc((void**)&h->perm, m->rows * sizeof(int32_t), h->stream));
   KPM_CUDA(cudaMemcpyAsync(h->perm, perm.data(), m->rows * sizeof(int32_t),
                            cudaMemcpyHostToDevice, h->stream));
