@@ -282,6 +282,18 @@ def _normalize_orbs_where(syst, where):
 _PHASE_POOL = None
 
 
+def _host_pool():
+    """Thread pool over the host's cores for numpy work that releases the
+    GIL (complex exp, large copies)."""
+    global _PHASE_POOL
+    if _PHASE_POOL is None:
+        import concurrent.futures
+        import os
+        _PHASE_POOL = concurrent.futures.ThreadPoolExecutor(
+            max_workers=max(1, min(32, os.cpu_count() or 1)))
+    return _PHASE_POOL
+
+
 def _phases(u):
     """exp(2j * pi * u) elementwise, bit-identical to numpy's expression
     (the same ufuncs on each element), computed in chunks on the host's
@@ -290,18 +302,28 @@ def _phases(u):
     chunk = 1 << 18
     if n < 4 * chunk:
         return np.exp(2j * np.pi * u)
-    global _PHASE_POOL
-    if _PHASE_POOL is None:
-        import concurrent.futures
-        import os
-        _PHASE_POOL = concurrent.futures.ThreadPoolExecutor(
-            max_workers=max(1, min(32, os.cpu_count() or 1)))
     out = np.empty(n, dtype=complex)
 
     def work(i):
         out[i:i + chunk] = np.exp(2j * np.pi * u[i:i + chunk])
 
-    list(_PHASE_POOL.map(work, range(0, n, chunk)))
+    list(_host_pool().map(work, range(0, n, chunk)))
+    return out
+
+
+def _stack_vectors(vectors):
+    """The vectors as the rows of one complex array (what np.array makes of
+    them), copied on the host's cores when they are large."""
+    vs = [np.asarray(v, complex) for v in vectors]
+    n = vs[0].shape[0] if vs and vs[0].ndim == 1 else -1
+    if n < (1 << 20) or any(v.ndim != 1 or v.shape[0] != n for v in vs):
+        return np.array(vs)
+    out = np.empty((len(vs), n), dtype=complex)
+
+    def work(i):
+        out[i] = vs[i]
+
+    list(_host_pool().map(work, range(len(vs))))
     return out
 
 
@@ -549,8 +571,8 @@ class SpectralDensity:
                                  "may be updated at a time.")
 
         if new_vectors:
-            vecs = np.array([np.asarray(self._vector_factory[r], complex)
-                             for r in range(have, num_vectors)])
+            vecs = _stack_vectors(self._vector_factory[r]
+                                  for r in range(have, num_vectors))
             if vecs.ndim != 2 or vecs.shape[1] != self._ham_csr.shape[0]:
                 raise ValueError('vectors must have the length of the '
                                  'Hamiltonian')
@@ -928,8 +950,8 @@ class Correlator:
                 + self._b)
 
     def _vectors(self):
-        return np.array([np.asarray(self._vector_factory[r], complex)
-                         for r in range(self._vector_factory.num_vectors)])
+        return _stack_vectors(self._vector_factory[r]
+                              for r in range(self._vector_factory.num_vectors))
 
     def _compute(self):
         vecs = self._vectors()
