@@ -53,24 +53,30 @@ template <> struct EllPay<1> {
 // input x) into the BF16x3 store row, 2 writes V alpha_n, with V's entries
 // in an ELL copy aligned with H's, so that V shares H's gathered rows; the
 // products follow the separate store kernel's operation order.
-template <int K, int MODE, bool DOTS, int RPI, int VPL, int SM = 0>
+template <int K, int MODE, bool DOTS, int RPI, int VPL, int SM = 0,
+          int SW = LANES>
 __global__ void __launch_bounds__(STEP_THREADS, ell_min_blocks<K, RPI>())
 cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
                      const float2* __restrict__ eval, StoreArgs sa) {
   static_assert(SM == 0 || (!DOTS && RPI == 1), "store fusion: no dots");
+  // SW lanes per slot: 16, or 8 for the store steps of 16-vector blocks
+  // (twice the rows in flight; the dot-product layout assumes 16)
+  static_assert(SW == LANES || (SW == 8 && !DOTS), "8-lane slots: no dots");
   using Pay = EllPay<VPL>;
   using PT = typename Pay::T;
-  constexpr int G = LANES * VPL;
+  constexpr int G = SW * VPL;
   constexpr int KQ = K / 4;
-  const int lane = threadIdx.x & (LANES - 1);
-  const int slot = threadIdx.x / LANES;
-  const int wq = slot >> 1, half = slot & 1, wl = threadIdx.x & 31;
+  constexpr int SPW = 32 / SW;                // slots per warp
+  constexpr int NSLOT = STEP_THREADS / SW;    // slots per block
+  const int lane = threadIdx.x & (SW - 1);
+  const int slot = threadIdx.x / SW;
+  const int wq = slot / SPW, half = slot % SPW, wl = threadIdx.x & 31;
   // FP64 accumulators of this slot's lanes, then the in-block reduction
-  __shared__ double red[DOTS ? SLOTS : 1][DOTS ? G * 3 : 1];
-  // ELL entries of each warp's next two rows (per row-per-iteration u),
+  __shared__ double red[DOTS ? NSLOT : 1][DOTS ? G * 3 : 1];
+  // ELL entries of each warp's next SPW rows (per row-per-iteration u),
   // double-buffered
-  __shared__ __align__(16) int32_t sidx[STEP_THREADS / 32][2][RPI][2 * K];
-  __shared__ __align__(16) float2 sval[STEP_THREADS / 32][2][RPI][2 * K];
+  __shared__ __align__(16) int32_t sidx[STEP_THREADS / 32][2][RPI][SPW * K];
+  __shared__ __align__(16) float2 sval[STEP_THREADS / 32][2][RPI][SPW * K];
 
   const PT* __restrict__ x = reinterpret_cast<const PT*>(p.x);
   const PT* prev = reinterpret_cast<const PT*>(p.prev);
@@ -78,14 +84,14 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
   const int work = p.xitems * p.groups;
   // row counters in 32 bits (CSR indices are int32); addresses in 64
   const int rows = (int)p.rows;
-  const int stride = p.xitems * SLOTS;
+  const int stride = p.xitems * NSLOT;
   const float shift = p.shift;
   constexpr int FLUSH = 32;
 
-  // Copy the entries of rows r0 + h + u * stride (h < 2, u < RPI) into
-  // stage buffer b: 16-byte chunks, two rows' indices then their values.
+  // Copy the entries of rows r0 + h + u * stride (h < SPW, u < RPI) into
+  // stage buffer b: 16-byte chunks, the rows' indices then their values.
   auto stage = [&](int r0, int b) {
-    constexpr int IC = K / 2, VC = K;
+    constexpr int IC = SPW * K / 4, VC = SPW * K / 2;
     for (int c = wl; c < RPI * (IC + VC); c += 32) {
       const int u = c / (IC + VC), d = c % (IC + VC);
       const int base = r0 + u * stride;
@@ -105,7 +111,7 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
   for (int w = blockIdx.x; w < work; w += gridDim.x) {
     const int xi = w / p.groups;
     const int g = w - xi * p.groups;
-    const int col = g * LANES + lane;
+    const int col = g * SW + lane;
     double* my = DOTS ? &red[slot][lane * VPL * 3] : nullptr;
     if constexpr (DOTS) {
 #pragma unroll
@@ -116,10 +122,10 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
     for (int k = 0; k < VPL; ++k) fn[k] = fr[k] = fi[k] = 0.f;
     int pending = 0;
 
-    // the warp's two slots walk adjacent rows; the entries of its next
-    // row pair are in flight while the current pair computes, so a row's
-    // gathers go out together with its own vector loads
-    const int wb0 = xi * SLOTS + 2 * wq;
+    // the warp's slots walk adjacent rows; the entries of its next rows
+    // are in flight while the current ones compute, so a row's gathers go
+    // out together with its own vector loads
+    const int wb0 = xi * NSLOT + SPW * wq;
     if (wb0 < rows) stage(wb0, 0);
     cp_async_commit();
     int sb = 0;
@@ -266,7 +272,7 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
       for (int e = threadIdx.x; e < G * 3; e += blockDim.x) {
         double s = 0.0;
 #pragma unroll
-        for (int q = 0; q < SLOTS; ++q) s += red[q][e];
+        for (int q = 0; q < NSLOT; ++q) s += red[q][e];
         dst[(int64_t)e * p.xitems] = s;
       }
       __syncthreads();
@@ -274,14 +280,15 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
   }
 }
 
-template <int K, int MODE, bool DOTS, int RPI, int VPL, int SM = 0>
+template <int K, int MODE, bool DOTS, int RPI, int VPL, int SM = 0,
+          int SW = LANES>
 static int launch_ell_t(kpm_handle* h, const StepArgs& a,
                         const StoreArgs& sa = StoreArgs{}) {
   static int occ = -1;
   if (occ < 0) {
     int blocks = 0;
     KPM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &blocks, cheb_step_ell_kernel<K, MODE, DOTS, RPI, VPL, SM>,
+        &blocks, cheb_step_ell_kernel<K, MODE, DOTS, RPI, VPL, SM, SW>,
         STEP_THREADS, 0));
     occ = blocks > 0 ? blocks : 1;
   }
@@ -300,7 +307,7 @@ static int launch_ell_t(kpm_handle* h, const StepArgs& a,
     h->prof_used += 2;
     KPM_CUDA(cudaEventRecord(e0, h->stream));
   }
-  cheb_step_ell_kernel<K, MODE, DOTS, RPI, VPL, SM>
+  cheb_step_ell_kernel<K, MODE, DOTS, RPI, VPL, SM, SW>
       <<<(unsigned)grid, STEP_THREADS, 0, h->stream>>>(a, h->H.ell_idx,
                                                         h->H.ell_val, sa);
   count_launch(1);
@@ -309,12 +316,25 @@ static int launch_ell_t(kpm_handle* h, const StepArgs& a,
   return KPM_OK;
 }
 
+// Store steps (no dot products).  Blocks of 16 vectors (one complex64
+// vector per lane in 16-lane slots) run as 8-lane slots of two vectors per
+// lane: the same 128 bytes per row, twice the rows in flight per warp, and
+// each vector's arithmetic unchanged.
 template <int K, int VPL, int SM>
 static int dispatch_store_mode(kpm_handle* h, int mode, const StepArgs& a,
                                const StoreArgs& sa) {
-  return mode == STEP_FIRST
-             ? launch_ell_t<K, STEP_FIRST, false, 1, VPL, SM>(h, a, sa)
-             : launch_ell_t<K, STEP_RECUR, false, 1, VPL, SM>(h, a, sa);
+  if constexpr (VPL == 1) {
+    StepArgs a2 = a;
+    a2.vpl = 2;
+    a2.rp = a.rp / 2;
+    return mode == STEP_FIRST
+               ? launch_ell_t<K, STEP_FIRST, false, 1, 2, SM, 8>(h, a2, sa)
+               : launch_ell_t<K, STEP_RECUR, false, 1, 2, SM, 8>(h, a2, sa);
+  } else {
+    return mode == STEP_FIRST
+               ? launch_ell_t<K, STEP_FIRST, false, 1, VPL, SM>(h, a, sa)
+               : launch_ell_t<K, STEP_RECUR, false, 1, VPL, SM>(h, a, sa);
+  }
 }
 
 template <int K, int VPL>
