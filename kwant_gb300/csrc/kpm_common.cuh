@@ -148,8 +148,6 @@ struct kpm_handle {
   // stages, 64-byte rows; measured 3.09 ms on the 200x200x2 / R=16 / M=256
   // workload) or 16 (four stages, 32-byte rows; 6.13 ms)
   int tc_kc = 32;
-  // rows per iteration of the ELL step kernel (1 or 2)
-  int step_rpi = 1;
   // optional locality reordering: device row p holds original row perm[p]
   int32_t* perm = nullptr;            // device, new -> old (null: identity)
   std::vector<int32_t> h_iperm;       // host, old -> new

@@ -1016,7 +1016,6 @@ int kpm_create_ex(const kpm_csr_desc* ham, double a, double b, int precision,
     return KPM_ECUDA;
   }
   h->own_stream = true;
-  if (const char* rpi = getenv("KPM_STEP_RPI")) h->step_rpi = atoi(rpi) == 2 ? 2 : 1;
   if (const char* kc = getenv("KPM_TC_KC")) h->tc_kc = atoi(kc) == 32 ? 32 : 16;
   const double scale = h->precision == KPM_PREC_MIXED ? 2.0 / a : 0.0;
   if (flags & KPM_FLAG_REORDER) {

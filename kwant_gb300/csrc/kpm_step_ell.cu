@@ -1,16 +1,21 @@
 // Complex64 Chebyshev step on an ELL copy of the Hamiltonian.
 //
-// Same arithmetic as the complex64 branch of cheb_step_kernel (kpm_core.cu),
-// entry for entry and in the same order (ELL padding adds 0 * x exactly, and
-// the FP32 -> FP64 flush points and the reduction order are unchanged), so
-// results are bit-identical; it differs only in how it feeds the memory
-// system.  The two slots of a warp walk adjacent rows; the column indices
-// and values of the warp's next row pair are copied into shared memory
-// with cp.async (16-byte chunks, no row-pointer load) while the current
-// pair computes, so a row's gathers go out together with its own vector
-// entry and its alpha_{n-1} entry: one dependent memory round trip per row
-// (a CSR row costs four).  The FP64 dot-product accumulators live in shared
-// memory to keep registers (and so occupancy) low.
+// Every row gets the products of the complex64 branch of cheb_step_kernel
+// (kpm_core.cu), entry for entry and in the same order (ELL padding adds
+// 0 * x exactly), so the Chebyshev vectors are bit-identical to it; the
+// fused DOS dot products are accumulated per 8-lane slot, which groups the
+// rows of each FP32 partial differently from the CSR kernel (a fixed order,
+// the same for every vector whatever its group size).
+//
+// A slot is 8 lanes with two (16-vector groups) or four (32-vector groups)
+// complex64 vectors per lane: 128 or 256 bytes per row, and four rows in
+// flight per warp.  The column indices and values of a warp's next four
+// rows are copied into shared memory with cp.async (16-byte chunks, no
+// row-pointer load) while the current ones compute, so a row's gathers go
+// out together with its own vector entry and its alpha_{n-1} entry: one
+// dependent memory round trip per row (a CSR row costs four).  The FP64
+// dot-product accumulators live in shared memory to keep registers (and so
+// occupancy) low.
 
 #include "kpm_common.cuh"
 #include "kpm_internal.cuh"
@@ -18,8 +23,9 @@
 namespace kpm {
 
 // Blocks per SM the register budget is sized for: 4 x 256 threads leaves
-// 64 registers per thread, which every variant fits without spilling (at 5
-// blocks, 48 registers, the fused-dots step spills and runs 1.6x slower).
+// 64 registers per thread, which the variants in use fit without spilling
+// (at 5 blocks, 48 registers, the fused-dots step spills and runs 1.6x
+// slower).
 #ifndef KPM_ELL_MIN_BLOCKS
 #define KPM_ELL_MIN_BLOCKS 4
 #endif
@@ -37,31 +43,39 @@ template <> struct EllPay<2> {
     return make_float4(r[0], i[0], r[1], i[1]);
   }
 };
-template <> struct EllPay<1> {
-  using T = float2;
-  __device__ static float re(const float2& v, int) { return v.x; }
-  __device__ static float im(const float2& v, int) { return v.y; }
-  __device__ static float2 make(const float (&r)[1], const float (&i)[1]) {
-    return make_float2(r[0], i[0]);
+struct alignas(32) F8 {
+  float4 a, b;
+};
+template <> struct EllPay<4> {
+  using T = F8;
+  __device__ static float re(const F8& v, int k) {
+    const float4& h = k < 2 ? v.a : v.b;
+    return (k & 1) ? h.z : h.x;
+  }
+  __device__ static float im(const F8& v, int k) {
+    const float4& h = k < 2 ? v.a : v.b;
+    return (k & 1) ? h.w : h.y;
+  }
+  __device__ static F8 make(const float (&r)[4], const float (&i)[4]) {
+    return F8{make_float4(r[0], i[0], r[1], i[1]),
+              make_float4(r[2], i[2], r[3], i[3])};
   }
 };
 
-// VPL complex64 vectors per lane: 2 (groups of 32 vectors) or 1 (groups of
-// 16, for blocks of at most 16 vectors); every vector gets the same FMA
-// sequence either way.
+// VPL complex64 vectors per lane of an SW-lane slot: 2 (groups of 16
+// vectors) or 4 (groups of 32); every vector gets the same FMA sequence
+// either way.
 // SM (store mode, the correlator's recursions): 1 also writes alpha_n (the
 // input x) into the BF16x3 store row, 2 writes V alpha_n, with V's entries
 // in an ELL copy aligned with H's, so that V shares H's gathered rows; the
 // products follow the separate store kernel's operation order.
 template <int K, int MODE, bool DOTS, int RPI, int VPL, int SM = 0,
-          int SW = LANES>
+          int SW = 8>
 __global__ void __launch_bounds__(STEP_THREADS, ell_min_blocks<K, RPI>())
 cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
                      const float2* __restrict__ eval, StoreArgs sa) {
   static_assert(SM == 0 || (!DOTS && RPI == 1), "store fusion: no dots");
-  // SW lanes per slot: 16, or 8 for the store steps of 16-vector blocks
-  // (twice the rows in flight; the dot-product layout assumes 16)
-  static_assert(SW == LANES || (SW == 8 && !DOTS), "8-lane slots: no dots");
+  static_assert(SW == 8 || SW == 16, "8- or 16-lane slots");
   using Pay = EllPay<VPL>;
   using PT = typename Pay::T;
   constexpr int G = SW * VPL;
@@ -281,7 +295,7 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
 }
 
 template <int K, int MODE, bool DOTS, int RPI, int VPL, int SM = 0,
-          int SW = LANES>
+          int SW = 8>
 static int launch_ell_t(kpm_handle* h, const StepArgs& a,
                         const StoreArgs& sa = StoreArgs{}) {
   static int occ = -1;
@@ -323,62 +337,49 @@ static int launch_ell_t(kpm_handle* h, const StepArgs& a,
 template <int K, int VPL, int SM>
 static int dispatch_store_mode(kpm_handle* h, int mode, const StepArgs& a,
                                const StoreArgs& sa) {
-  if constexpr (VPL == 1) {
-    StepArgs a2 = a;
-    a2.vpl = 2;
-    a2.rp = a.rp / 2;
-    return mode == STEP_FIRST
-               ? launch_ell_t<K, STEP_FIRST, false, 1, 2, SM, 8>(h, a2, sa)
-               : launch_ell_t<K, STEP_RECUR, false, 1, 2, SM, 8>(h, a2, sa);
-  } else {
-    return mode == STEP_FIRST
-               ? launch_ell_t<K, STEP_FIRST, false, 1, VPL, SM>(h, a, sa)
-               : launch_ell_t<K, STEP_RECUR, false, 1, VPL, SM>(h, a, sa);
-  }
+  return mode == STEP_FIRST
+             ? launch_ell_t<K, STEP_FIRST, false, 1, VPL, SM>(h, a, sa)
+             : launch_ell_t<K, STEP_RECUR, false, 1, VPL, SM>(h, a, sa);
 }
 
 template <int K, int VPL>
-static int dispatch_store(kpm_handle* h, int mode, const StepArgs& a,
-                          const StoreArgs& sa) {
-  return sa.smode == 2 ? dispatch_store_mode<K, VPL, 2>(h, mode, a, sa)
-                       : dispatch_store_mode<K, VPL, 1>(h, mode, a, sa);
-}
-
-template <int K, int RPI, int VPL>
 static int dispatch_mode(kpm_handle* h, int mode, bool dots,
                          const StepArgs& a, const StoreArgs* sa) {
-  if constexpr (RPI == 1)
-    if (sa && sa->smode) return dispatch_store<K, VPL>(h, mode, a, *sa);
+  if (sa && sa->smode)
+    return sa->smode == 2 ? dispatch_store_mode<K, VPL, 2>(h, mode, a, *sa)
+                          : dispatch_store_mode<K, VPL, 1>(h, mode, a, *sa);
   if (mode == STEP_FIRST)
-    return dots ? launch_ell_t<K, STEP_FIRST, true, RPI, VPL>(h, a)
-                : launch_ell_t<K, STEP_FIRST, false, RPI, VPL>(h, a);
-  return dots ? launch_ell_t<K, STEP_RECUR, true, RPI, VPL>(h, a)
-              : launch_ell_t<K, STEP_RECUR, false, RPI, VPL>(h, a);
+    return dots ? launch_ell_t<K, STEP_FIRST, true, 1, VPL>(h, a)
+                : launch_ell_t<K, STEP_FIRST, false, 1, VPL>(h, a);
+  return dots ? launch_ell_t<K, STEP_RECUR, true, 1, VPL>(h, a)
+              : launch_ell_t<K, STEP_RECUR, false, 1, VPL>(h, a);
 }
 
-template <int RPI, int VPL>
+template <int VPL>
 static int dispatch_k(kpm_handle* h, int mode, bool dots, const StepArgs& a,
                       const StoreArgs* sa) {
   switch (h->H.ell_k) {
-    case 4: return dispatch_mode<4, RPI, VPL>(h, mode, dots, a, sa);
-    case 8: return dispatch_mode<8, RPI, VPL>(h, mode, dots, a, sa);
-    case 12: return dispatch_mode<12, RPI, VPL>(h, mode, dots, a, sa);
-    case 16: return dispatch_mode<16, RPI, VPL>(h, mode, dots, a, sa);
+    case 4: return dispatch_mode<4, VPL>(h, mode, dots, a, sa);
+    case 8: return dispatch_mode<8, VPL>(h, mode, dots, a, sa);
+    case 12: return dispatch_mode<12, VPL>(h, mode, dots, a, sa);
+    case 16: return dispatch_mode<16, VPL>(h, mode, dots, a, sa);
   }
   set_error("ELL width %d not supported", h->H.ell_k);
   return KPM_EUNSUPPORTED;
 }
 
+// The block layout holds one (16-vector groups) or two (32-vector groups)
+// complex64 vectors per 16-byte lane of a 16-lane row; the ELL step runs
+// both as 8-lane slots with twice as many vectors per lane: the same bytes
+// per row, twice the rows in flight per warp, and the same slot of every
+// row and the same flush points for every vector whatever its group size.
 int launch_step_ell(kpm_handle* h, int mode, bool dots, const StepArgs& a,
                     const StoreArgs* sa) {
-  const bool store = sa && sa->smode;
-  if (a.vpl == 1)
-    return h->step_rpi == 2 && !store
-               ? dispatch_k<2, 1>(h, mode, dots, a, nullptr)
-               : dispatch_k<1, 1>(h, mode, dots, a, sa);
-  if (h->step_rpi == 2 && !store)
-    return dispatch_k<2, 2>(h, mode, dots, a, nullptr);
-  return dispatch_k<1, 2>(h, mode, dots, a, sa);
+  StepArgs w = a;
+  w.vpl = 2 * a.vpl;
+  w.rp = a.rp / 2;
+  return a.vpl == 1 ? dispatch_k<2>(h, mode, dots, w, sa)
+                    : dispatch_k<4>(h, mode, dots, w, sa);
 }
 
 }  // namespace kpm

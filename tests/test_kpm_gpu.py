@@ -78,6 +78,22 @@ def test_rmt_add_vectors_bit_identical(kpm):
     assert _rel(np.array(sd._moments_list), g['vec_moments_list']) < TOL
 
 
+def test_mixed_add_vectors_bit_identical_across_group_sizes(kpm):
+    """Mixed precision: 10 vectors (a 16-vector block) plus 30 more (a
+    32-vector block) give the same moments, bit for bit, as 40 vectors at
+    once (two 32-vector groups): every vector sees the same row partition,
+    slot and flush points whatever its block's group size."""
+    g = load('square100')
+    ham = csr(g)
+    sd = _sd(kpm, ham, g, num_moments=40, num_vectors=10, precision='mixed')
+    sd.add_vectors(30)
+    fresh = _sd(kpm, ham, g, num_moments=40, num_vectors=40,
+                precision='mixed')
+    assert np.array_equal(np.array(sd._moments_list),
+                          np.array(fresh._moments_list))
+    assert np.array_equal(sd.densities, fresh.densities)
+
+
 def test_rmt_operator_identity_matrix(kpm):
     g = load('rmt20')
     sd = _sd(kpm, g['ham'], g, num_moments=200, num_vectors=5,

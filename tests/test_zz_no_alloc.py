@@ -6,8 +6,12 @@ The test plays such a caller: it allocates every buffer itself (with torch)
 and passes device pointers through the C ABI; the result must match the
 regular, allocating entry point (kpm_block_dos_moments) within the FP64
 parity tolerance of the other tests, on two calls in a row (the second call
-runs over the scratch the first one left behind).  This file is collected
-last so that a failure here does not stop the rest of the GPU suite.
+runs over the scratch the first one left behind).  In mixed precision the
+two entry points compute the same Chebyshev vectors with different step
+kernels (CSR here, ELL there) whose FP32 dot-product partials group the
+rows differently, so they agree to FP32 partial-sum rounding (1e-8).  This
+file is collected last so that a failure here does not stop the rest of
+the GPU suite.
 """
 
 import ctypes as C
@@ -19,7 +23,7 @@ from golden_io import load, csr, ref_vectors
 
 pytestmark = pytest.mark.gpu
 
-TOL = 1e-12
+TOL = {'fp64': 1e-12, 'mixed': 1e-8}
 
 
 class DeviceCsr(C.Structure):
@@ -85,7 +89,7 @@ def test_noalloc_matches_allocating_entry_point(precision):
         got = moments.cpu().numpy().view(np.complex128).reshape(M, Rpad)
         got = got[:, :R].T
         err = np.max(np.abs(got - expected)) / np.max(np.abs(expected))
-        assert err < TOL, (call, err)
+        assert err < TOL[precision], (call, err)
 
 
 def test_noalloc_rejects_oversized_requests():
