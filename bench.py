@@ -300,12 +300,12 @@ def run_ours(args):
     avg_step_ms = step_ms / max(n_step, 1)
     achieved = B / (avg_step_ms / 1e3) / 1e9
     # DRAM bytes per step launch: ncu dram__bytes_read + dram__bytes_write
-    # of one cheb_step_ell launch on the 500 x 500-cell, R = 64 case (796.7
+    # of one cheb_step_ell launch on the 500 x 500-cell, R = 64 case (774.5
     # MB against 794.0 MB algorithmic; the workload here is too large for a
     # multi-pass capture), scaled to this launch by its algorithmic bytes
     traffic = None
     if args.precision == 'mixed' and args.reorder and R == 64:
-        traffic = B * (796.7 / 794.0)
+        traffic = B * (774.5 / 794.0)
 
     # ---- accuracy vs the FP64 path (untimed) -------------------------------
     accuracy = None
