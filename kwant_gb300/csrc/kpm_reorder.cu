@@ -36,31 +36,35 @@ void rcm_order(int64_t n, const int32_t* indptr, const int32_t* indices,
   std::vector<int32_t> by_deg(n);
   for (int64_t i = 0; i < n; ++i) by_deg[cnt[deg[i]]++] = (int32_t)i;
 
+  // breadth-first from each component's lowest-degree node; the unseen
+  // neighbours of a node are appended in (degree, index) order, sorted in
+  // place by insertion (rows are short)
   std::vector<char> seen(n, 0);
-  perm.clear();
-  perm.reserve(n);
-  std::vector<int32_t> nb;
-  int64_t seed_pos = 0;
-  while ((int64_t)perm.size() < n) {
+  perm.assign(n, 0);
+  auto before = [&](int32_t p, int32_t q) {
+    return deg[p] < deg[q] || (deg[p] == deg[q] && p < q);
+  };
+  int64_t tail = 0, seed_pos = 0;
+  while (tail < n) {
     while (seen[by_deg[seed_pos]]) ++seed_pos;
     const int32_t seed = by_deg[seed_pos];
-    size_t head = perm.size();
-    perm.push_back(seed);
+    int64_t head = tail;
+    perm[tail++] = seed;
     seen[seed] = 1;
-    while (head < perm.size()) {
+    while (head < tail) {
       const int32_t u = perm[head++];
-      nb.clear();
+      const int64_t first = tail;
       for (int32_t k = indptr[u]; k < indptr[u + 1]; ++k) {
         const int32_t v = indices[k];
-        if (!seen[v]) {
-          seen[v] = 1;
-          nb.push_back(v);
+        if (seen[v]) continue;
+        seen[v] = 1;
+        int64_t j = tail++;
+        while (j > first && before(v, perm[j - 1])) {
+          perm[j] = perm[j - 1];
+          --j;
         }
+        perm[j] = v;
       }
-      std::sort(nb.begin(), nb.end(), [&](int32_t p, int32_t q) {
-        return deg[p] < deg[q] || (deg[p] == deg[q] && p < q);
-      });
-      perm.insert(perm.end(), nb.begin(), nb.end());
     }
   }
   std::reverse(perm.begin(), perm.end());
