@@ -29,7 +29,10 @@ namespace kpm {
 #ifndef KPM_ELL_MIN_BLOCKS
 #define KPM_ELL_MIN_BLOCKS 4
 #endif
-constexpr int ell_min_blocks() { return KPM_ELL_MIN_BLOCKS; }
+template <int K, int RPI>
+constexpr int ell_min_blocks() {
+  return RPI != 1 ? 1 : KPM_ELL_MIN_BLOCKS;
+}
 
 template <int VPL> struct EllPay;
 template <> struct EllPay<2> {
@@ -66,11 +69,16 @@ template <> struct EllPay<4> {
 // input x) into the BF16x3 store row, 2 writes V alpha_n, with V's entries
 // in an ELL copy aligned with H's, so that V shares H's gathered rows; the
 // products follow the separate store kernel's operation order.
-template <int K, int MODE, bool DOTS, int VPL, int SM = 0, int SW = 8>
-__global__ void __launch_bounds__(STEP_THREADS, ell_min_blocks())
+// RPI (rows per slot iteration) is 1 in every launch.  The per-row arrays
+// stay: rewriting them as scalars changed the compiler's load schedule and
+// made the fused-dots step 25 % slower (0.563 -> 0.702 ms on the 2e6-orbital
+// graphene workload) at the same register count.
+template <int K, int MODE, bool DOTS, int RPI, int VPL, int SM = 0,
+          int SW = 8>
+__global__ void __launch_bounds__(STEP_THREADS, ell_min_blocks<K, RPI>())
 cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
                      const float2* __restrict__ eval, StoreArgs sa) {
-  static_assert(SM == 0 || !DOTS, "store fusion: no dots");
+  static_assert(SM == 0 || (!DOTS && RPI == 1), "store fusion: no dots");
   static_assert(SW == 8 || SW == 16, "8- or 16-lane slots");
   using Pay = EllPay<VPL>;
   using PT = typename Pay::T;
@@ -85,8 +93,8 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
   __shared__ double red[DOTS ? NSLOT : 1][DOTS ? G * 3 : 1];
   // ELL entries of each warp's next SPW rows (per row-per-iteration u),
   // double-buffered
-  __shared__ __align__(16) int32_t sidx[STEP_THREADS / 32][2][SPW * K];
-  __shared__ __align__(16) float2 sval[STEP_THREADS / 32][2][SPW * K];
+  __shared__ __align__(16) int32_t sidx[STEP_THREADS / 32][2][RPI][SPW * K];
+  __shared__ __align__(16) float2 sval[STEP_THREADS / 32][2][RPI][SPW * K];
 
   const PT* __restrict__ x = reinterpret_cast<const PT*>(p.x);
   const PT* prev = reinterpret_cast<const PT*>(p.prev);
@@ -98,20 +106,21 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
   const float shift = p.shift;
   constexpr int FLUSH = 32;
 
-  // Copy the entries of rows r0 + h (h < SPW) into
+  // Copy the entries of rows r0 + h + u * stride (h < SPW, u < RPI) into
   // stage buffer b: 16-byte chunks, the rows' indices then their values.
   auto stage = [&](int r0, int b) {
     constexpr int IC = SPW * K / 4, VC = SPW * K / 2;
-    for (int d = wl; d < IC + VC; d += 32) {
-      const int base = r0;
+    for (int c = wl; c < RPI * (IC + VC); c += 32) {
+      const int u = c / (IC + VC), d = c % (IC + VC);
+      const int base = r0 + u * stride;
       if (d < IC) {
         if (base + (4 * d) / K < rows)
-          cp_async16(&sidx[wq][b][4 * d],
+          cp_async16(&sidx[wq][b][u][4 * d],
                      eidx + (int64_t)base * K + 4 * d);
       } else {
         const int e = d - IC;
         if (base + (2 * e) / K < rows)
-          cp_async16(&sval[wq][b][2 * e],
+          cp_async16(&sval[wq][b][u][2 * e],
                      eval + (int64_t)base * K + 2 * e);
       }
     }
@@ -138,52 +147,62 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
     if (wb0 < rows) stage(wb0, 0);
     cp_async_commit();
     int sb = 0;
-    for (int wb = wb0; wb < rows; wb += stride) {
-      if (wb + stride < rows) stage(wb + stride, sb ^ 1);
+    for (int wb = wb0; wb < rows; wb += RPI * stride) {
+      if (wb + RPI * stride < rows) stage(wb + RPI * stride, sb ^ 1);
       cp_async_commit();
       cp_async_wait_prev();
       __syncwarp();
-      const int64_t row = wb + half;
-      const bool ok = row < rows;
-      PT xv, pv;
-      int4 c4[KQ];
-      float4 hv[2 * KQ];
-      if (ok) {
-        const int64_t r = row;
-        xv = x[r * p.rp + col];
-        if constexpr (MODE == STEP_RECUR) pv = prev[r * p.rp + col];
-        const int4* ri = reinterpret_cast<const int4*>(&sidx[wq][sb][half * K]);
+      const int i0 = wb + half;
+      int64_t row[RPI];
+      bool ok[RPI];
+#pragma unroll
+      for (int u = 0; u < RPI; ++u) {
+        row[u] = i0 + u * stride;
+        ok[u] = row[u] < rows;
+      }
+      PT xv[RPI], pv[RPI];
+      int4 c4[RPI][KQ];
+      float4 hv[RPI][2 * KQ];
+#pragma unroll
+      for (int u = 0; u < RPI; ++u) {
+        if (!ok[u]) continue;
+        const int64_t r = row[u];
+        xv[u] = x[r * p.rp + col];
+        if constexpr (MODE == STEP_RECUR) pv[u] = prev[r * p.rp + col];
+        const int4* ri = reinterpret_cast<const int4*>(&sidx[wq][sb][u][half * K]);
         const float4* rv =
-            reinterpret_cast<const float4*>(&sval[wq][sb][half * K]);
+            reinterpret_cast<const float4*>(&sval[wq][sb][u][half * K]);
 #pragma unroll
         for (int q = 0; q < KQ; ++q) {
-          c4[q] = ri[q];
-          hv[2 * q] = rv[2 * q];
-          hv[2 * q + 1] = rv[2 * q + 1];
+          c4[u][q] = ri[q];
+          hv[u][2 * q] = rv[2 * q];
+          hv[u][2 * q + 1] = rv[2 * q + 1];
         }
       }
-      if (ok) {
+#pragma unroll
+      for (int u = 0; u < RPI; ++u) {
+        if (!ok[u]) continue;
         float ar[VPL], ai[VPL];
         float sr[VPL], si[VPL];        // store values (SM == 2: V alpha_n)
 #pragma unroll
         for (int k = 0; k < VPL; ++k) {
-          ar[k] = shift * Pay::re(xv, k);
-          ai[k] = shift * Pay::im(xv, k);
+          ar[k] = shift * Pay::re(xv[u], k);
+          ai[k] = shift * Pay::im(xv[u], k);
           sr[k] = si[k] = 0.f;
         }
         const float4* vv = SM == 2
-            ? reinterpret_cast<const float4*>(sa.vell + (int64_t)row * K)
+            ? reinterpret_cast<const float4*>(sa.vell + (int64_t)row[u] * K)
             : nullptr;
 #pragma unroll
         for (int q = 0; q < KQ; ++q) {
-          const int cc[4] = {c4[q].x, c4[q].y, c4[q].z, c4[q].w};
+          const int cc[4] = {c4[u][q].x, c4[u][q].y, c4[u][q].z, c4[u][q].w};
           PT xx[4];
 #pragma unroll
           for (int t = 0; t < 4; ++t) xx[t] = x[(int64_t)cc[t] * p.rp + col];
-          const float hr[4] = {hv[2 * q].x, hv[2 * q].z,
-                               hv[2 * q + 1].x, hv[2 * q + 1].z};
-          const float hi[4] = {hv[2 * q].y, hv[2 * q].w,
-                               hv[2 * q + 1].y, hv[2 * q + 1].w};
+          const float hr[4] = {hv[u][2 * q].x, hv[u][2 * q].z,
+                               hv[u][2 * q + 1].x, hv[u][2 * q + 1].z};
+          const float hi[4] = {hv[u][2 * q].y, hv[u][2 * q].w,
+                               hv[u][2 * q + 1].y, hv[u][2 * q + 1].w};
 #pragma unroll
           for (int t = 0; t < 4; ++t) {
 #pragma unroll
@@ -215,9 +234,9 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
           for (int k = 0; k < VPL; ++k) {
             const int64_t vec = (int64_t)g * G + (int64_t)lane * VPL + k;
             if (vec < sa.R) {
-              const float re = SM == 2 ? sr[k] : Pay::re(xv, k);
-              const float im = SM == 2 ? si[k] : Pay::im(xv, k);
-              store_put<STORE_BF16X3>(sa.store, (int64_t)row * sa.R + vec,
+              const float re = SM == 2 ? sr[k] : Pay::re(xv[u], k);
+              const float im = SM == 2 ? si[k] : Pay::im(xv[u], k);
+              store_put<STORE_BF16X3>(sa.store, (int64_t)row[u] * sa.R + vec,
                                       re, im);
             }
           }
@@ -229,15 +248,15 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
             orr[k] = 0.5f * ar[k];
             oii[k] = 0.5f * ai[k];
           } else {
-            orr[k] = ar[k] - Pay::re(pv, k);
-            oii[k] = ai[k] - Pay::im(pv, k);
+            orr[k] = ar[k] - Pay::re(pv[u], k);
+            oii[k] = ai[k] - Pay::im(pv[u], k);
           }
         }
-        out[(int64_t)row * p.rp + col] = Pay::make(orr, oii);
+        out[(int64_t)row[u] * p.rp + col] = Pay::make(orr, oii);
         if constexpr (DOTS) {
 #pragma unroll
           for (int k = 0; k < VPL; ++k) {
-            const float vr = Pay::re(xv, k), vi = Pay::im(xv, k);
+            const float vr = Pay::re(xv[u], k), vi = Pay::im(xv[u], k);
             fn[k] = fmaf(vr, vr, fmaf(vi, vi, fn[k]));
             fr[k] = fmaf(orr[k], vr, fmaf(oii[k], vi, fr[k]));
             fi[k] = fmaf(orr[k], vi, fmaf(-oii[k], vr, fi[k]));
@@ -279,14 +298,15 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
   }
 }
 
-template <int K, int MODE, bool DOTS, int VPL, int SM = 0, int SW = 8>
+template <int K, int MODE, bool DOTS, int RPI, int VPL, int SM = 0,
+          int SW = 8>
 static int launch_ell_t(kpm_handle* h, const StepArgs& a,
                         const StoreArgs& sa = StoreArgs{}) {
   static int occ = -1;
   if (occ < 0) {
     int blocks = 0;
     KPM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &blocks, cheb_step_ell_kernel<K, MODE, DOTS, VPL, SM, SW>,
+        &blocks, cheb_step_ell_kernel<K, MODE, DOTS, RPI, VPL, SM, SW>,
         STEP_THREADS, 0));
     occ = blocks > 0 ? blocks : 1;
   }
@@ -305,7 +325,7 @@ static int launch_ell_t(kpm_handle* h, const StepArgs& a,
     h->prof_used += 2;
     KPM_CUDA(cudaEventRecord(e0, h->stream));
   }
-  cheb_step_ell_kernel<K, MODE, DOTS, VPL, SM, SW>
+  cheb_step_ell_kernel<K, MODE, DOTS, RPI, VPL, SM, SW>
       <<<(unsigned)grid, STEP_THREADS, 0, h->stream>>>(a, h->H.ell_idx,
                                                         h->H.ell_val, sa);
   count_launch(1);
@@ -322,8 +342,8 @@ template <int K, int VPL, int SM>
 static int dispatch_store_mode(kpm_handle* h, int mode, const StepArgs& a,
                                const StoreArgs& sa) {
   return mode == STEP_FIRST
-             ? launch_ell_t<K, STEP_FIRST, false, VPL, SM>(h, a, sa)
-             : launch_ell_t<K, STEP_RECUR, false, VPL, SM>(h, a, sa);
+             ? launch_ell_t<K, STEP_FIRST, false, 1, VPL, SM>(h, a, sa)
+             : launch_ell_t<K, STEP_RECUR, false, 1, VPL, SM>(h, a, sa);
 }
 
 template <int K, int VPL>
@@ -333,10 +353,10 @@ static int dispatch_mode(kpm_handle* h, int mode, bool dots,
     return sa->smode == 2 ? dispatch_store_mode<K, VPL, 2>(h, mode, a, *sa)
                           : dispatch_store_mode<K, VPL, 1>(h, mode, a, *sa);
   if (mode == STEP_FIRST)
-    return dots ? launch_ell_t<K, STEP_FIRST, true, VPL>(h, a)
-                : launch_ell_t<K, STEP_FIRST, false, VPL>(h, a);
-  return dots ? launch_ell_t<K, STEP_RECUR, true, VPL>(h, a)
-              : launch_ell_t<K, STEP_RECUR, false, VPL>(h, a);
+    return dots ? launch_ell_t<K, STEP_FIRST, true, 1, VPL>(h, a)
+                : launch_ell_t<K, STEP_FIRST, false, 1, VPL>(h, a);
+  return dots ? launch_ell_t<K, STEP_RECUR, true, 1, VPL>(h, a)
+              : launch_ell_t<K, STEP_RECUR, false, 1, VPL>(h, a);
 }
 
 template <int VPL>
