@@ -212,12 +212,36 @@ def run_reference(args):
         'config': {'workload': _workload_name(args), 'nnz': int(ham.nnz),
                    'R': procs, 'M': args.ref_moments},
         'cpu_baseline': {'value': value, 'unit': UNIT, 'cores': procs,
-                         'kind': 'port', 'sample': sample},
+                         'kind': 'port', 'sample': sample,
+                         'cpu': _cpu_model()},
         'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0,
                 'd2h_bytes_per_step': 0},
     }
     print(json.dumps(line))
     return 0
+
+
+def _cpu_model():
+    """The host CPU's model name (from /proc/cpuinfo; Arm cores report no
+    model name, then the implementer / part codes), and the machine type."""
+    import platform
+    name, impl, part = None, None, None
+    try:
+        with open('/proc/cpuinfo') as f:
+            for line in f:
+                k, _, v = line.partition(':')
+                k, v = k.strip(), v.strip()
+                if k == 'model name' and name is None:
+                    name = v
+                elif k == 'CPU implementer' and impl is None:
+                    impl = v
+                elif k == 'CPU part' and part is None:
+                    part = v
+    except OSError:
+        pass
+    if name is None and impl is not None:
+        name = 'implementer %s part %s' % (impl, part)
+    return '%s (%s)' % (name or 'unknown', platform.machine())
 
 
 def _workload_name(args):
@@ -413,8 +437,10 @@ def run_ours(args):
             base.close()
         cpu = {'value': v, 'unit': UNIT, 'cores': procs, 'kind': 'port',
                'sample': '%d vectors x %d moments of the same workload, one '
-                         'spawned process per vector (%.1f s)'
-                         % (procs, args.ref_moments, dt)}
+                         'spawned process per vector (%.1f s; scipy\'s CSR '
+                         'matvec is single-threaded)'
+                         % (procs, args.ref_moments, dt),
+               'cpu': _cpu_model()}
 
     if rank == 0:
         line = {
