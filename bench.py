@@ -240,7 +240,10 @@ def _cpu_model():
     except OSError:
         pass
     if name is None and impl is not None:
-        name = 'implementer %s part %s' % (impl, part)
+        arm = {'0xd0c': 'Neoverse-N1', '0xd40': 'Neoverse-V1',
+               '0xd49': 'Neoverse-N2', '0xd4f': 'Neoverse-V2'}
+        name = ('Arm ' + arm[part] if impl == '0x41' and part in arm
+                else 'implementer %s part %s' % (impl, part))
     return '%s (%s)' % (name or 'unknown', platform.machine())
 
 
