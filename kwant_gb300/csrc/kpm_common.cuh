@@ -135,9 +135,15 @@ struct kpm_handle {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   kpm::Matrix H;
-  // dot-product partials: [groups][xitems][group][3] doubles
+  // dot-product partials: [group][vector*3 + component][xitems] doubles
   double* partials = nullptr;
   size_t partials_cap = 0;
+  // host vectors already copied to the device ([R][N] complex128, in flight
+  // on the handle's stream order): the next upload of exactly that host
+  // array uses and frees it instead of copying again
+  void* vec_staging = nullptr;
+  const void* vec_staging_src = nullptr;
+  size_t vec_staging_bytes = 0;
   int resident_step_blocks = 0;
   cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
   bool timed = false;

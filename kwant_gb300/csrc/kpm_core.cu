@@ -361,9 +361,18 @@ int upload_vectors(kpm_handle* h, const double* host, int64_t R, int64_t N,
                    int64_t Rpad, void* dst) {
   void* staging = nullptr;
   size_t bytes = (size_t)R * N * 16;
-  KPM_TRY(dev_alloc(&staging, bytes, h->stream));
-  cudaError_t e = cudaMemcpyAsync(staging, host, bytes,
-                                  cudaMemcpyHostToDevice, h->stream);
+  cudaError_t e = cudaSuccess;
+  if (h->vec_staging && h->vec_staging_src == host &&
+      h->vec_staging_bytes == bytes) {
+    staging = h->vec_staging;          // copied ahead of time
+    h->vec_staging = nullptr;
+    h->vec_staging_src = nullptr;
+    h->vec_staging_bytes = 0;
+  } else {
+    KPM_TRY(dev_alloc(&staging, bytes, h->stream));
+    e = cudaMemcpyAsync(staging, host, bytes, cudaMemcpyHostToDevice,
+                        h->stream);
+  }
   if (e != cudaSuccess) {
     dev_free(staging, h->stream);
     KPM_CUDA(e);
@@ -1061,6 +1070,7 @@ int kpm_destroy(kpm_handle* h) {
   if (!h) return KPM_OK;
   free_matrix(&h->H, h->stream);
   free_family(h);
+  dev_free(h->vec_staging, h->stream);
   dev_free(h->partials, h->stream);
   dev_free(h->perm, h->stream);
   if (h->ev_start) cudaEventDestroy(h->ev_start);

@@ -421,11 +421,42 @@ int kpm_dos(const kpm_csr_desc* ham, double a, double b, int precision,
             const double* vecs, int64_t R, int64_t M, int kernel,
             double* moments_out, double* gammas_out, double* densities_out) {
   KPM_REQUIRE(ham && vecs && R > 0 && M >= 2, "kpm_dos: invalid argument");
+  KPM_REQUIRE(ham->rows > 0, "kpm_dos: invalid CSR descriptor");
+  // Copy the vectors to the device on a stream of their own first, so that
+  // the copy overlaps the handle set-up (the RCM order is computed on the
+  // host); the handle's stream waits for it before the block uses it.
+  const size_t vbytes = (size_t)R * ham->rows * 16;
+  cudaStream_t vs = nullptr;
+  cudaEvent_t vdone = nullptr;
+  void* vstage = nullptr;
+  if (cudaStreamCreateWithFlags(&vs, cudaStreamNonBlocking) == cudaSuccess &&
+      cudaEventCreateWithFlags(&vdone, cudaEventDisableTiming) ==
+          cudaSuccess &&
+      cudaMallocAsync(&vstage, vbytes, vs) == cudaSuccess &&
+      cudaMemcpyAsync(vstage, vecs, vbytes, cudaMemcpyHostToDevice, vs) ==
+          cudaSuccess &&
+      cudaEventRecord(vdone, vs) == cudaSuccess) {
+  } else {
+    cudaGetLastError();
+    if (vstage) cudaFreeAsync(vstage, vs);
+    vstage = nullptr;                   // the block copies them itself
+  }
   kpm_handle* h = nullptr;
   // the mixed-precision one-shot path stores the Hamiltonian in RCM order
-  KPM_TRY(kpm_create_ex(ham, a, b, precision,
-                        precision == KPM_PREC_MIXED ? KPM_FLAG_REORDER : 0,
-                        &h));
+  int cst = kpm_create_ex(ham, a, b, precision,
+                          precision == KPM_PREC_MIXED ? KPM_FLAG_REORDER : 0,
+                          &h);
+  if (cst == KPM_OK && vstage &&
+      cudaStreamWaitEvent(h->stream, vdone, 0) == cudaSuccess) {
+    h->vec_staging = vstage;            // freed by the upload or the handle
+    h->vec_staging_src = vecs;
+    h->vec_staging_bytes = vbytes;
+    vstage = nullptr;
+  }
+  if (vstage) cudaFreeAsync(vstage, vs);
+  if (vdone) cudaEventDestroy(vdone);
+  if (vs) cudaStreamDestroy(vs);
+  if (cst != KPM_OK) return cst;
   kpm_block* blk = nullptr;
   int st = kpm_block_create(h, vecs, R, 0, &blk);
   double* mom = nullptr;

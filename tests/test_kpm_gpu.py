@@ -78,6 +78,29 @@ def test_rmt_add_vectors_bit_identical(kpm):
     assert _rel(np.array(sd._moments_list), g['vec_moments_list']) < TOL
 
 
+@pytest.mark.parametrize('precision', ['fp64', 'mixed'])
+def test_one_shot_dos_c_abi_matches_oracle(kpm, precision):
+    """kpm_dos, the one-shot C entry point (handle with the RCM order in
+    mixed precision, vector upload overlapped with the handle set-up,
+    recursion, device reconstruction, download), against the oracle's whole
+    SpectralDensity pipeline on the same vectors and bounds."""
+    from kwant_gb300 import _lib
+    g = load('square100')
+    ham = csr(g)
+    n = ham.shape[0]
+    R, M = 6, 60
+    _, vecs = ref_vectors(g['seed'], n, R)
+    ref = ko.spectral_density(ham, vecs, g['lmin'], g['lmax'], M)
+    a, b = ref['a'], ref['b']
+    prec = _lib.PREC_MIXED if precision == 'mixed' else _lib.PREC_FP64
+    for _ in range(2):      # a second call runs on a fresh handle
+        mom, gam, rho = _lib.dos(ham, a, b, prec, vecs, M)
+        tol = 1e-12 if precision == 'fp64' else 1e-5
+        assert _rel(mom, ref['moments_list']) < tol
+        assert _rel(rho.real, ref['densities']) < tol
+        assert _rel(gam.real, ref['gammas']) < tol
+
+
 def test_mixed_add_vectors_bit_identical_across_group_sizes(kpm):
     """Mixed precision: 10 vectors (a 16-vector block) plus 30 more (a
     32-vector block) give the same moments, bit for bit, as 40 vectors at
