@@ -114,6 +114,16 @@ KPM_API int kpm_create(const kpm_csr_desc* ham, double a, double b, int precisio
  * transparently; moments are invariant under the reordering.  No reference
  * counterpart (the reference multiplies in the given order). */
 #define KPM_FLAG_REORDER 1
+/* KPM_PREC_MIXED only: run the DOS recursion on plain complex64 vectors
+ * instead of the default compensated form.  The default keeps a bfloat16
+ * correction next to every complex64 element (12 instead of 8 bytes) and
+ * computes each step and the moment dot products with error-free FP32
+ * transformations, which keeps the per-orbital DOS within ~1e-6 of the
+ * FP64 recursion at every Chebyshev node; the plain form moves a third
+ * fewer bytes and is off by up to ~1e-4 at the outermost nodes, where the
+ * reconstruction divides by sqrt(1 - x^2).  No reference counterpart (the
+ * reference computes in complex128). */
+#define KPM_FLAG_PLAIN_C64 2
 KPM_API int kpm_create_ex(const kpm_csr_desc* ham, double a, double b,
                           int precision, int flags, kpm_handle** out);
 /* Use an external CUDA stream (cudaStream_t) for all work of the handle. */
@@ -212,11 +222,15 @@ KPM_API int kpm_dos(const kpm_csr_desc* ham, double a, double b, int precision,
  *   moments: M * Rpad complex128, written as [moment][vector].
  * Work is enqueued on `stream` (a cudaStream_t; NULL = default stream) and
  * the call returns without waiting: results are valid once the stream has
- * completed.  The first call on a device looks up the scratch array's device
- * address (cudaGetSymbolAddress, with that device current) and caches it;
- * make that first call before any stream capture.  Calls whose GPU work
- * overlaps in time share the scratch array and race; the array keeps the
- * last call's contents, and every call writes what it reads.  Sizes whose
+ * completed.  The first call in each device context looks up the scratch
+ * array's device address (cudaGetSymbolAddress, with that device current)
+ * and caches it with the context's id, so a new context (after
+ * cudaDeviceReset, or one the caller made current) gets its own lookup;
+ * make the first call in a context before any stream capture.  Calls whose
+ * GPU work overlaps in time (different streams, threads or processes
+ * sharing the device context) share the scratch array and race: serialise
+ * them.  The array keeps the last call's contents, and every call writes
+ * what it reads.  Sizes whose
  * scratch would exceed KPM_NOALLOC_SCRATCH_BYTES (more than about 500
  * vectors at the largest row-partition count) are rejected with KPM_EINVAL. */
 typedef struct kpm_device_csr {

@@ -25,10 +25,14 @@ KPM_EUNSUPPORTED = -7
 
 PREC_FP64 = 0
 PREC_MIXED = 1
+# host-side code: KPM_PREC_MIXED with KPM_FLAG_PLAIN_C64 (plain complex64
+# DOS recursion, no compensation)
+PREC_SINGLE = 2
 KERNEL_NONE = 0
 KERNEL_JACKSON = 1
 KERNEL_LORENTZ = 2
 FLAG_REORDER = 1
+FLAG_PLAIN_C64 = 2
 
 
 class KPMError(RuntimeError):
@@ -220,8 +224,12 @@ class Handle:
         self.reorder = bool(reorder)
         h = C.c_void_p()
         self._children = weakref.WeakSet()
-        check(lib.kpm_create_ex(csr.ref(), self.a, self.b, precision,
-                                FLAG_REORDER if reorder else 0, C.byref(h)))
+        flags = FLAG_REORDER if reorder else 0
+        cprec = precision
+        if precision == PREC_SINGLE:
+            cprec, flags = PREC_MIXED, flags | FLAG_PLAIN_C64
+        check(lib.kpm_create_ex(csr.ref(), self.a, self.b, cprec, flags,
+                                C.byref(h)))
         self._h = h
 
     @property

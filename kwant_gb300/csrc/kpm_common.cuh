@@ -129,6 +129,10 @@ struct Matrix {
 
 struct kpm_handle {
   int precision = KPM_PREC_FP64;
+  // mixed precision: DOS blocks keep a bfloat16 lo part next to every
+  // complex64 element and step with the compensated kernel (cleared by
+  // KPM_FLAG_PLAIN_C64; needs the complex64 ELL copy)
+  bool compensated = false;
   int device = 0;
   int num_sms = 0;
   double a = 1.0, b = 0.0;
@@ -179,6 +183,10 @@ struct kpm_block {
   bool keep_a0 = false;
   void* a0 = nullptr;    // [N][Rpad]
   void* buf[2] = {nullptr, nullptr};
+  // compensated blocks: bfloat16 lo parts of a0 / buf, [N][Rpad] words
+  // (null otherwise); valid for a0 always, for buf while mode is DOS
+  uint32_t* lo_a0 = nullptr;
+  uint32_t* lo_buf[2] = {nullptr, nullptr};
   void* p_cur = nullptr;   // alpha_n (a0 or one of buf)
   void* p_prev = nullptr;  // alpha_{n-1}
   double* mu01 = nullptr;   // [Rpad][2] complex: mu0, mu1 per vector

@@ -357,8 +357,75 @@ __global__ void from_interleaved_kernel(const InT* __restrict__ in,
   }
 }
 
+// [R][N] complex128 -> hi [N][Rpad] complex64 + lo [N][Rpad] bfloat16 x 2:
+// hi = RN(v), lo = RZ_bf16(RZ_f32(v - hi)) (v - hi is exact in FP64).  The
+// split of hi + lo (as downloaded) gives back the same hi and lo.
+__device__ __forceinline__ float lo_part(double v, float hi) {
+  const float d = __double2float_rz(v - (double)hi);
+  return __uint_as_float(__float_as_uint(d) & 0xffff0000u);
+}
+__global__ void to_interleaved_hilo_kernel(const double2* __restrict__ in,
+                                           float2* __restrict__ out,
+                                           uint32_t* __restrict__ lo,
+                                           int64_t N, int64_t R, int64_t Rpad,
+                                           const int32_t* __restrict__ perm) {
+  __shared__ double2 tile[32][33];
+  const int64_t n0 = (int64_t)blockIdx.x * 32;
+  const int64_t r0 = (int64_t)blockIdx.y * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    int64_t r = r0 + k, n = n0 + threadIdx.x;
+    double2 v = make_double2(0.0, 0.0);
+    if (r < R && n < N) v = in[r * N + (perm ? perm[n] : n)];
+    tile[k][threadIdx.x] = v;
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    int64_t n = n0 + k, r = r0 + threadIdx.x;
+    if (n < N && r < Rpad) {
+      const double2 v = tile[threadIdx.x][k];
+      const float hr = (float)v.x, hi = (float)v.y;
+      out[n * Rpad + r] = make_float2(hr, hi);
+      lo[n * Rpad + r] = (__float_as_uint(lo_part(v.x, hr)) >> 16) |
+                         (__float_as_uint(lo_part(v.y, hi)) & 0xffff0000u);
+    }
+  }
+}
+
+// hi + lo [N][Rpad] -> [R][N] complex128 (exact)
+__global__ void from_interleaved_hilo_kernel(const float2* __restrict__ in,
+                                             const uint32_t* __restrict__ lo,
+                                             double2* __restrict__ out,
+                                             int64_t N, int64_t R,
+                                             int64_t Rpad,
+                                             const int32_t* __restrict__ perm) {
+  __shared__ double2 tile[32][33];
+  const int64_t n0 = (int64_t)blockIdx.x * 32;
+  const int64_t r0 = (int64_t)blockIdx.y * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    int64_t n = n0 + k, r = r0 + threadIdx.x;
+    double2 v = make_double2(0.0, 0.0);
+    if (n < N && r < Rpad) {
+      const float2 f = in[n * Rpad + r];
+      const uint32_t w = lo[n * Rpad + r];
+      v = make_double2((double)f.x + (double)__uint_as_float(w << 16),
+                       (double)f.y + (double)__uint_as_float(w & 0xffff0000u));
+    }
+    tile[k][threadIdx.x] = v;
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    int64_t r = r0 + k, n = n0 + threadIdx.x;
+    if (r < R && n < N) out[r * N + (perm ? perm[n] : n)] = tile[threadIdx.x][k];
+  }
+}
+
 int upload_vectors(kpm_handle* h, const double* host, int64_t R, int64_t N,
                    int64_t Rpad, void* dst) {
+  return upload_vectors_lo(h, host, R, N, Rpad, dst, nullptr);
+}
+
+int upload_vectors_lo(kpm_handle* h, const double* host, int64_t R,
+                      int64_t N, int64_t Rpad, void* dst, uint32_t* lo) {
   void* staging = nullptr;
   size_t bytes = (size_t)R * N * 16;
   cudaError_t e = cudaSuccess;
@@ -378,7 +445,10 @@ int upload_vectors(kpm_handle* h, const double* host, int64_t R, int64_t N,
     KPM_CUDA(e);
   }
   dim3 blk(32, 8), grd((unsigned)ceil_div(N, 32), (unsigned)ceil_div(Rpad, 32));
-  if (h->precision == KPM_PREC_MIXED)
+  if (h->precision == KPM_PREC_MIXED && lo)
+    to_interleaved_hilo_kernel<<<grd, blk, 0, h->stream>>>(
+        (const double2*)staging, (float2*)dst, lo, N, R, Rpad, h->perm);
+  else if (h->precision == KPM_PREC_MIXED)
     to_interleaved_kernel<float2><<<grd, blk, 0, h->stream>>>(
         (const double2*)staging, (float2*)dst, N, R, Rpad, h->perm);
   else
@@ -393,11 +463,19 @@ int upload_vectors(kpm_handle* h, const double* host, int64_t R, int64_t N,
 
 int download_vectors(kpm_handle* h, const void* src, int64_t R, int64_t N,
                      int64_t Rpad, double* host) {
+  return download_vectors_lo(h, src, nullptr, R, N, Rpad, host);
+}
+
+int download_vectors_lo(kpm_handle* h, const void* src, const uint32_t* lo,
+                        int64_t R, int64_t N, int64_t Rpad, double* host) {
   void* staging = nullptr;
   size_t bytes = (size_t)R * N * 16;
   KPM_TRY(dev_alloc(&staging, bytes, h->stream));
   dim3 blk(32, 8), grd((unsigned)ceil_div(N, 32), (unsigned)ceil_div(Rpad, 32));
-  if (h->precision == KPM_PREC_MIXED)
+  if (h->precision == KPM_PREC_MIXED && lo)
+    from_interleaved_hilo_kernel<<<grd, blk, 0, h->stream>>>(
+        (const float2*)src, lo, (double2*)staging, N, R, Rpad, h->perm);
+  else if (h->precision == KPM_PREC_MIXED)
     from_interleaved_kernel<float2><<<grd, blk, 0, h->stream>>>(
         (const float2*)src, (double2*)staging, N, R, Rpad, h->perm);
   else
@@ -845,6 +923,48 @@ int block_advance(kpm_block* b, bool dots) {
   return KPM_OK;
 }
 
+uint32_t* block_lo(const kpm_block* b, const void* hi) {
+  if (!b->lo_a0 || !hi) return nullptr;
+  if (hi == b->buf[0]) return b->lo_buf[0];
+  if (hi == b->buf[1]) return b->lo_buf[1];
+  if (hi == b->a0) return b->lo_a0;
+  return nullptr;
+}
+
+// block_advance on hi + lo vectors: the same buffer rotation, with each lo
+// part following its hi part.
+int block_advance_hilo(kpm_block* b) {
+  void* x = b->p_cur;
+  void* out;
+  const void* prev = nullptr;
+  int mode;
+  if (b->steps_done == 0) {
+    out = b->buf[0];
+    mode = STEP_FIRST;
+  } else {
+    if (b->p_prev == b->a0 && b->keep_a0)
+      out = (b->p_cur == b->buf[0]) ? b->buf[1] : b->buf[0];
+    else
+      out = b->p_prev;
+    prev = b->p_prev;
+    mode = STEP_RECUR;
+  }
+  HiloArgs q{};
+  q.xlo = block_lo(b, x);
+  q.plo = block_lo(b, prev);
+  q.olo = block_lo(b, out);
+  if (!q.xlo || !q.olo || (mode == STEP_RECUR && !q.plo)) {
+    set_error("compensated step: block has no lo part for its buffers");
+    return KPM_ESTATE;
+  }
+  StepArgs a = step_args(b, x, prev, out);
+  KPM_TRY(launch_step_hilo(b->h, mode, a, q));
+  b->p_prev = b->p_cur;
+  b->p_cur = out;
+  b->steps_done += 1;
+  return KPM_OK;
+}
+
 int block_advance_store(kpm_block* b, int smode, const float2* vell,
                         const StoreRow& row, int64_t R) {
   kpm_handle* h = b->h;
@@ -1025,6 +1145,8 @@ int kpm_create_ex(const kpm_csr_desc* ham, double a, double b, int precision,
     return KPM_ECUDA;
   }
   h->own_stream = true;
+  h->compensated =
+      precision == KPM_PREC_MIXED && !(flags & KPM_FLAG_PLAIN_C64);
   if (const char* kc = getenv("KPM_TC_KC")) h->tc_kc = atoi(kc) == 32 ? 32 : 16;
   const double scale = h->precision == KPM_PREC_MIXED ? 2.0 / a : 0.0;
   if (flags & KPM_FLAG_REORDER) {
@@ -1149,7 +1271,16 @@ int kpm_block_create(kpm_handle* h, const double* vecs, int64_t R,
   if (st == KPM_OK)
     st = dev_alloc((void**)&b->mu01, (size_t)b->Rpad * 2 * sizeof(double2),
                    h->stream);
-  if (st == KPM_OK) st = upload_vectors(h, vecs, R, b->N, b->Rpad, b->a0);
+  if (st == KPM_OK && h->compensated && h->H.ell_k > 0) {
+    const size_t lbytes = (size_t)b->N * b->Rpad * sizeof(uint32_t);
+    st = dev_alloc((void**)&b->lo_buf[0], lbytes, h->stream);
+    if (st == KPM_OK) st = dev_alloc((void**)&b->lo_buf[1], lbytes, h->stream);
+    if (st == KPM_OK && b->keep_a0)
+      st = dev_alloc((void**)&b->lo_a0, lbytes, h->stream);
+    if (st == KPM_OK && !b->keep_a0) b->lo_a0 = b->lo_buf[1];
+  }
+  if (st == KPM_OK)
+    st = upload_vectors_lo(h, vecs, R, b->N, b->Rpad, b->a0, b->lo_a0);
   if (st == KPM_OK) {
     cudaError_t e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) {
@@ -1185,6 +1316,9 @@ int kpm_block_randomize(kpm_block* b, uint64_t seed) {
         static_cast<double2*>(b->a0), b->N, b->R, b->Rpad, key);
   count_launch(1);
   KPM_CHECK_LAUNCH();
+  if (b->lo_a0)  // the generated complex64 vectors are exact: lo = 0
+    KPM_CUDA(cudaMemsetAsync(b->lo_a0, 0, (size_t)total * sizeof(uint32_t),
+                             h->stream));
   return kpm_block_rewind(b);
 }
 
@@ -1207,6 +1341,9 @@ int kpm_block_destroy(kpm_block* b) {
   dev_free(b->buf[0], s);
   dev_free(b->buf[1], s);
   if (b->keep_a0) dev_free(b->a0, s);
+  dev_free(b->lo_buf[0], s);
+  dev_free(b->lo_buf[1], s);
+  if (b->keep_a0) dev_free(b->lo_a0, s);
   dev_free(b->mu01, s);
   dev_free(b->op_coef, s);
   cudaStreamSynchronize(s);
@@ -1249,8 +1386,10 @@ int kpm_block_restore(kpm_block* b, int64_t steps_done, int mode,
     // alpha_n in buf[0], alpha_{n-1} in buf[1]; the next step writes
     // alpha_{n+1} over alpha_{n-1} (when the block does not keep a0, a0
     // is buf[1] and is not needed again)
-    KPM_TRY(upload_vectors(h, alpha_cur, b->R, b->N, b->Rpad, b->buf[0]));
-    KPM_TRY(upload_vectors(h, alpha_prev, b->R, b->N, b->Rpad, b->buf[1]));
+    KPM_TRY(upload_vectors_lo(h, alpha_cur, b->R, b->N, b->Rpad, b->buf[0],
+                              b->lo_buf[0]));
+    KPM_TRY(upload_vectors_lo(h, alpha_prev, b->R, b->N, b->Rpad, b->buf[1],
+                              b->lo_buf[1]));
     b->p_cur = b->buf[0];
     b->p_prev = b->buf[1];
   }
@@ -1268,15 +1407,20 @@ int kpm_block_restore(kpm_block* b, int64_t steps_done, int mode,
 
 int kpm_block_state(kpm_block* b, double* alpha_prev, double* alpha_cur) {
   KPM_REQUIRE(b && alpha_cur, "kpm_block_state: null argument");
+  // lo parts are kept by the DOS recursion (and exist for a0 from the start)
+  const bool lo = b->lo_a0 && (b->mode == 0 || b->steps_done == 0);
   if (alpha_prev) {
     if (!b->p_prev) {
       set_error("kpm_block_state: no previous vector before the first step");
       return KPM_ESTATE;
     }
-    KPM_TRY(download_vectors(b->h, b->p_prev, b->R, b->N, b->Rpad,
-                             alpha_prev));
+    KPM_TRY(download_vectors_lo(b->h, b->p_prev,
+                                lo ? block_lo(b, b->p_prev) : nullptr, b->R,
+                                b->N, b->Rpad, alpha_prev));
   }
-  return download_vectors(b->h, b->p_cur, b->R, b->N, b->Rpad, alpha_cur);
+  return download_vectors_lo(b->h, b->p_cur,
+                             lo ? block_lo(b, b->p_cur) : nullptr, b->R, b->N,
+                             b->Rpad, alpha_cur);
 }
 
 int kpm_block_dos_moments(kpm_block* b, int64_t m_start, int64_t m_end,
@@ -1309,13 +1453,15 @@ int kpm_block_dos_moments(kpm_block* b, int64_t m_start, int64_t m_end,
   auto slot = [&](int64_t m) -> int64_t {
     return (m >= m_start && m < m_end) ? m - m_start : -1;
   };
+  // compensated blocks: hi + lo vectors and error-free steps
+  const bool hilo = b->lo_a0 != nullptr;
   if (st == KPM_OK && m_start == 0) {
-    st = block_advance(b, true);
+    st = hilo ? block_advance_hilo(b) : block_advance(b, true);
     if (st == KPM_OK) st = finalize(b, STEP_FIRST, mom, slot(0), slot(1));
   }
   int64_t n0 = m_start / 2 > 1 ? m_start / 2 : 1;
   for (int64_t n = n0; st == KPM_OK && n < m_end / 2; ++n) {
-    st = block_advance(b, true);
+    st = hilo ? block_advance_hilo(b) : block_advance(b, true);
     if (st == KPM_OK)
       st = finalize(b, STEP_RECUR, mom, slot(2 * n), slot(2 * n + 1));
   }

@@ -22,7 +22,7 @@ struct StepArgs {
   int vpl;          // complex64 vectors per lane: 2 (groups of 32) or 1
   int groups;
   int xitems;
-  double* partials; // [groups][xitems][group][3]
+  double* partials; // [group][vector*3 + component][xitems]
 };
 
 // Fused store of alpha_n's row (the correlator's recursions, ELL step,
@@ -34,6 +34,15 @@ struct StoreArgs {
   const float2* vell;
   StoreRow store;
   int64_t R;
+};
+
+// bfloat16 lo parts of a compensated (hi + lo) mixed-precision block:
+// [rows][Rpad] words, bf16 re in the low half, im in the high half
+struct HiloArgs {
+  const uint32_t* xlo;  // lo of alpha_n
+  const uint32_t* plo;  // lo of alpha_{n-1} (may alias olo)
+  uint32_t* olo;        // lo of alpha_{n+1}
+  int64_t lrp;          // lane payloads per row (set by the launcher)
 };
 
 void count_launch(int n);
@@ -67,6 +76,17 @@ int upload_vectors(kpm_handle* h, const double* host, int64_t R, int64_t N,
                    int64_t Rpad, void* dst);
 int download_vectors(kpm_handle* h, const void* src, int64_t R, int64_t N,
                      int64_t Rpad, double* host);
+// the same for compensated blocks: lo (bfloat16 x 2 words, [N][Rpad]) is
+// written on upload (exact split of the complex128 input into hi + lo) and
+// added on download (exact); lo null: complex64 only
+int upload_vectors_lo(kpm_handle* h, const double* host, int64_t R,
+                      int64_t N, int64_t Rpad, void* dst, uint32_t* lo);
+int download_vectors_lo(kpm_handle* h, const void* src, const uint32_t* lo,
+                        int64_t R, int64_t N, int64_t Rpad, double* host);
+// lo part belonging to one of the block's hi buffers (null if none)
+uint32_t* block_lo(const kpm_block* b, const void* hi);
+// block_advance of a compensated block (DOS dots always fused)
+int block_advance_hilo(kpm_block* b);
 
 int launch_step(kpm_handle* h, int mode, bool dots, const StepArgs& a);
 // widest ELL row (entries) the complex64 ELL step kernel is built for
@@ -75,6 +95,9 @@ constexpr int ELL_MAX = 16;
 int build_ell(kpm_handle* h, const kpm_csr_desc* m, Matrix* out);
 int launch_step_ell(kpm_handle* h, int mode, bool dots, const StepArgs& a,
                     const StoreArgs* sa = nullptr);
+// compensated DOS step on a hi + lo block (complex64 ELL handle), dots fused
+int launch_step_hilo(kpm_handle* h, int mode, const StepArgs& a,
+                     const HiloArgs& q);
 StepArgs step_args(kpm_block* b, const void* x, const void* prev, void* out);
 int block_advance(kpm_block* b, bool dots);
 // block_advance without dot products that also writes the store row of the

@@ -16,6 +16,8 @@
 // calls share it: calls whose GPU work overlaps in time (different streams,
 // threads or processes sharing the device context) race on it.
 
+#include <cuda.h>
+
 #include <mutex>
 
 #include "kpm_common.cuh"
@@ -29,18 +31,54 @@ static __device__ __align__(256) double
 constexpr int NOALLOC_MAX_DEVICES = 64;
 static std::mutex g_noalloc_mutex;
 static double* g_noalloc_addr[NOALLOC_MAX_DEVICES] = {nullptr};
+static unsigned long long g_noalloc_ctx[NOALLOC_MAX_DEVICES] = {0};
 static int g_noalloc_sms[NOALLOC_MAX_DEVICES] = {0};
 
-// Device address of the scratch array for the current device.  The name
-// g_noalloc_scratch in host code is only a host-side stand-in, so the address
-// is looked up once per device (with that device current) and cached.
+// Id of the current device context (unique over the process lifetime), 0
+// when none is current yet.  The driver calls come through the runtime's
+// entry-point lookup, so the library needs no link to the driver library.
+static unsigned long long current_context_id() {
+  using GetCurrent = CUresult (*)(CUcontext*);
+  using GetId = CUresult (*)(CUcontext, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    looked_up = true;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent",
+                                         (void**)&get_current, 12000,
+                                         cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      get_current = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", (void**)&get_id, 12000,
+                                         cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      get_id = nullptr;
+    cudaGetLastError();
+  }
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx ||
+      get_id(ctx, &id) != CUDA_SUCCESS)
+    return 0;
+  return id;
+}
+
+// Device address of the scratch array in the current device context.  The
+// name g_noalloc_scratch in host code is only a host-side stand-in, so the
+// address is looked up (with the device current) on the first call in each
+// context and cached with the context's id: after cudaDeviceReset, or in a
+// context the caller made current, the module can sit at another address,
+// and the next call looks it up again.
 static int noalloc_scratch(double** scratch, int* sms) {
   int dev = -1;
   KPM_CUDA(cudaGetDevice(&dev));
   KPM_REQUIRE(dev >= 0 && dev < NOALLOC_MAX_DEVICES,
               "kpm_dos_moments_noalloc: device ordinal %d not supported", dev);
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_addr[dev]) {
+  unsigned long long ctx = current_context_id();
+  if (!g_noalloc_addr[dev] || ctx == 0 || ctx != g_noalloc_ctx[dev]) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || p == nullptr) {
@@ -53,6 +91,8 @@ static int noalloc_scratch(double** scratch, int* sms) {
     KPM_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
     g_noalloc_sms[dev] = n;
     g_noalloc_addr[dev] = static_cast<double*>(p);
+    // the lookup made a context current if none was
+    g_noalloc_ctx[dev] = ctx ? ctx : current_context_id();
   }
   *scratch = g_noalloc_addr[dev];
   *sms = g_noalloc_sms[dev];

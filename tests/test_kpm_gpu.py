@@ -156,13 +156,38 @@ def test_square100_fp64(kpm):
     assert _rel(sd.densities, g['densities']) < TOL
 
 
-def test_square100_mixed_dos_error(kpm):
+@pytest.mark.parametrize('precision', ['mixed', 'single'])
+def test_square100_mixed_dos_error(kpm, precision):
     g = load('square100')
     ham = csr(g)
     n = ham.shape[0]
-    sd = _sd(kpm, ham, g, num_moments=100, num_vectors=10, precision='mixed')
+    sd = _sd(kpm, ham, g, num_moments=100, num_vectors=10,
+             precision=precision)
     err = np.max(np.abs(sd.densities - g['densities'])) / n
     assert err < 1e-5, err
+
+
+def test_mixed_dos_all_nodes_long_expansion(kpm):
+    """Mixed precision against the oracle on a long expansion: graphene
+    flake of 200 x 200 cells (8e4 orbitals) with a Peierls flux of 1/1000
+    per hexagon and W = 0.5, R = 4, M = 2000, the same vectors and raw
+    bounds.  The per-orbital DOS must be within 1e-5 at every one of the
+    2M Chebyshev nodes, the outermost ones (x = +-0.99999992, where the
+    reconstruction divides by sqrt(1 - x^2) ~ 4e-4) included; the plain
+    complex64 recursion misses that there by an order of magnitude."""
+    from kwant_gb300 import lattices
+    syst = lattices.honeycomb(200, t=1.0, flux=1.0 / 1000, W=0.5, seed=0)
+    ham = syst.hamiltonian_submatrix(sparse=True).tocsr()
+    n, R, M = ham.shape[0], 4, 2000
+    v0, vecs = ref_vectors(1, n, R)
+    lmin, lmax = ko.spectral_bounds(ham, 0.05, v0)
+    ref = ko.spectral_density(ham, vecs, lmin, lmax, M)
+    sd = kpm.SpectralDensity(ham, bounds=(lmin, lmax),
+                             vector_factory=list(vecs), num_vectors=R,
+                             num_moments=M, precision='mixed')
+    assert np.array_equal(sd.energies, ref['energies'])
+    err = np.abs(sd.densities.real - ref['densities'].real) / n
+    assert err.max() < 1e-5, (err.max(), sd.energies[np.argmax(err)])
 
 
 # --------------------------------------------------------------- operators

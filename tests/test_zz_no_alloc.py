@@ -6,12 +6,14 @@ The test plays such a caller: it allocates every buffer itself (with torch)
 and passes device pointers through the C ABI; the result must match the
 regular, allocating entry point (kpm_block_dos_moments) within the FP64
 parity tolerance of the other tests, on two calls in a row (the second call
-runs over the scratch the first one left behind).  In mixed precision the
-two entry points compute the same Chebyshev vectors with different step
-kernels (CSR here, ELL there) whose FP32 dot-product partials group the
-rows differently, so they agree to FP32 partial-sum rounding (1e-8).  This
-file is collected last so that a failure here does not stop the rest of
-the GPU suite.
+runs over the scratch the first one left behind); in FP64 it must also
+match the reference's own moments (the square100 fixture).  In mixed
+precision this entry point runs the plain complex64 recursion, so it is
+compared with a handle in that form (KPM_FLAG_PLAIN_C64): the two compute
+the same Chebyshev vectors with different step kernels (CSR here, ELL
+there) whose FP32 dot-product partials group the rows differently, so they
+agree to FP32 partial-sum rounding (1e-8).  This file is collected last so
+that a failure here does not stop the rest of the GPU suite.
 """
 
 import ctypes as C
@@ -47,8 +49,9 @@ def test_noalloc_matches_allocating_entry_point(precision):
     mixed = precision == 'mixed'
     prec = _lib.PREC_MIXED if mixed else _lib.PREC_FP64
 
-    # the existing, allocating entry point
-    h = _lib.Handle(ham, a, b, prec)
+    # the existing, allocating entry point (plain complex64 form in mixed
+    # precision, the arithmetic of this entry point)
+    h = _lib.Handle(ham, a, b, _lib.PREC_SINGLE if mixed else prec)
     blk = _lib.Block(h, vecs, keep_a0=True)
     expected = blk.dos_moments(0, M)
     blk.close()
@@ -90,6 +93,11 @@ def test_noalloc_matches_allocating_entry_point(precision):
         got = got[:, :R].T
         err = np.max(np.abs(got - expected)) / np.max(np.abs(expected))
         assert err < TOL[precision], (call, err)
+        if not mixed:
+            ref = g['moments_list']
+            err = np.max(np.abs(got[:, :ref.shape[1]] - ref)) / \
+                np.max(np.abs(ref))
+            assert err < TOL[precision], (call, err)
 
 
 def test_noalloc_rejects_oversized_requests():
