@@ -54,12 +54,17 @@ def make_workload(cells, vectors, seed_dis=0, seed_vec=1):
     return ham, v0, vecs
 
 
+VEC_BYTES = {'mixed': 12, 'single': 8, 'fp64': 16}
+
+
 def step_bytes(nnz, n, R, precision):
     """Algorithmic HBM bytes of one Chebyshev step over R vectors:
     values + column indices + row pointers + read alpha_n, read alpha_{n-1},
-    write alpha_{n+1} (complex64 or complex128)."""
-    sv = 8 if precision == 'mixed' else 16
-    return nnz * sv + 4 * nnz + 4 * (n + 1) + 3 * n * R * sv
+    write alpha_{n+1}.  Vector elements: complex64 plus a bfloat16 x 2
+    correction (12 B, 'mixed'), complex64 (8 B, 'single') or complex128
+    (16 B); values complex64 (8 B) or complex128 (16 B)."""
+    sv = 16 if precision == 'fp64' else 8
+    return nnz * sv + 4 * nnz + 4 * (n + 1) + 3 * n * R * VEC_BYTES[precision]
 
 
 # ------------------------------------------------------------------ clocks
@@ -273,10 +278,11 @@ def run_ours(args):
     R, M = args.vectors, args.moments
     lo, hi = kpm.spectral_bounds(ham, 0.05, v0, 'lanczos')
     a, b = kpm._rescale_ab(lo, hi, 0.05)
-    prec = _lib.PREC_MIXED if args.precision == 'mixed' else _lib.PREC_FP64
+    prec = {'mixed': _lib.PREC_MIXED, 'single': _lib.PREC_SINGLE,
+            'fp64': _lib.PREC_FP64}[args.precision]
     csr = _lib.Csr(ham)
     handle = _lib.Handle(csr, a, b, prec,
-                         reorder=args.reorder and args.precision == 'mixed')
+                         reorder=args.reorder and args.precision != 'fp64')
     block = _lib.Block(handle, vecs, keep_a0=True)
     stream = torch.cuda.ExternalStream(handle.stream())
     setup_s = time.perf_counter() - t_setup
@@ -331,7 +337,7 @@ def run_ours(args):
     # MB against 794.0 MB algorithmic; the workload here is too large for a
     # multi-pass capture), scaled to this launch by its algorithmic bytes
     traffic = None
-    if args.precision == 'mixed' and args.reorder and R == 64:
+    if args.precision == 'single' and args.reorder and R == 64:
         traffic = B * (774.5 / 794.0)
 
     # ---- accuracy vs the FP64 path (untimed) -------------------------------
@@ -339,7 +345,7 @@ def run_ours(args):
     if args.accuracy and rank == 0:
         nodes = kpm._chebyshev_nodes(2 * M)
         mom64 = None
-        if prec == _lib.PREC_MIXED:
+        if prec != _lib.PREC_FP64:
             h64 = _lib.Handle(csr, a, b, _lib.PREC_FP64)
             b64 = _lib.Block(h64, vecs, keep_a0=True)
             s64 = torch.cuda.ExternalStream(h64.stream())
@@ -378,7 +384,7 @@ def run_ours(args):
 
     # ---- e2e through the C ABI one-shot call (host buffers) ----------------
     e2e = None
-    if args.e2e and rank == 0:
+    if args.e2e and rank == 0 and args.precision != 'single':
         pin_vec = torch.empty((R, n, 2), dtype=torch.float64,
                               pin_memory=True)
         pin_vec.numpy()[:] = vecs.view(np.float64).reshape(R, n, 2)
@@ -451,24 +457,25 @@ def run_ours(args):
             'steps': args.steps, 'warmup': args.warmup,
             'ms_per_step': ms_per_step, 'higher_is_better': True,
             'scaling': 'weak', 'vs_baseline': None,
-            'dtype': 'c64+f64acc' if args.precision == 'mixed' else 'c128',
+            'dtype': {'mixed': 'c64+bf16lo, f64acc', 'single': 'c64+f64acc',
+                      'fp64': 'c128'}[args.precision],
             'data': 'synthetic',
             'config': {'workload': _workload_name(args),
                        'precision': args.precision, 'nnz': int(nnz),
                        'orbitals': int(n), 'R': R, 'M': M,
                        'matvec_steps_per_step': M // 2,
                        'l2': 'inputs larger than L2 (vector blocks %.2f GB '
-                             'each), no flush' % (n * R * (8 if args.precision
-                                                          == 'mixed' else 16)
-                                                  / 1e9),
+                             'each), no flush' % (n * R * VEC_BYTES[
+                                 args.precision] / 1e9),
                        'setup_s': setup_s, 'parallelism':
                        'replicas' if world > 1 else 'single'},
             'roofline': {'bound': 'hbm', 'achieved': achieved,
                          'peak': hbm_peak, 'unit': 'GB/s',
                          'frac': achieved / hbm_peak, 'traffic': traffic,
-                         'kernel': ('cheb_step_ell_kernel'
-                                    if args.precision == 'mixed' else
-                                    'cheb_step_kernel') +
+                         'kernel': {'mixed': 'cheb_step_hilo_kernel',
+                                    'single': 'cheb_step_ell_kernel',
+                                    'fp64': 'cheb_step_kernel'}[
+                                        args.precision] +
                                    ' (fused step + moment dots)',
                          'algorithmic_bytes_per_launch': B,
                          'avg_launch_ms': avg_step_ms,
@@ -874,7 +881,8 @@ def main():
     p.add_argument('--steps', type=int, default=5)
     p.add_argument('--warmup', type=int, default=3)
     p.add_argument('--impl', default='ours', choices=['ours', 'reference'])
-    p.add_argument('--precision', default='mixed', choices=['mixed', 'fp64'])
+    p.add_argument('--precision', default='mixed',
+                   choices=['mixed', 'single', 'fp64'])
     p.add_argument('--cells', type=int, default=1000)
     p.add_argument('--vectors', type=int, default=64)
     p.add_argument('--moments', type=int, default=2000)

@@ -352,6 +352,20 @@ KPM_API int kpm_correlator_moments(kpm_handle* h, double a2, double b2,
                                    int64_t R, int64_t M, int gemm, int per_vector,
                                    double* mu_out);
 
+/* Fermi-weighted node sums for a grid of (mu, T) points, the device form
+ * of SpectralDensity.integrate (Gauss-Chebyshev sum, kwant/kpm.py:297-316)
+ * and of Correlator.__call__ (Simpson over the nodes, kwant/kpm.py:
+ * 608-630) with fermi_distribution (kwant/kpm.py:990-1009):
+ *   out[p][w] = sum_k weights[k] * f(energies[k]; mu[p], T[p]) * values[k][w]
+ * energies, weights: n doubles; values: n x W complex128; out: P x W
+ * complex128.  mu and temperature: P doubles (T >= 0; T = 0 is the step
+ * E - mu < 0), or both NULL for f = 1 (then P = 1).  The caller folds the
+ * quadrature weights and any energy-dependent factor into weights. */
+KPM_API int kpm_fermi_sums(int64_t n, const double* energies,
+                           const double* weights, int64_t W,
+                           const double* values, int64_t P, const double* mu,
+                           const double* temperature, double* out);
+
 /* Integral factor of Correlator._build_integral_factor (kwant/kpm.py:
  * 720-760) on the device: mu (M x M complex128), kernel weights g (M, with
  * g[0] already halved), nodes x_k (2M) -> factor (2M complex128). */

@@ -115,6 +115,7 @@ def _load():
         'kpm_handle_matvec': [P, P, P],
         'kpm_correlator_moments': [P, D, D, P, P, P, I64, I64, I, I, P],
         'kpm_integral_factor': [I64, P, P, P, P],
+        'kpm_fermi_sums': [I64, P, P, I64, P, I64, P, P, P],
         'kpm_last_kernel_ms': [P, P],
         'kpm_dos_moments_noalloc': [P, D, D, I, P, I64, I64, P, P, P],
         'kpm_last_gemm': [P, P, P],
@@ -461,6 +462,31 @@ def correlator_moments(handle, a2, b2, v_alpha, v_beta, vecs, M, gemm=2,
                                      va.ref(), vb.ref(), ptr(vecs), R, M,
                                      int(gemm), 1 if per_vector else 0,
                                      ptr(out)))
+    return out
+
+
+def fermi_sums(energies, weights, values, mu=None, temperature=None):
+    """sum_k weights[k] * f(energies[k]; mu, T) * values[k, :] on the
+    device for every (mu, T) point (f = 1 without mu): values (n, W)
+    complex, mu / temperature 1-D of length P -> (P, W) complex128."""
+    e = np.ascontiguousarray(energies, dtype=np.float64)
+    w = np.ascontiguousarray(weights, dtype=np.float64)
+    v = c128(values)
+    n, W = v.shape
+    if mu is None:
+        P, pm, pt = 1, None, None
+    else:
+        pm = np.ascontiguousarray(mu, dtype=np.float64).ravel()
+        pt = np.ascontiguousarray(temperature, dtype=np.float64).ravel()
+        if pm.shape != pt.shape:
+            raise ValueError('mu and temperature must have the same size')
+        if np.any(pt < 0):
+            raise ValueError('temperature must be non-negative')
+        P = pm.size
+    out = np.empty((P, W), dtype=np.complex128)
+    check(lib.kpm_fermi_sums(n, ptr(e), ptr(w), W, ptr(v), P,
+                             ptr(pm) if pm is not None else None,
+                             ptr(pt) if pt is not None else None, ptr(out)))
     return out
 
 

@@ -278,6 +278,46 @@ __global__ void chebval_kernel(int64_t M, int64_t W,
                         __dadd_rn(c0.y, __dmul_rn(c1.y, xe)));
 }
 
+// Fermi-weighted sums over the energy nodes for a grid of (mu, T) points:
+// out[p][w] = sum_k weight[k] * f(E_k; mu_p, T_p) * values[k][w], with
+// f = fermi_distribution of kwant/kpm.py:990-1009 (T = 0: the step
+// E - mu < 0; otherwise 1 / (1 + exp((E - mu) / T))), or f = 1 when mu is
+// null.  One block per (p, w); each thread sums a strided share of the nodes
+// in FP64 and the block reduces in a fixed order.
+__global__ void fermi_sums_kernel(int64_t n, const double* __restrict__ e,
+                                  const double* __restrict__ wt,
+                                  const double2* __restrict__ vals, int64_t W,
+                                  const double* __restrict__ mu,
+                                  const double* __restrict__ temp,
+                                  double2* __restrict__ out) {
+  const int64_t p = blockIdx.x / W, w = blockIdx.x % W;
+  const double m = mu ? mu[p] : 0.0, T = mu ? temp[p] : 0.0;
+  double sr = 0.0, si = 0.0;
+  for (int64_t k = threadIdx.x; k < n; k += blockDim.x) {
+    double f = 1.0;
+    if (mu) {
+      const double d = e[k] - m;
+      f = T == 0.0 ? (d < 0.0 ? 1.0 : 0.0) : 1.0 / (1.0 + exp(d / T));
+    }
+    const double c = wt[k] * f;
+    const double2 v = vals[k * W + w];
+    sr += c * v.x;
+    si += c * v.y;
+  }
+  __shared__ double rr[256], ri[256];
+  rr[threadIdx.x] = sr;
+  ri[threadIdx.x] = si;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) {
+      rr[threadIdx.x] += rr[threadIdx.x + s];
+      ri[threadIdx.x] += ri[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = make_double2(rr[0], ri[0]);
+}
+
 extern "C" {
 
 int kpm_chebval(int64_t M, int64_t W, const double* coefs, int64_t E,
@@ -363,6 +403,68 @@ int kpm_reconstruct(int64_t R, int64_t M, int64_t W, const double* moments,
   cudaStreamSynchronize(s);
   KPM_CUDA(e);
   return st;
+}
+
+int kpm_fermi_sums(int64_t n, const double* energies, const double* weights,
+                   int64_t W, const double* values, int64_t P,
+                   const double* mu, const double* temperature, double* out) {
+  KPM_REQUIRE(n > 0 && W > 0 && P > 0 && energies && weights && values &&
+                  out && (mu == nullptr) == (temperature == nullptr) &&
+                  (mu != nullptr || P == 1),
+              "kpm_fermi_sums: invalid argument");
+  KPM_REQUIRE(P * W < (int64_t)1 << 31, "kpm_fermi_sums: grid too large");
+  for (int64_t p = 0; mu && p < P; ++p)
+    KPM_REQUIRE(temperature[p] >= 0.0,
+                "kpm_fermi_sums: temperature must be non-negative");
+  int dev, sms;
+  KPM_TRY(init_device(&dev, &sms));
+  cudaStream_t s = 0;
+  double *de = nullptr, *dw = nullptr, *dmu = nullptr, *dT = nullptr;
+  double2 *dv = nullptr, *dout = nullptr;
+  int st = dev_alloc((void**)&de, n * sizeof(double), s);
+  if (st == KPM_OK) st = dev_alloc((void**)&dw, n * sizeof(double), s);
+  if (st == KPM_OK)
+    st = dev_alloc((void**)&dv, (size_t)n * W * sizeof(double2), s);
+  if (st == KPM_OK && mu) st = dev_alloc((void**)&dmu, P * sizeof(double), s);
+  if (st == KPM_OK && mu) st = dev_alloc((void**)&dT, P * sizeof(double), s);
+  if (st == KPM_OK)
+    st = dev_alloc((void**)&dout, (size_t)P * W * sizeof(double2), s);
+  cudaError_t e = cudaSuccess;
+  if (st == KPM_OK) {
+    e = cudaMemcpyAsync(de, energies, n * sizeof(double),
+                        cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dw, weights, n * sizeof(double),
+                          cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dv, values, (size_t)n * W * sizeof(double2),
+                          cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && mu)
+      e = cudaMemcpyAsync(dmu, mu, P * sizeof(double), cudaMemcpyHostToDevice,
+                          s);
+    if (e == cudaSuccess && mu)
+      e = cudaMemcpyAsync(dT, temperature, P * sizeof(double),
+                          cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+      fermi_sums_kernel<<<(unsigned)(P * W), 256, 0, s>>>(n, de, dw, dv, W,
+                                                          dmu, dT, dout);
+      count_launch(1);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(out, dout, (size_t)P * W * sizeof(double2),
+                          cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  }
+  dev_free(de, s);
+  dev_free(dw, s);
+  dev_free(dv, s);
+  dev_free(dmu, s);
+  dev_free(dT, s);
+  dev_free(dout, s);
+  if (st != KPM_OK) return st;
+  KPM_CUDA(e);
+  return KPM_OK;
 }
 
 int kpm_integral_factor(int64_t M, const double* mu, const double* g,

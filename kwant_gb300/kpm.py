@@ -106,6 +106,36 @@ def _reorder_default(reorder, precision):
     return bool(reorder)
 
 
+def _simpson_weights(x):
+    """Weights w with sum(w * y) = scipy.integrate.simpson(y, x=x), the
+    quadrature of Correlator.__call__ (kwant/kpm.py:627): the composite
+    Simpson rule for irregularly spaced points (parabola through each pair
+    of intervals), and for an even number of points Simpson on all but the
+    last interval plus Cartwright's correction for it (the form scipy uses
+    since 1.11).  Simpson is linear in y, so the weights depend on x only."""
+    x = np.asarray(x, dtype=float)
+    n = x.size
+    w = np.zeros(n)
+    if n < 2:
+        return w
+    h = np.diff(x)
+    if n == 2:
+        return np.full(2, 0.5 * h[0])
+    stop = n - 2 if n % 2 else n - 3          # triples (i, i+1, i+2)
+    for i in range(0, stop, 2):
+        h0, h1 = h[i], h[i + 1]
+        hs, hp = h0 + h1, h0 * h1
+        w[i] += hs / 6.0 * (2.0 - h1 / h0)
+        w[i + 1] += hs / 6.0 * (hs * hs / hp)
+        w[i + 2] += hs / 6.0 * (2.0 - h0 / h1)
+    if n % 2 == 0:
+        h0, h1 = h[-2], h[-1]
+        w[-1] += (2 * h1 ** 2 + 3 * h0 * h1) / (6 * (h1 + h0))
+        w[-2] += (h1 ** 2 + 3.0 * h0 * h1) / (6 * h0)
+        w[-3] -= h1 ** 3 / (6 * h0 * (h0 + h1))
+    return w
+
+
 def _chebyshev_nodes(n_sampling):
     """kwant/kpm.py:1190-1194."""
     raw, step = np.linspace(np.pi, 0, n_sampling, endpoint=False,
@@ -676,14 +706,47 @@ class SpectralDensity:
         return np.transpose(vals / g_e)
 
     def integrate(self, distribution_function=None):
-        """kwant/kpm.py:297-316."""
+        """kwant/kpm.py:297-316: the Gauss-Chebyshev sum
+        a / (2M) * sum_k gamma_k f(E_k), summed on the device (the
+        distribution function, a Python callable, is evaluated on the
+        host at the 2M energies)."""
         factor = self._a / (2 * self.num_moments)
+        gam = np.asarray(self._gammas)
+        vals = gam.reshape(gam.shape[0], -1)
+        n = vals.shape[0]
         if distribution_function is None:
-            rho = self._gammas
+            d = np.ones(n)
         else:
-            distribution_array = distribution_function(self.energies)
-            rho = np.transpose(self._gammas.transpose() * distribution_array)
-        return factor * np.sum(rho, axis=0)
+            d = np.asarray(distribution_function(self.energies))
+            d = np.broadcast_to(d, (n,))
+        out = _lib.fermi_sums(self.energies, factor * d.real, vals)[0]
+        if np.iscomplexobj(d):
+            out = out + 1j * _lib.fermi_sums(self.energies, factor * d.imag,
+                                             vals)[0]
+        if not (np.iscomplexobj(gam) or np.iscomplexobj(d)):
+            out = out.real
+        return out[0] if gam.ndim == 1 else out.reshape(gam.shape[1:])
+
+    def integrate_sweep(self, mu=0, temperature=0):
+        """``integrate(lambda E: fermi_distribution(E, mu, T))`` for a
+        whole grid of (mu, temperature) points in one device launch (no
+        reference counterpart; the reference evaluates one distribution
+        per call, kwant/kpm.py:297-316): mu and temperature broadcast
+        against each other; the result has their broadcast shape (plus the
+        operator's output shape)."""
+        mu, temperature = np.broadcast_arrays(np.asarray(mu, float),
+                                              np.asarray(temperature, float))
+        if np.any(temperature < 0):
+            raise ValueError("temperature must be non-negative")
+        factor = self._a / (2 * self.num_moments)
+        gam = np.asarray(self._gammas)
+        vals = gam.reshape(gam.shape[0], -1)
+        w = np.full(vals.shape[0], factor)
+        out = _lib.fermi_sums(self.energies, w, vals, mu.ravel(),
+                              temperature.ravel())
+        if not np.iscomplexobj(gam):
+            out = out.real
+        return out.reshape(mu.shape + gam.shape[1:])
 
     def add_moments(self, num_moments=None, *, energy_resolution=None):
         """kwant/kpm.py:318-358."""
@@ -981,35 +1044,35 @@ class Correlator:
                  for m in self.moments_matrix]).T
 
     def __call__(self, mu=0, temperature=0):
-        """kwant/kpm.py:608-630."""
-        e = self.energies
-        e_rescaled = (e - self._b) / self._a
-        distribution_array = fermi_distribution(e, mu, temperature)
-        integrand = np.divide(distribution_array, (1 - e_rescaled ** 2) ** 2)
-        integrand = np.multiply(integrand, self._integral_factor)
-        integral = simpson(integrand, x=e_rescaled)
-        prefactor = 2 * 4**2 / ((2 * self._a) ** 2)
-        return prefactor * integral
+        """kwant/kpm.py:608-630: prefactor * Simpson over the rescaled
+        nodes of f(E; mu, T) / (1 - e^2)^2 * factor(e), summed on the
+        device."""
+        if temperature < 0:
+            raise ValueError("temperature must be non-negative")
+        return self.sweep(mu, temperature)[()]
 
     def sweep(self, mu=0, temperature=0):
-        """``self(mu, temperature)`` over a grid: ``mu`` and
-        ``temperature`` broadcast against each other and the result has
-        their broadcast shape.  One vectorised Simpson integration over the
-        2M energies for all points (no reference counterpart: the reference
-        evaluates one (mu, temperature) per call, kwant/kpm.py:608-630)."""
+        """``self(mu, temperature)`` over a grid in one device launch:
+        ``mu`` and ``temperature`` broadcast against each other and the
+        result has their broadcast shape (no reference counterpart: the
+        reference evaluates one (mu, temperature) per call,
+        kwant/kpm.py:608-630).  The Simpson weights of the rescaled nodes,
+        the (1 - e^2)^-2 factor and the prefactor 2 * 4^2 / (2a)^2 are
+        folded into one weight per node on the host; the Fermi function
+        and the sums over nodes run on the device."""
         mu, temperature = np.broadcast_arrays(np.asarray(mu, float),
                                               np.asarray(temperature, float))
+        if np.any(temperature < 0):
+            raise ValueError("temperature must be non-negative")
         e = self.energies
         e_rescaled = (e - self._b) / self._a
-        flat_mu, flat_t = mu.ravel(), temperature.ravel()
-        dist = np.empty((flat_mu.size, e.size))
-        for k in range(flat_mu.size):
-            dist[k] = fermi_distribution(e, flat_mu[k], flat_t[k])
-        integrand = dist / ((1 - e_rescaled ** 2) ** 2)
-        integrand = integrand * self._integral_factor
-        integral = simpson(integrand, x=e_rescaled, axis=-1)
         prefactor = 2 * 4**2 / ((2 * self._a) ** 2)
-        return (prefactor * integral).reshape(mu.shape)
+        w = prefactor * _simpson_weights(e_rescaled) / \
+            ((1 - e_rescaled ** 2) ** 2)
+        factor = np.asarray(self._integral_factor)
+        vals = factor.reshape(factor.shape[0], -1)
+        out = _lib.fermi_sums(e, w, vals, mu.ravel(), temperature.ravel())
+        return out.reshape(mu.shape + factor.shape[1:])
 
     def add_moments(self, num_moments=None, *, energy_resolution=None):
         """kwant/kpm.py:637-664 (recomputed on the device with the larger
