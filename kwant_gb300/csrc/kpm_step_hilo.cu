@@ -16,13 +16,15 @@
 // What: every vector element is stored as a complex64 "hi" part plus a
 // bfloat16 "lo" correction (4 more bytes per complex element, in a separate
 // [row][vector] array), and each step computes a_{n+1} = 2H~ a_n - a_{n-1}
-// to ~2^-38 relative with error-free FP32 transformations before splitting
-// it again:
+// to ~2^-38 (relative to the anchor below) with error-free FP32
+// transformations before splitting it again:
 //   * the hi products h * x_hi are accumulated from an anchor C = 32: every
 //     partial sum stays within a factor two of the previous one, so
 //     s1 = fma(h, x, s), m = s - s1 (exact, Sterbenz) and e = fma(h, x, m)
 //     give the rounding error of each fused multiply-add exactly; the errors
-//     are summed in FP32 (they are ~2^-19 each);
+//     are summed in FP32 (they are ~2^-19 each).  Components far below the
+//     anchor (|x| < ~1e-5, the decaying tails of a localised vector) keep
+//     only FP32 precision; their share of every moment is as small;
 //   * the lo products h * x_lo (and the lo part of a_{n-1}) are one FP32
 //     sum: a 2^-24 error on a 2^-24-relative quantity;
 //   * hi = RN(v), lo = RZ_bf16(RZ(v - hi)): round toward zero keeps |lo| at
@@ -49,67 +51,114 @@ namespace kpm {
 // gracefully, not the hi part)
 constexpr float HILO_ANCHOR = 32.0f;
 
-__device__ __forceinline__ float bf_re(uint32_t w) {
-  return __uint_as_float(w << 16);
+// Packed (re, im) pairs: every operation below runs on a float2 with one
+// FFMA2 / FADD2 / FMUL2 instruction.  Intrinsics only: nothing may be
+// contracted or reassociated in the error-free transformations.
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+  return __ffma2_rn(b, make_float2(-1.f, -1.f), a);   // a - b, one rounding
 }
-__device__ __forceinline__ float bf_im(uint32_t w) {
-  return __uint_as_float(w & 0xffff0000u);
-}
-// truncate two floats to bfloat16 (round toward zero): re in the low half
-__device__ __forceinline__ uint32_t bf_pack_rz(float re, float im) {
-  return __byte_perm(__float_as_uint(re), __float_as_uint(im), 0x7632);
-}
-
 // s + a*b with its rounding error added to c (exact while s stays within a
-// factor two of the anchor).  Intrinsics: nothing may be contracted or
-// reassociated here.
-__device__ __forceinline__ void acc_fma(float& s, float& c, float a, float b) {
-  const float s1 = __fmaf_rn(a, b, s);
-  const float m = __fsub_rn(s, s1);
-  c = __fadd_rn(c, __fmaf_rn(a, b, m));
+// factor two of the anchor)
+__device__ __forceinline__ void acc_fma(float2& s, float2& c, float2 a,
+                                        float2 b) {
+  const float2 s1 = __ffma2_rn(a, b, s);
+  const float2 m = sub2(s, s1);
+  c = __fadd2_rn(c, __ffma2_rn(a, b, m));
   s = s1;
 }
 // s - b with its rounding error added to c
-__device__ __forceinline__ void acc_sub(float& s, float& c, float b) {
-  const float s1 = __fsub_rn(s, b);
-  const float m = __fsub_rn(s, s1);
-  c = __fadd_rn(c, __fsub_rn(m, b));
+__device__ __forceinline__ void acc_sub(float2& s, float2& c, float2 b) {
+  const float2 s1 = sub2(s, b);
+  const float2 m = sub2(s, s1);
+  c = __fadd2_rn(c, sub2(m, b));
   s = s1;
 }
-// Dot2 accumulation (TwoProd + TwoSum) of a*b into (s, c)
-__device__ __forceinline__ void dot2(float& s, float& c, float a, float b) {
-  const float p = __fmul_rn(a, b);
-  const float pe = __fmaf_rn(a, b, -p);
-  const float t = __fadd_rn(s, p);
-  const float z = __fsub_rn(t, s);
-  const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
+// Dot2 accumulation of a*b into (s, c) (Ogita, Rump & Oishi 2005: TwoProd
+// by FMA, Knuth's TwoSum; scale-invariant)
+__device__ __forceinline__ void dot2(float2& s, float2& c, float2 a,
+                                     float2 b) {
+  const float2 p = __fmul2_rn(a, b);
+  const float2 pe =
+      __ffma2_rn(a, b, __fmul2_rn(p, make_float2(-1.f, -1.f)));
+  const float2 t = __fadd2_rn(s, p);
+  const float2 z = sub2(t, s);
+  const float2 e = __fadd2_rn(sub2(s, sub2(t, z)), sub2(p, z));
   s = t;
-  c = __fadd_rn(c, __fadd_rn(e, pe));
+  c = __fadd2_rn(c, __fadd2_rn(e, pe));
+}
+// bfloat16 pair word (re in the low half) -> (re, im)
+__device__ __forceinline__ float2 lo_pair(uint32_t w) {
+  return make_float2(__uint_as_float(w << 16),
+                     __uint_as_float(w & 0xffff0000u));
+}
+// truncate (re, im) to bfloat16 (round toward zero): re in the low half
+__device__ __forceinline__ uint32_t lo_pack_rz(float2 v) {
+  return __byte_perm(__float_as_uint(v.x), __float_as_uint(v.y), 0x7632);
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(
+                   static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
+               "l"(src)
+               : "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
+// Block size by ELL width: each thread stages a row's own x, alpha_{n-1}
+// and K gathered rows (24 bytes each, hi and lo), double-buffered; the
+// block must leave room for two or three blocks per SM.
+template <int K> struct HiloCfg {
+  static constexpr int THREADS = K <= 4 ? 256 : (K <= 12 ? 128 : 64);
+  static constexpr int ITEMS = K + 2;
+  static constexpr int NW = THREADS / 32;
+  static constexpr int NSLOT = THREADS / 8;
+  static constexpr size_t SMEM =
+      2 * ITEMS * THREADS * (sizeof(float4) + sizeof(uint2)) +
+      NW * 3 * 4 * K * (sizeof(int32_t) + sizeof(float2)) +
+      NSLOT * 48 * sizeof(double);
+};
+
 // The step over 16-vector sub-groups in 8-lane slots whose lanes hold two
-// complex64 vectors each (a float4 of hi parts, a uint2 of lo parts).
-// MODE STEP_FIRST: a_1 = H~ a_0 with the FP64 dots mu_0 = <a_0|a_0> and
-// <a_1|a_0>; STEP_RECUR: a_{n+1} = 2 H~ a_n - a_{n-1} with the compensated
-// dots <a_n|a_n>, <a_n+1|a_n>.
+// complex64 vectors each (a float4 of hi parts, a uint2 of lo parts).  A
+// warp's four slots walk adjacent rows.  Per row iteration each thread
+// copies its next row's slices (own x, alpha_{n-1} and the K gathered rows,
+// hi and lo) into shared memory with cp.async while it computes the current
+// row from the previous copies, and the warp's ELL entries are staged two
+// iterations ahead (their column indices address those copies), so a row's
+// memory latency overlaps the previous row's arithmetic.  MODE STEP_FIRST:
+// a_1 = H~ a_0 with the FP64 dots mu_0 = <a_0|a_0> and <a_1|a_0>;
+// STEP_RECUR: a_{n+1} = 2 H~ a_n - a_{n-1} with the compensated dots
+// <a_n|a_n>, <a_n+1|a_n>.
+//
+// Per vector, P = sum hr (xr, xi) and Q = sum hi (xr, xi) (the diagonal
+// shift and -a_{n-1} go into P) are anchored compensated sums, so
+// re = P.x - Q.y and im = P.y + Q.x recombine exactly: both anchored sums
+// lie in the anchor's binade, their difference is exact (Sterbenz) and the
+// sum of their offsets from the anchor fits in 24 bits.
 template <int K, int MODE>
-__global__ void __launch_bounds__(STEP_THREADS)
+__global__ void __launch_bounds__(HiloCfg<K>::THREADS)
 cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
                       const int32_t* __restrict__ eidx,
                       const float2* __restrict__ eval) {
-  constexpr int SW = 8;
-  constexpr int VPL = 2;
-  constexpr int G = SW * VPL;
-  constexpr int KQ = K / 4;
-  constexpr int SPW = 32 / SW;
-  constexpr int NSLOT = STEP_THREADS / SW;
-  constexpr int FLUSH = 32;
-  const int lane = threadIdx.x & (SW - 1);
-  const int slot = threadIdx.x / SW;
-  const int wq = slot / SPW, half = slot % SPW, wl = threadIdx.x & 31;
-  __shared__ double red[NSLOT][G * 3];
-  __shared__ __align__(16) int32_t sidx[STEP_THREADS / 32][2][SPW * K];
-  __shared__ __align__(16) float2 sval[STEP_THREADS / 32][2][SPW * K];
+  using Cfg = HiloCfg<K>;
+  constexpr int T = Cfg::THREADS, ITEMS = Cfg::ITEMS, NSLOT = Cfg::NSLOT;
+  constexpr int SW = 8, G = 16, SPW = 4, FLUSH = 32;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float4* vhi = reinterpret_cast<float4*>(smem);              // [2][ITEMS][T]
+  uint2* vlo = reinterpret_cast<uint2*>(vhi + 2 * ITEMS * T);  // [2][ITEMS][T]
+  int32_t* sidx = reinterpret_cast<int32_t*>(vlo + 2 * ITEMS * T);
+  float2* sval = reinterpret_cast<float2*>(sidx + Cfg::NW * 3 * 4 * K);
+  double* red = reinterpret_cast<double*>(sval + Cfg::NW * 3 * 4 * K);
+
+  const int tid = threadIdx.x;
+  const int lane = tid & (SW - 1);
+  const int slot = tid / SW;
+  const int wq = slot / SPW, half = slot % SPW, wl = tid & 31;
+  int32_t* widx = sidx + wq * 3 * 4 * K;   // this warp's ring: [3][SPW * K]
+  float2* wval = sval + wq * 3 * 4 * K;
 
   const float4* __restrict__ x = reinterpret_cast<const float4*>(p.x);
   const float4* prev = reinterpret_cast<const float4*>(p.prev);
@@ -120,20 +169,41 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
   const int work = p.xitems * p.groups;
   const int rows = (int)p.rows;
   const int stride = p.xitems * NSLOT;
-  const float shift = p.shift;
+  const float2 shift = f2(p.shift);
   const float C = HILO_ANCHOR;
 
-  auto stage = [&](int r0, int b) {
+  // ELL entries of the warp's rows r0 .. r0 + 3 into ring buffer b
+  auto stage_ell = [&](int r0, int b) {
     constexpr int IC = SPW * K / 4, VC = SPW * K / 2;
     for (int c = wl; c < IC + VC; c += 32) {
       if (c < IC) {
         if (r0 + (4 * c) / K < rows)
-          cp_async16(&sidx[wq][b][4 * c], eidx + (int64_t)r0 * K + 4 * c);
+          cp_async16(widx + b * 4 * K + 4 * c, eidx + (int64_t)r0 * K + 4 * c);
       } else {
         const int e = c - IC;
         if (r0 + (2 * e) / K < rows)
-          cp_async16(&sval[wq][b][2 * e], eval + (int64_t)r0 * K + 2 * e);
+          cp_async16(wval + b * 4 * K + 2 * e, eval + (int64_t)r0 * K + 2 * e);
       }
+    }
+  };
+  // this thread's slices of row r (ELL entries in ring buffer eb) into
+  // vector buffer vb
+  auto stage_vec = [&](int r, int vb, int eb, int col) {
+    if (r >= rows) return;
+    float4* dh = vhi + vb * ITEMS * T + tid;
+    uint2* dl = vlo + vb * ITEMS * T + tid;
+    cp_async16(dh, x + (int64_t)r * p.rp + col);
+    cp_async8(dl, xl + (int64_t)r * q.lrp + col);
+    if constexpr (MODE == STEP_RECUR) {
+      cp_async16(dh + T, prev + (int64_t)r * p.rp + col);
+      cp_async8(dl + T, pl + (int64_t)r * q.lrp + col);
+    }
+    const int32_t* ci = widx + eb * 4 * K + half * K;
+#pragma unroll
+    for (int t = 0; t < K; ++t) {
+      const int64_t c = ci[t];
+      cp_async16(dh + (2 + t) * T, x + c * p.rp + col);
+      cp_async8(dl + (2 + t) * T, xl + c * q.lrp + col);
     }
   };
 
@@ -141,122 +211,123 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
     const int xi = w / p.groups;
     const int g = w - xi * p.groups;
     const int col = g * SW + lane;
-    double* my = &red[slot][lane * VPL * 3];
+    double* my = red + slot * (G * 3) + lane * 6;   // vectors 2 lane, +1
 #pragma unroll
-    for (int e = 0; e < VPL * 3; ++e) my[e] = 0.0;
-    // compensated FP32 dot accumulators (STEP_RECUR)
-    float sn[VPL], cn[VPL], sr[VPL], cr[VPL], fi[VPL];
+    for (int e = 0; e < 6; ++e) my[e] = 0.0;
+    // compensated FP32 dots (STEP_RECUR): <a_n|a_n> as (xr^2, xi^2) sums,
+    // Re <a_n+1|a_n> as (or xr, oi xi) sums, Im plain
+    float2 dns[2], dnc[2], drs[2], drc[2];
+    float fim[2];
 #pragma unroll
-    for (int k = 0; k < VPL; ++k) sn[k] = cn[k] = sr[k] = cr[k] = fi[k] = 0.f;
+    for (int k = 0; k < 2; ++k) {
+      dns[k] = dnc[k] = drs[k] = drc[k] = make_float2(0.f, 0.f);
+      fim[k] = 0.f;
+    }
     int pending = 0;
 
     const int wb0 = xi * NSLOT + SPW * wq;
-    if (wb0 < rows) stage(wb0, 0);
+    stage_ell(wb0, 0);
     cp_async_commit();
-    int sb = 0;
-    for (int wb = wb0; wb < rows; wb += stride) {
-      if (wb + stride < rows) stage(wb + stride, sb ^ 1);
+    stage_ell(wb0 + stride, 1);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncwarp();
+    stage_vec(wb0 + half, 0, 0, col);
+    cp_async_commit();
+    int it = 0;
+    for (int wb = wb0; wb < rows; wb += stride, ++it) {
+      const int e0 = it % 3, e1 = (it + 1) % 3, e2 = (it + 2) % 3;
+      const int vb = it & 1;
+      stage_ell(wb + 2 * stride, e2);
       cp_async_commit();
-      cp_async_wait_prev();
+      // pending groups: ELL(it + 1), vectors(it), ELL(it + 2)
+      cp_async_wait<1>();
       __syncwarp();
-      const int64_t r = wb + half;
+      stage_vec(wb + stride + half, vb ^ 1, e1, col);
+      cp_async_commit();
+      const int r = wb + half;
       if (r < rows) {
-        const float4 xv = x[r * p.rp + col];
-        const uint2 xlv = xl[r * q.lrp + col];
-        float4 pv = make_float4(0.f, 0.f, 0.f, 0.f);
-        uint2 plv = make_uint2(0u, 0u);
+        const float4* sh = vhi + vb * ITEMS * T + tid;
+        const uint2* sl = vlo + vb * ITEMS * T + tid;
+        const float4 xo = sh[0];
+        const uint2 xol = sl[0];
+        const float2 xk[2] = {make_float2(xo.x, xo.y),
+                              make_float2(xo.z, xo.w)};
+        const uint32_t xlw[2] = {xol.x, xol.y};
+        float2 Ps[2], Pc[2], Qs[2], Qc[2], LP[2], LQ[2];
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+          Ps[k] = Qs[k] = f2(C);
+          Pc[k] = Qc[k] = LQ[k] = make_float2(0.f, 0.f);
+          acc_fma(Ps[k], Pc[k], shift, xk[k]);
+          LP[k] = __fmul2_rn(shift, lo_pair(xlw[k]));
+        }
+        const float2* hv = wval + e0 * 4 * K + half * K;
+#pragma unroll
+        for (int t = 0; t < K; ++t) {
+          const float2 h = hv[t];
+          const float2 hr = f2(h.x), hi = f2(h.y);
+          const float4 gx = sh[(2 + t) * T];
+          const uint2 gl = sl[(2 + t) * T];
+          const float2 gk[2] = {make_float2(gx.x, gx.y),
+                                make_float2(gx.z, gx.w)};
+          const uint32_t glw[2] = {gl.x, gl.y};
+#pragma unroll
+          for (int k = 0; k < 2; ++k) {
+            acc_fma(Ps[k], Pc[k], hr, gk[k]);
+            acc_fma(Qs[k], Qc[k], hi, gk[k]);
+            const float2 l = lo_pair(glw[k]);
+            LP[k] = __ffma2_rn(hr, l, LP[k]);
+            LQ[k] = __ffma2_rn(hi, l, LQ[k]);
+          }
+        }
         if constexpr (MODE == STEP_RECUR) {
-          pv = prev[r * p.rp + col];
-          plv = pl[r * q.lrp + col];
+          const float4 pv = sh[T];
+          const uint2 plv = sl[T];
+          const float2 pk[2] = {make_float2(pv.x, pv.y),
+                                make_float2(pv.z, pv.w)};
+          const uint32_t plw[2] = {plv.x, plv.y};
+#pragma unroll
+          for (int k = 0; k < 2; ++k) {
+            acc_sub(Ps[k], Pc[k], pk[k]);
+            LP[k] = sub2(LP[k], lo_pair(plw[k]));
+          }
         }
-        const int4* ri =
-            reinterpret_cast<const int4*>(&sidx[wq][sb][half * K]);
-        const float4* rv =
-            reinterpret_cast<const float4*>(&sval[wq][sb][half * K]);
-        const float xr[2] = {xv.x, xv.z}, xim[2] = {xv.y, xv.w};
-        const uint32_t xw[2] = {xlv.x, xlv.y};
-        float s_r[2], c_r[2], s_i[2], c_i[2], l_r[2], l_i[2];
+        float2 ohi[2];
+        uint32_t olw[2];
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
-          s_r[k] = s_i[k] = C;
-          c_r[k] = c_i[k] = 0.f;
-          acc_fma(s_r[k], c_r[k], shift, xr[k]);
-          acc_fma(s_i[k], c_i[k], shift, xim[k]);
-          l_r[k] = __fmul_rn(shift, bf_re(xw[k]));
-          l_i[k] = __fmul_rn(shift, bf_im(xw[k]));
+          // v = (re, im) of the anchored sums (exact), cc = their
+          // compensation plus the lo bracket
+          const float2 v = make_float2(
+              __fsub_rn(Ps[k].x, Qs[k].y),
+              __fadd_rn(__fsub_rn(Ps[k].y, C), __fsub_rn(Qs[k].x, C)));
+          const float2 cc = make_float2(
+              __fadd_rn(__fsub_rn(Pc[k].x, Qc[k].y),
+                        __fsub_rn(LP[k].x, LQ[k].y)),
+              __fadd_rn(__fadd_rn(Pc[k].y, Qc[k].x),
+                        __fadd_rn(LP[k].y, LQ[k].x)));
+          float2 h = __fadd2_rn(v, cc);                 // hi = RN(v)
+          float2 l = __fadd2_rz(sub2(v, h), cc);        // lo = RZ(v - hi)
+          if constexpr (MODE == STEP_FIRST) {           // a_1 = (2 H~ a_0) / 2
+            h = __fmul2_rn(h, f2(0.5f));
+            l = __fmul2_rn(l, f2(0.5f));
+          }
+          ohi[k] = h;
+          olw[k] = lo_pack_rz(l);
         }
-#pragma unroll
-        for (int qq = 0; qq < KQ; ++qq) {
-          const int4 c4 = ri[qq];
-          const float4 h01 = rv[2 * qq], h23 = rv[2 * qq + 1];
-          const int cc[4] = {c4.x, c4.y, c4.z, c4.w};
-          const float hr[4] = {h01.x, h01.z, h23.x, h23.z};
-          const float hi[4] = {h01.y, h01.w, h23.y, h23.w};
-          float4 xx[4];
-          uint2 xxl[4];
-#pragma unroll
-          for (int t = 0; t < 4; ++t) {
-            xx[t] = x[(int64_t)cc[t] * p.rp + col];
-            xxl[t] = xl[(int64_t)cc[t] * q.lrp + col];
-          }
-#pragma unroll
-          for (int t = 0; t < 4; ++t) {
-            const float gr[2] = {xx[t].x, xx[t].z};
-            const float gi[2] = {xx[t].y, xx[t].w};
-            const uint32_t gw[2] = {xxl[t].x, xxl[t].y};
-#pragma unroll
-            for (int k = 0; k < 2; ++k) {
-              acc_fma(s_r[k], c_r[k], hr[t], gr[k]);
-              acc_fma(s_r[k], c_r[k], -hi[t], gi[k]);
-              acc_fma(s_i[k], c_i[k], hr[t], gi[k]);
-              acc_fma(s_i[k], c_i[k], hi[t], gr[k]);
-              const float lr = bf_re(gw[k]), li = bf_im(gw[k]);
-              l_r[k] = __fmaf_rn(hr[t], lr, __fmaf_rn(-hi[t], li, l_r[k]));
-              l_i[k] = __fmaf_rn(hr[t], li, __fmaf_rn(hi[t], lr, l_i[k]));
-            }
-          }
-        }
-        float orr[2], oii[2], olr[2], oli[2];
-#pragma unroll
-        for (int k = 0; k < 2; ++k) {
-          if constexpr (MODE == STEP_RECUR) {
-            const float pr[2] = {pv.x, pv.z}, pim[2] = {pv.y, pv.w};
-            const uint32_t pw[2] = {plv.x, plv.y};
-            acc_sub(s_r[k], c_r[k], pr[k]);
-            acc_sub(s_i[k], c_i[k], pim[k]);
-            l_r[k] = __fsub_rn(l_r[k], bf_re(pw[k]));
-            l_i[k] = __fsub_rn(l_i[k], bf_im(pw[k]));
-          }
-          // v = (s - C) + (c + l): hi = RN(v), lo = RZ(v - hi)
-          const float v0r = __fsub_rn(s_r[k], C), v0i = __fsub_rn(s_i[k], C);
-          const float tr = __fadd_rn(c_r[k], l_r[k]);
-          const float ti = __fadd_rn(c_i[k], l_i[k]);
-          float hr_ = __fadd_rn(v0r, tr), hi_ = __fadd_rn(v0i, ti);
-          float lr_ = __fadd_rz(__fsub_rn(v0r, hr_), tr);
-          float li_ = __fadd_rz(__fsub_rn(v0i, hi_), ti);
-          if constexpr (MODE == STEP_FIRST) {  // a_1 = (2 H~ a_0) / 2
-            hr_ *= 0.5f;
-            hi_ *= 0.5f;
-            lr_ *= 0.5f;
-            li_ *= 0.5f;
-          }
-          orr[k] = hr_;
-          oii[k] = hi_;
-          olr[k] = lr_;
-          oli[k] = li_;
-        }
-        const uint32_t ow[2] = {bf_pack_rz(olr[0], oli[0]),
-                                bf_pack_rz(olr[1], oli[1])};
-        out[r * p.rp + col] = make_float4(orr[0], oii[0], orr[1], oii[1]);
-        ol[r * q.lrp + col] = make_uint2(ow[0], ow[1]);
+        out[(int64_t)r * p.rp + col] =
+            make_float4(ohi[0].x, ohi[0].y, ohi[1].x, ohi[1].y);
+        ol[(int64_t)r * q.lrp + col] = make_uint2(olw[0], olw[1]);
         if constexpr (MODE == STEP_FIRST) {
           // mu_0 and <a_1|a_0> in FP64 from hi + lo
 #pragma unroll
           for (int k = 0; k < 2; ++k) {
-            const double ar = (double)xr[k] + (double)bf_re(xw[k]);
-            const double ai = (double)xim[k] + (double)bf_im(xw[k]);
-            const double br = (double)orr[k] + (double)bf_re(ow[k]);
-            const double bi = (double)oii[k] + (double)bf_im(ow[k]);
+            const float2 al = lo_pair(xlw[k]), bl = lo_pair(olw[k]);
+            const double ar = (double)xk[k].x + (double)al.x;
+            const double ai = (double)xk[k].y + (double)al.y;
+            const double br = (double)ohi[k].x + (double)bl.x;
+            const double bi = (double)ohi[k].y + (double)bl.y;
             my[k * 3 + 0] += ar * ar + ai * ai;
             my[k * 3 + 1] += br * ar + bi * ai;
             my[k * 3 + 2] += br * ai - bi * ar;
@@ -264,42 +335,45 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
         } else {
 #pragma unroll
           for (int k = 0; k < 2; ++k) {
-            dot2(sn[k], cn[k], xr[k], xr[k]);
-            dot2(sn[k], cn[k], xim[k], xim[k]);
-            dot2(sr[k], cr[k], orr[k], xr[k]);
-            dot2(sr[k], cr[k], oii[k], xim[k]);
-            fi[k] = fmaf(orr[k], xim[k], fmaf(-oii[k], xr[k], fi[k]));
+            dot2(dns[k], dnc[k], xk[k], xk[k]);
+            dot2(drs[k], drc[k], ohi[k], xk[k]);
+            fim[k] = fmaf(ohi[k].x, xk[k].y, fmaf(-ohi[k].y, xk[k].x, fim[k]));
           }
           if (++pending == FLUSH) {
 #pragma unroll
             for (int k = 0; k < 2; ++k) {
-              my[k * 3 + 0] += (double)sn[k] + (double)cn[k];
-              my[k * 3 + 1] += (double)sr[k] + (double)cr[k];
-              my[k * 3 + 2] += (double)fi[k];
-              sn[k] = cn[k] = sr[k] = cr[k] = fi[k] = 0.f;
+              my[k * 3 + 0] += ((double)dns[k].x + (double)dns[k].y) +
+                               ((double)dnc[k].x + (double)dnc[k].y);
+              my[k * 3 + 1] += ((double)drs[k].x + (double)drs[k].y) +
+                               ((double)drc[k].x + (double)drc[k].y);
+              my[k * 3 + 2] += (double)fim[k];
+              dns[k] = dnc[k] = drs[k] = drc[k] = make_float2(0.f, 0.f);
+              fim[k] = 0.f;
             }
             pending = 0;
           }
         }
       }
       __syncwarp();
-      sb ^= 1;
     }
+    cp_async_wait<0>();
     if constexpr (MODE == STEP_RECUR) {
 #pragma unroll
       for (int k = 0; k < 2; ++k) {
-        my[k * 3 + 0] += (double)sn[k] + (double)cn[k];
-        my[k * 3 + 1] += (double)sr[k] + (double)cr[k];
-        my[k * 3 + 2] += (double)fi[k];
+        my[k * 3 + 0] += ((double)dns[k].x + (double)dns[k].y) +
+                         ((double)dnc[k].x + (double)dnc[k].y);
+        my[k * 3 + 1] += ((double)drs[k].x + (double)drs[k].y) +
+                         ((double)drc[k].x + (double)drc[k].y);
+        my[k * 3 + 2] += (double)fim[k];
       }
     }
     __syncthreads();
     // partials are addressed by vector: [vector*3 + component][xitems]
     double* dst = p.partials + (int64_t)g * (G * 3) * p.xitems + xi;
-    for (int e = threadIdx.x; e < G * 3; e += blockDim.x) {
+    for (int e = tid; e < G * 3; e += T) {
       double s = 0.0;
 #pragma unroll
-      for (int sl = 0; sl < NSLOT; ++sl) s += red[sl][e];
+      for (int sl = 0; sl < NSLOT; ++sl) s += red[sl * (G * 3) + e];
       dst[(int64_t)e * p.xitems] = s;
     }
     __syncthreads();
@@ -309,11 +383,15 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
 template <int K, int MODE>
 static int launch_hilo_t(kpm_handle* h, const StepArgs& a,
                          const HiloArgs& q) {
+  using Cfg = HiloCfg<K>;
   static int occ = -1;
   if (occ < 0) {
+    KPM_CUDA(cudaFuncSetAttribute(cheb_step_hilo_kernel<K, MODE>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)Cfg::SMEM));
     int blocks = 0;
     KPM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &blocks, cheb_step_hilo_kernel<K, MODE>, STEP_THREADS, 0));
+        &blocks, cheb_step_hilo_kernel<K, MODE>, Cfg::THREADS, Cfg::SMEM));
     occ = blocks > 0 ? blocks : 1;
   }
   const int64_t work = (int64_t)a.xitems * a.groups;
@@ -332,8 +410,8 @@ static int launch_hilo_t(kpm_handle* h, const StepArgs& a,
     KPM_CUDA(cudaEventRecord(e0, h->stream));
   }
   cheb_step_hilo_kernel<K, MODE>
-      <<<(unsigned)grid, STEP_THREADS, 0, h->stream>>>(a, q, h->H.ell_idx,
-                                                        h->H.ell_val);
+      <<<(unsigned)grid, Cfg::THREADS, Cfg::SMEM, h->stream>>>(
+          a, q, h->H.ell_idx, h->H.ell_val);
   count_launch(1);
   KPM_CHECK_LAUNCH();
   if (e1) KPM_CUDA(cudaEventRecord(e1, h->stream));

@@ -139,6 +139,16 @@ def test_rmt_call_and_integrate(kpm):
     assert abs(sd.integrate() - g['integrate']) < 1e-10
     f = sd.integrate(lambda e: kpm.fermi_distribution(e, 0.1, 0.05))
     assert abs(f - g['integrate_fermi']) < 1e-10
+    # the batched device sweep: the same sums for a grid of (mu, T)
+    grid = sd.integrate_sweep(mu=[[0.1], [-0.3]], temperature=[0.05, 0.0])
+    assert grid.shape == (2, 2)
+    assert abs(grid[0, 0] - g['integrate_fermi']) < 1e-10
+    for i, m in enumerate((0.1, -0.3)):
+        for j, T in enumerate((0.05, 0.0)):
+            ref = sd.integrate(lambda e: kpm.fermi_distribution(e, m, T))
+            assert abs(grid[i, j] - ref) < 1e-13 * max(1.0, abs(ref))
+    with pytest.raises(ValueError):
+        sd.integrate_sweep(0.0, -1.0)
 
 
 def test_custom_kernel_runs_on_host_values(kpm):
