@@ -133,6 +133,14 @@ struct kpm_handle {
   // complex64 element and step with the compensated kernel (cleared by
   // KPM_FLAG_PLAIN_C64; needs the complex64 ELL copy)
   bool compensated = false;
+  // compensated DOS: ELL copy with every row's diagonal entry first and the
+  // diagonal shift -2b/a folded into it (rebuilt on the device by each DOS
+  // call); dg_ok: every row had a real diagonal entry (else the general
+  // compensated kernel runs)
+  int32_t* dg_idx = nullptr;
+  float2* dg_val = nullptr;
+  int* dg_flag = nullptr;
+  bool dg_ok = false;
   int device = 0;
   int num_sms = 0;
   double a = 1.0, b = 0.0;

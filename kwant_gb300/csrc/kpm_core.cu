@@ -1195,6 +1195,9 @@ int kpm_destroy(kpm_handle* h) {
   dev_free(h->vec_staging, h->stream);
   dev_free(h->partials, h->stream);
   dev_free(h->perm, h->stream);
+  dev_free(h->dg_idx, h->stream);
+  dev_free(h->dg_val, h->stream);
+  dev_free(h->dg_flag, h->stream);
   if (h->ev_start) cudaEventDestroy(h->ev_start);
   if (h->ev_stop) cudaEventDestroy(h->ev_stop);
   for (cudaEvent_t e : h->prof_events) cudaEventDestroy(e);
@@ -1455,6 +1458,7 @@ int kpm_block_dos_moments(kpm_block* b, int64_t m_start, int64_t m_end,
   };
   // compensated blocks: hi + lo vectors and error-free steps
   const bool hilo = b->lo_a0 != nullptr;
+  if (st == KPM_OK && hilo) st = prepare_hilo(h);
   if (st == KPM_OK && m_start == 0) {
     st = hilo ? block_advance_hilo(b) : block_advance(b, true);
     if (st == KPM_OK) st = finalize(b, STEP_FIRST, mom, slot(0), slot(1));

@@ -98,6 +98,9 @@ int launch_step_ell(kpm_handle* h, int mode, bool dots, const StepArgs& a,
 // compensated DOS step on a hi + lo block (complex64 ELL handle), dots fused
 int launch_step_hilo(kpm_handle* h, int mode, const StepArgs& a,
                      const HiloArgs& q);
+// (re)build the handle's diagonal-first ELL copy for the compensated step
+// from its current complex64 ELL values
+int prepare_hilo(kpm_handle* h);
 StepArgs step_args(kpm_block* b, const void* x, const void* prev, void* out);
 int block_advance(kpm_block* b, bool dots);
 // block_advance without dot products that also writes the store row of the

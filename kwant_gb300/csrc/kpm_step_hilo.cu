@@ -102,17 +102,30 @@ __device__ __forceinline__ void cp_async8(void* dst, const void* src) {
                "l"(src)
                : "memory");
 }
+// 16-byte asynchronous global -> shared copy through L1 (gathered rows:
+// the rows of a warp share neighbours)
+__device__ __forceinline__ void cp_async16_ca(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(
+                   static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
+               "l"(src)
+               : "memory");
+}
 template <int N>
 __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-// Block size by ELL width: each thread stages a row's own x, alpha_{n-1}
-// and K gathered rows (24 bytes each, hi and lo), double-buffered; the
-// block must leave room for two or three blocks per SM.
-template <int K> struct HiloCfg {
+// Block size by ELL width: each thread stages a row's own x (unless it is
+// the first gathered row, D0), alpha_{n-1} and K gathered rows (24 bytes
+// each, hi and lo), double-buffered; the block must leave room for two or
+// three blocks per SM.
+template <int K, bool D0> struct HiloCfg {
   static constexpr int THREADS = K <= 4 ? 256 : (K <= 12 ? 128 : 64);
-  static constexpr int ITEMS = K + 2;
+  static constexpr int ITEMS = K + (D0 ? 1 : 2);
+  // staged item indices: the row's own x, alpha_{n-1}, first gathered row
+  static constexpr int OWN = D0 ? 1 : 0;
+  static constexpr int PREV = D0 ? 0 : 1;
+  static constexpr int GATH = D0 ? 1 : 2;
   static constexpr int NW = THREADS / 32;
   static constexpr int NSLOT = THREADS / 8;
   static constexpr size_t SMEM =
@@ -138,12 +151,17 @@ template <int K> struct HiloCfg {
 // re = P.x - Q.y and im = P.y + Q.x recombine exactly: both anchored sums
 // lie in the anchor's binade, their difference is exact (Sterbenz) and the
 // sum of their offsets from the anchor fits in 24 bits.
-template <int K, int MODE>
-__global__ void __launch_bounds__(HiloCfg<K>::THREADS)
+//
+// D0: the ELL rows hold the diagonal entry first, with the shift folded in
+// and a zero imaginary part (prepare_hilo); the own x is then the first
+// gathered row, and the diagonal contributes to P only.
+template <int K, int MODE, bool D0>
+__global__ void __launch_bounds__(HiloCfg<K, D0>::THREADS)
 cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
                       const int32_t* __restrict__ eidx,
                       const float2* __restrict__ eval) {
-  using Cfg = HiloCfg<K>;
+  using Cfg = HiloCfg<K, D0>;
+  constexpr int OWN = Cfg::OWN, PREV = Cfg::PREV, GATH = Cfg::GATH;
   constexpr int T = Cfg::THREADS, ITEMS = Cfg::ITEMS, NSLOT = Cfg::NSLOT;
   constexpr int SW = 8, G = 16, SPW = 4, FLUSH = 32;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -170,6 +188,12 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
   const int rows = (int)p.rows;
   const int stride = p.xitems * NSLOT;
   const float2 shift = f2(p.shift);
+  // lane payloads per row, the same for the hi (float4) and lo (uint2)
+  // arrays: element offsets are one 32 x 32 -> 64-bit multiply per row
+  const uint32_t rp = (uint32_t)p.rp;
+  auto off = [rp](int row, int col) -> int64_t {
+    return (int64_t)((uint64_t)(uint32_t)row * rp) + col;
+  };
   const float C = HILO_ANCHOR;
 
   // ELL entries of the warp's rows r0 .. r0 + 3 into ring buffer b
@@ -192,18 +216,21 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
     if (r >= rows) return;
     float4* dh = vhi + vb * ITEMS * T + tid;
     uint2* dl = vlo + vb * ITEMS * T + tid;
-    cp_async16(dh, x + (int64_t)r * p.rp + col);
-    cp_async8(dl, xl + (int64_t)r * q.lrp + col);
+    const int64_t o = off(r, col);
+    if constexpr (!D0) {
+      cp_async16(dh + OWN * T, x + o);
+      cp_async8(dl + OWN * T, xl + o);
+    }
     if constexpr (MODE == STEP_RECUR) {
-      cp_async16(dh + T, prev + (int64_t)r * p.rp + col);
-      cp_async8(dl + T, pl + (int64_t)r * q.lrp + col);
+      cp_async16(dh + PREV * T, prev + o);
+      cp_async8(dl + PREV * T, pl + o);
     }
     const int32_t* ci = widx + eb * 4 * K + half * K;
 #pragma unroll
     for (int t = 0; t < K; ++t) {
-      const int64_t c = ci[t];
-      cp_async16(dh + (2 + t) * T, x + c * p.rp + col);
-      cp_async8(dl + (2 + t) * T, xl + c * q.lrp + col);
+      const int64_t oc = off(ci[t], col);
+      cp_async16_ca(dh + (GATH + t) * T, x + oc);
+      cp_async8(dl + (GATH + t) * T, xl + oc);
     }
   };
 
@@ -234,10 +261,8 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
     __syncwarp();
     stage_vec(wb0 + half, 0, 0, col);
     cp_async_commit();
-    int it = 0;
-    for (int wb = wb0; wb < rows; wb += stride, ++it) {
-      const int e0 = it % 3, e1 = (it + 1) % 3, e2 = (it + 2) % 3;
-      const int vb = it & 1;
+    int e0 = 0, e1 = 1, e2 = 2, vb = 0;   // ring positions of rows it, +1, +2
+    for (int wb = wb0; wb < rows; wb += stride) {
       stage_ell(wb + 2 * stride, e2);
       cp_async_commit();
       // pending groups: ELL(it + 1), vectors(it), ELL(it + 2)
@@ -249,8 +274,8 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
       if (r < rows) {
         const float4* sh = vhi + vb * ITEMS * T + tid;
         const uint2* sl = vlo + vb * ITEMS * T + tid;
-        const float4 xo = sh[0];
-        const uint2 xol = sl[0];
+        const float4 xo = sh[OWN * T];
+        const uint2 xol = sl[OWN * T];
         const float2 xk[2] = {make_float2(xo.x, xo.y),
                               make_float2(xo.z, xo.w)};
         const uint32_t xlw[2] = {xol.x, xol.y};
@@ -259,31 +284,37 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
         for (int k = 0; k < 2; ++k) {
           Ps[k] = Qs[k] = f2(C);
           Pc[k] = Qc[k] = LQ[k] = make_float2(0.f, 0.f);
-          acc_fma(Ps[k], Pc[k], shift, xk[k]);
-          LP[k] = __fmul2_rn(shift, lo_pair(xlw[k]));
+          if constexpr (D0) {
+            LP[k] = make_float2(0.f, 0.f);
+          } else {
+            acc_fma(Ps[k], Pc[k], shift, xk[k]);
+            LP[k] = __fmul2_rn(shift, lo_pair(xlw[k]));
+          }
         }
         const float2* hv = wval + e0 * 4 * K + half * K;
 #pragma unroll
         for (int t = 0; t < K; ++t) {
           const float2 h = hv[t];
           const float2 hr = f2(h.x), hi = f2(h.y);
-          const float4 gx = sh[(2 + t) * T];
-          const uint2 gl = sl[(2 + t) * T];
+          const float4 gx = sh[(GATH + t) * T];
+          const uint2 gl = sl[(GATH + t) * T];
           const float2 gk[2] = {make_float2(gx.x, gx.y),
                                 make_float2(gx.z, gx.w)};
           const uint32_t glw[2] = {gl.x, gl.y};
 #pragma unroll
           for (int k = 0; k < 2; ++k) {
             acc_fma(Ps[k], Pc[k], hr, gk[k]);
-            acc_fma(Qs[k], Qc[k], hi, gk[k]);
             const float2 l = lo_pair(glw[k]);
             LP[k] = __ffma2_rn(hr, l, LP[k]);
-            LQ[k] = __ffma2_rn(hi, l, LQ[k]);
+            if (!D0 || t > 0) {    // a D0 row's first entry is real
+              acc_fma(Qs[k], Qc[k], hi, gk[k]);
+              LQ[k] = __ffma2_rn(hi, l, LQ[k]);
+            }
           }
         }
         if constexpr (MODE == STEP_RECUR) {
-          const float4 pv = sh[T];
-          const uint2 plv = sl[T];
+          const float4 pv = sh[PREV * T];
+          const uint2 plv = sl[PREV * T];
           const float2 pk[2] = {make_float2(pv.x, pv.y),
                                 make_float2(pv.z, pv.w)};
           const uint32_t plw[2] = {plv.x, plv.y};
@@ -316,9 +347,9 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
           ohi[k] = h;
           olw[k] = lo_pack_rz(l);
         }
-        out[(int64_t)r * p.rp + col] =
-            make_float4(ohi[0].x, ohi[0].y, ohi[1].x, ohi[1].y);
-        ol[(int64_t)r * q.lrp + col] = make_uint2(olw[0], olw[1]);
+        const int64_t o = off(r, col);
+        out[o] = make_float4(ohi[0].x, ohi[0].y, ohi[1].x, ohi[1].y);
+        ol[o] = make_uint2(olw[0], olw[1]);
         if constexpr (MODE == STEP_FIRST) {
           // mu_0 and <a_1|a_0> in FP64 from hi + lo
 #pragma unroll
@@ -355,6 +386,11 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
         }
       }
       __syncwarp();
+      const int e_old = e0;
+      e0 = e1;
+      e1 = e2;
+      e2 = e_old;
+      vb ^= 1;
     }
     cp_async_wait<0>();
     if constexpr (MODE == STEP_RECUR) {
@@ -380,18 +416,19 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
   }
 }
 
-template <int K, int MODE>
+template <int K, int MODE, bool D0>
 static int launch_hilo_t(kpm_handle* h, const StepArgs& a,
                          const HiloArgs& q) {
-  using Cfg = HiloCfg<K>;
+  using Cfg = HiloCfg<K, D0>;
   static int occ = -1;
   if (occ < 0) {
-    KPM_CUDA(cudaFuncSetAttribute(cheb_step_hilo_kernel<K, MODE>,
+    KPM_CUDA(cudaFuncSetAttribute(cheb_step_hilo_kernel<K, MODE, D0>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)Cfg::SMEM));
     int blocks = 0;
     KPM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &blocks, cheb_step_hilo_kernel<K, MODE>, Cfg::THREADS, Cfg::SMEM));
+        &blocks, cheb_step_hilo_kernel<K, MODE, D0>, Cfg::THREADS,
+        Cfg::SMEM));
     occ = blocks > 0 ? blocks : 1;
   }
   const int64_t work = (int64_t)a.xitems * a.groups;
@@ -409,9 +446,9 @@ static int launch_hilo_t(kpm_handle* h, const StepArgs& a,
     h->prof_used += 2;
     KPM_CUDA(cudaEventRecord(e0, h->stream));
   }
-  cheb_step_hilo_kernel<K, MODE>
+  cheb_step_hilo_kernel<K, MODE, D0>
       <<<(unsigned)grid, Cfg::THREADS, Cfg::SMEM, h->stream>>>(
-          a, q, h->H.ell_idx, h->H.ell_val);
+          a, q, D0 ? h->dg_idx : h->H.ell_idx, D0 ? h->dg_val : h->H.ell_val);
   count_launch(1);
   KPM_CHECK_LAUNCH();
   if (e1) KPM_CUDA(cudaEventRecord(e1, h->stream));
@@ -421,8 +458,73 @@ static int launch_hilo_t(kpm_handle* h, const StepArgs& a,
 template <int K>
 static int dispatch_hilo_k(kpm_handle* h, int mode, const StepArgs& a,
                            const HiloArgs& q) {
-  return mode == STEP_FIRST ? launch_hilo_t<K, STEP_FIRST>(h, a, q)
-                            : launch_hilo_t<K, STEP_RECUR>(h, a, q);
+  if (h->dg_ok)
+    return mode == STEP_FIRST ? launch_hilo_t<K, STEP_FIRST, true>(h, a, q)
+                              : launch_hilo_t<K, STEP_RECUR, true>(h, a, q);
+  return mode == STEP_FIRST ? launch_hilo_t<K, STEP_FIRST, false>(h, a, q)
+                            : launch_hilo_t<K, STEP_RECUR, false>(h, a, q);
+}
+
+// Diagonal-first copy of the ELL rows: the first entry whose column is the
+// row (a CSR diagonal, or else the zero padding entry) moves to slot 0 with
+// the shift added to its value; the other entries keep their order.  *bad
+// is set when a row has no such entry or a diagonal with a nonzero
+// imaginary part.
+__global__ void diag_first_kernel(int64_t n, int K,
+                                  const int32_t* __restrict__ eidx,
+                                  const float2* __restrict__ eval,
+                                  float shift, int32_t* __restrict__ oidx,
+                                  float2* __restrict__ oval, int* bad) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int32_t* ri = eidx + r * K;
+  const float2* rv = eval + r * K;
+  int d = -1;
+  for (int t = 0; t < K; ++t)
+    if (ri[t] == (int32_t)r) {
+      d = t;
+      break;
+    }
+  if (d < 0 || rv[d].y != 0.f) {
+    atomicOr(bad, 1);
+    d = -1;
+  }
+  int o = 0;
+  if (d >= 0) {
+    oidx[r * K] = (int32_t)r;
+    oval[r * K] = make_float2(__fadd_rn(rv[d].x, shift), 0.f);
+    o = 1;
+  }
+  for (int t = 0; t < K; ++t) {
+    if (t == d) continue;
+    oidx[r * K + o] = ri[t];
+    oval[r * K + o] = rv[t];
+    ++o;
+  }
+}
+
+int prepare_hilo(kpm_handle* h) {
+  const int K = h->H.ell_k;
+  if (K == 0) return KPM_OK;
+  const int64_t n = h->H.rows;
+  const size_t cnt = (size_t)n * K;
+  if (!h->dg_idx) {
+    KPM_TRY(dev_alloc((void**)&h->dg_idx, cnt * sizeof(int32_t), h->stream));
+    KPM_TRY(dev_alloc((void**)&h->dg_val, cnt * sizeof(float2), h->stream));
+    KPM_TRY(dev_alloc((void**)&h->dg_flag, sizeof(int), h->stream));
+  }
+  KPM_CUDA(cudaMemsetAsync(h->dg_flag, 0, sizeof(int), h->stream));
+  diag_first_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, h->stream>>>(
+      n, K, h->H.ell_idx, h->H.ell_val, (float)(-2.0 * h->b / h->a),
+      h->dg_idx, h->dg_val, h->dg_flag);
+  count_launch(1);
+  KPM_CHECK_LAUNCH();
+  int bad = 0;
+  KPM_CUDA(cudaMemcpyAsync(&bad, h->dg_flag, sizeof(int),
+                           cudaMemcpyDeviceToHost, h->stream));
+  KPM_CUDA(cudaStreamSynchronize(h->stream));
+  h->dg_ok = bad == 0;
+  return KPM_OK;
 }
 
 // Every block runs as 16-vector sub-groups in 8-lane slots with two
@@ -443,7 +545,7 @@ int launch_step_hilo(kpm_handle* h, int mode, const StepArgs& a,
   w.rp = rpad / 2;
   w.groups = (int)(rpad / 16);
   HiloArgs wq = q;
-  wq.lrp = rpad / 2;
+  wq.lrp = rpad / 2;   // the kernel addresses lo with the hi stride
   switch (h->H.ell_k) {
     case 4: return dispatch_hilo_k<4>(h, mode, w, wq);
     case 8: return dispatch_hilo_k<8>(h, mode, w, wq);
