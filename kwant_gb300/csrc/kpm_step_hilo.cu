@@ -118,9 +118,10 @@ __device__ __forceinline__ void cp_async_wait() {
 // Block size by ELL width: each thread stages a row's own x (unless it is
 // the first gathered row, D0), alpha_{n-1} and K gathered rows (24 bytes
 // each, hi and lo), double-buffered; the block must leave room for two or
-// three blocks per SM.
+// three blocks per SM (K = 4: two blocks of 256, 78 KB each).
 template <int K, bool D0> struct HiloCfg {
   static constexpr int THREADS = K <= 4 ? 256 : (K <= 12 ? 128 : 64);
+  static constexpr int MIN_BLOCKS = K <= 4 ? 2 : 2;
   static constexpr int ITEMS = K + (D0 ? 1 : 2);
   // staged item indices: the row's own x, alpha_{n-1}, first gathered row
   static constexpr int OWN = D0 ? 1 : 0;
@@ -156,7 +157,8 @@ template <int K, bool D0> struct HiloCfg {
 // and a zero imaginary part (prepare_hilo); the own x is then the first
 // gathered row, and the diagonal contributes to P only.
 template <int K, int MODE, bool D0>
-__global__ void __launch_bounds__(HiloCfg<K, D0>::THREADS)
+__global__ void __launch_bounds__(HiloCfg<K, D0>::THREADS,
+                                  HiloCfg<K, D0>::MIN_BLOCKS)
 cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
                       const int32_t* __restrict__ eidx,
                       const float2* __restrict__ eval) {
@@ -234,6 +236,11 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
     }
   };
 
+  // partition-major work order: the sub-groups of a row partition run
+  // side by side (they share the partition's ELL rows in L2).  Measured on
+  // the 2e6-orbital graphene workload, R = 64: 1.08 ms per step against
+  // 1.12 ms sub-group-major; blocks of 192 or 160 threads (3 or 4 per SM)
+  // were slower still (1.15-1.22 ms)
   for (int w = blockIdx.x; w < work; w += gridDim.x) {
     const int xi = w / p.groups;
     const int g = w - xi * p.groups;
