@@ -158,9 +158,7 @@ class CpuBaseline:
         self.nnz = ham.nnz
         self.procs = procs
         self.vecs = vecs
-        ctx = mp.get_context('spawn')
-        self.pool = ctx.Pool(procs, initializer=_cpu_init,
-                             initargs=(self.tmp.name, a, b))
+        self.pool = _spawn_pool(procs, _cpu_init, (self.tmp.name, a, b))
 
     def run(self, M):
         t0 = time.perf_counter()
@@ -173,6 +171,25 @@ class CpuBaseline:
         self.pool.close()
         self.pool.join()
         os.unlink(self.tmp.name)
+
+
+def _spawn_pool(procs, init, initargs):
+    """A spawned process pool whose workers run single-threaded BLAS /
+    OpenMP (one process per core; many processes each with a threaded BLAS
+    oversubscribe the cores)."""
+    keys = ('OMP_NUM_THREADS', 'OPENBLAS_NUM_THREADS', 'MKL_NUM_THREADS')
+    old = {k: os.environ.get(k) for k in keys}
+    for k in keys:
+        os.environ[k] = '1'
+    try:
+        return mp.get_context('spawn').Pool(procs, initializer=init,
+                                            initargs=initargs)
+    finally:
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
 
 
 # ---------------------------------------------------------------- main arms
@@ -484,6 +501,11 @@ def run_ours(args):
             'cpu_baseline': cpu, 'e2e': e2e, 'gpu_launches': launches,
             'clocks': clk, 'accuracy': accuracy,
         }
+        if args.kubo and world == 1:
+            # the Kubo-Bastin workload at its default size, so that every
+            # default run measures it too (not part of this line's value)
+            line['kubo'] = kubo_record(args, 5, 3, cpu=args.cpu,
+                                       accuracy=args.accuracy)
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -589,12 +611,59 @@ def run_ldos(args):
     return 0
 
 
-def run_kubo(args):
-    """Kubo-Bastin workload (not the headline line): square 200 x 200, two
-    orbitals, t = 1, Rashba 0.3, exchange 0.2, W = 1 (seed 0), R = 16
-    vectors, M = 256 moments, sigma_xy.  One step = the device part of
-    conductivity(): both Chebyshev recursions with stored vectors and the
-    moments-matrix contraction on the tensor cores (BF16x3)."""
+# ------------------------------------------------------------ Kubo-Bastin
+_KW = {}
+
+
+def _kubo_cpu_init(path, lmin, lmax, M):
+    import scipy.sparse as sp
+    d = np.load(path)
+    mk = lambda k: sp.csr_matrix((d[k + '_data'], d[k + '_indices'],
+                                   d[k + '_indptr']), shape=tuple(d['shape']))
+    _KW.update(ham=mk('h'), vx=mk('vx'), vy=mk('vy'), lmin=lmin, lmax=lmax,
+               M=M)
+
+
+def _kubo_cpu_task(vec):
+    """The oracle port of kwant.kpm.conductivity's moments matrix
+    (Correlator, kwant/kpm.py:557-606 and :685-695) for one vector."""
+    from oracle import kpm_oracle as ko
+    t0 = time.perf_counter()
+    mu, _, _ = ko.correlator_moments_matrix(
+        _KW['ham'], [vec], _KW['lmin'], _KW['lmax'], _KW['M'], _KW['vx'],
+        _KW['vy'])
+    return mu, time.perf_counter() - t0
+
+
+def _sigma_grid(mu_mat, a, b, M, mus, temps):
+    """sigma_xy(mu, T) over a grid from a moments matrix, with this
+    package's device integral factor (kwant/kpm.py:720-760) and
+    Fermi-weighted Simpson sums (kwant/kpm.py:608-630)."""
+    from kwant_gb300 import _lib, kpm
+    g = np.asarray(kpm.jackson_kernel(np.ones(M)), dtype=float)
+    g[0] /= 2
+    nodes = kpm._chebyshev_nodes(2 * M)
+    factor = _lib.integral_factor(mu_mat, g, nodes)
+    w = (2 * 4 ** 2 / (2 * a) ** 2) * kpm._simpson_weights(nodes) / \
+        (1 - nodes ** 2) ** 2
+    mm, tt = np.meshgrid(mus, temps, indexing='ij')
+    out = _lib.fermi_sums(a * nodes + b, w, factor[:, None], mm.ravel(),
+                          tt.ravel())
+    return out.reshape(mm.shape)
+
+
+def _rel_linf(x, ref):
+    return float(np.max(np.abs(x - ref)) / np.max(np.abs(ref)))
+
+
+def kubo_record(args, steps, warmup, cpu=True, accuracy=True):
+    """Kubo-Bastin workload: square L x L, two orbitals, t = 1, Rashba 0.3,
+    exchange 0.2, W = 1 (seed 0), R vectors, M moments, sigma_xy.  A step is
+    the device part of conductivity(): both Chebyshev recursions with
+    stored vectors and the moments-matrix contraction on the tensor cores
+    (BF16x3).  Accuracy: sigma_xy on a (mu, T) grid against the FP64 path
+    (all R vectors) and against the oracle (the CPU sample's vectors); CPU
+    baseline: the oracle's moments matrix, one spawned process per vector."""
     import torch
     from kwant_gb300 import _lib, kpm, lattices
     L, R, M = args.kubo_l, args.kubo_vectors, args.kubo_moments
@@ -616,22 +685,24 @@ def run_kubo(args):
     cva, cvb = _lib.Csr(vx), _lib.Csr(vy)
     stream = torch.cuda.ExternalStream(h.stream())
 
-    def step():
-        return _lib.correlator_moments(h, a2, b2, cva, cvb, vecs, M, gemm=1)
+    def step(v=vecs, hd=h, gemm=1):
+        return _lib.correlator_moments(hd, a2, b2, cva, cvb, v, M, gemm=gemm)
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step()
     torch.cuda.synchronize()
+    launches0 = _lib.launch_count()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     gem = []
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         mu = step()
         gem.append(h.last_gemm())
     e1.record(stream)
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / args.steps
+    launches = _lib.launch_count() - launches0
+    ms = e0.elapsed_time(e1) / steps
     g_ms = float(np.median([g[0] for g in gem]))
     g_fl = gem[-1][1]
     peaks = {}
@@ -641,20 +712,13 @@ def run_kubo(args):
     tpeak = float(peaks.get('bf16_tflops', 1900.0))
     achieved = g_fl / (g_ms / 1e3) / 1e12
     complex_flops = 8.0 * R * M * M * n
-    mu64 = None
-    if args.accuracy:
-        h64 = _lib.Handle(ham, a, b, _lib.PREC_FP64)
-        mu64 = _lib.correlator_moments(h64, a2, b2, cva, cvb, vecs, M, gemm=0)
-        h64.close()
-    line = {
-        'metric': METRIC, 'value': 2 * nnz * R * M / (ms / 1e3), 'unit': UNIT,
-        'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup,
-        'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak',
-        'vs_baseline': None, 'dtype': 'c64 recursion + bf16x3 GEMM',
-        'data': 'synthetic',
-        'config': {'workload': 'kubo-bastin sigma_xy: rashba square %dx%d x2 '
-                               'orbitals, R=%d, M=%d' % (L, L, R, M),
-                   'nnz': int(nnz), 'orbitals': int(n)},
+    rec = {
+        'workload': 'kubo-bastin sigma_xy: rashba square %dx%d x2 orbitals, '
+                    'R=%d, M=%d' % (L, L, R, M),
+        'value': 2 * nnz * R * M / (ms / 1e3), 'unit': UNIT,
+        'ms_per_step': ms, 'nnz': int(nnz), 'orbitals': int(n),
+        'gpu_launches_per_step': launches / steps,
+        'dtype': 'c64 recursion + bf16x3 GEMM',
         'roofline': {'bound': 'tensor', 'achieved': achieved, 'peak': tpeak,
                      'unit': 'TFLOP/s', 'frac': achieved / tpeak,
                      # ncu dram bytes of one launch on the 60 x 60 x 2,
@@ -668,12 +732,84 @@ def run_kubo(args):
                          complex_flops / (g_ms / 1e3) / 1e12,
                      'peak_source': 'measured' if 'bf16_tflops' in peaks
                      else 'fallback'},
-        'accuracy': None if mu64 is None else {
-            'mu_rel_linf_vs_fp64': float(np.max(np.abs(mu - mu64)) /
-                                         np.max(np.abs(mu64)))},
+    }
+    mus = b + a * np.linspace(-0.8, 0.8, 17)
+    temps = np.array([0.05, 0.2])
+    if accuracy:
+        h64 = _lib.Handle(ham, a, b, _lib.PREC_FP64)
+        mu64 = step(hd=h64, gemm=0)
+        s_mixed = _sigma_grid(mu, a, b, M, mus, temps)
+        s_64 = _sigma_grid(mu64, a, b, M, mus, temps)
+        rec['accuracy'] = {
+            'mu_rel_linf_vs_fp64': _rel_linf(mu, mu64),
+            'sigma_xy_rel_linf_vs_fp64': _rel_linf(s_mixed, s_64),
+            'sigma_grid': '%d chemical potentials in b +- 0.8 a, T in %s'
+                          % (len(mus), temps.tolist()),
+            'reference': 'FP64 GPU path, all %d vectors' % R}
+    if cpu:
+        procs = min(args.cpu_procs or os.cpu_count() or 1, R)
+        tmp = tempfile.NamedTemporaryFile(suffix='.npz', delete=False)
+        tmp.close()
+        np.savez(tmp.name, shape=np.array(ham.shape),
+                 **{k + '_' + f: getattr(m, f) for k, m in
+                    (('h', ham), ('vx', vx.tocsr()), ('vy', vy.tocsr()))
+                    for f in ('data', 'indices', 'indptr')})
+        pool = _spawn_pool(procs, _kubo_cpu_init, (tmp.name, lo, hi, M))
+        try:
+            pool.map(_kubo_cpu_task, [vecs[0]] * procs)   # spawn + load
+            t0 = time.perf_counter()
+            res = pool.map(_kubo_cpu_task, list(vecs[:procs]))
+            dt = time.perf_counter() - t0
+        finally:
+            pool.close()
+            pool.join()
+            os.unlink(tmp.name)
+        rec['cpu_baseline'] = {
+            'value': 2 * nnz * procs * M / dt, 'unit': UNIT, 'cores': procs,
+            'kind': 'port', 'sample': '%d vectors x %d moments of the same '
+            'workload (both recursions and the moments matrix), one spawned '
+            'process per vector (%.1f s)' % (procs, M, dt),
+            'cpu': _cpu_model()}
+        if accuracy:
+            # sigma on the sample's vectors: oracle against both GPU paths
+            from oracle import kpm_oracle as ko
+            mu_o = np.mean([r[0] for r in res], axis=0)
+            fac = ko.integral_factor(mu_o, a, b, M)
+            s_o = np.array([[ko.conductivity_value(fac, a, b, M, m, t)
+                             for t in temps] for m in mus])
+            sub = vecs[:procs]
+            mu_m = step(v=sub)
+            mu_d = step(v=sub, hd=h64, gemm=0)
+            rec['accuracy'].update({
+                'sigma_xy_rel_linf_vs_oracle': _rel_linf(
+                    _sigma_grid(mu_m, a, b, M, mus, temps), s_o),
+                'sigma_xy_rel_linf_fp64_path_vs_oracle': _rel_linf(
+                    _sigma_grid(mu_d, a, b, M, mus, temps), s_o),
+                'mu_rel_linf_vs_oracle': _rel_linf(mu_m, mu_o),
+                'oracle_vectors': procs})
+    if accuracy:
+        h64.close()
+    h.close()
+    return rec
+
+
+def run_kubo(args):
+    """The Kubo-Bastin workload as its own bench line (not the headline)."""
+    rec = kubo_record(args, args.steps, args.warmup, cpu=args.cpu,
+                      accuracy=args.accuracy)
+    line = {
+        'metric': METRIC, 'value': rec['value'], 'unit': UNIT, 'n_gpus': 1,
+        'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': rec['ms_per_step'], 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': rec['dtype'],
+        'data': 'synthetic',
+        'config': {'workload': rec['workload'], 'nnz': rec['nnz'],
+                   'orbitals': rec['orbitals']},
+        'roofline': rec['roofline'], 'cpu_baseline': rec.get('cpu_baseline'),
+        'gpu_launches': int(rec['gpu_launches_per_step'] * args.steps),
+        'accuracy': rec.get('accuracy'),
     }
     print(json.dumps(line))
-    h.close()
     return 0
 
 
@@ -892,6 +1028,8 @@ def main():
     p.add_argument('--no-cpu', dest='cpu', action='store_false')
     p.add_argument('--no-accuracy', dest='accuracy', action='store_false')
     p.add_argument('--no-reorder', dest='reorder', action='store_false')
+    p.add_argument('--no-kubo', dest='kubo', action='store_false',
+                   help='leave the Kubo-Bastin sub-record out of the DOS line')
     args = p.parse_args()
     if args.warmup < 3 and args.impl == 'ours':
         print('warning: fewer than 3 warm-up steps', file=sys.stderr)

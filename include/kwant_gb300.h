@@ -101,6 +101,17 @@ KPM_API int kpm_last_error(char* buf, size_t len);
 /* Number of CUDA devices visible (0 when none). */
 KPM_API int kpm_device_count(int* count);
 
+/* Diagnostics (no reference counterpart).  KPM_DEBUG_WAIT_NS: limit, in ns
+ * of GPU time, of every bounded mbarrier wait in the tensor-core kernels
+ * (default 2e9).  KPM_DEBUG_STALL_TMA (tests only): when nonzero their TMA
+ * producers issue no loads, so the MMA thread's wait runs out; the kernel
+ * records the expiry, releases its tensor memory and returns, the call
+ * reports KPM_ETIMEOUT, and the CUDA context stays usable.  Process-wide
+ * settings, read at each launch. */
+#define KPM_DEBUG_WAIT_NS 1
+#define KPM_DEBUG_STALL_TMA 2
+KPM_API int kpm_debug_set(int key, int64_t value);
+
 /* ---- Hamiltonian handle ---------------------------------------------------
  * Replaces the rescaled LinearOperator of _rescale (kwant/kpm.py:1145-1187):
  * the device applies (H v - b v) / a.  a, b as computed by the caller from
@@ -173,7 +184,9 @@ KPM_API int kpm_block_restore(kpm_block* blk, int64_t steps_done, int mode,
  * 2<a_last|a_last> - mu_0).  Computes moments [m_start, m_end) of every
  * vector; m_start is 0 on the first call and the previous m_end when
  * resuming (add_moments, kwant/kpm.py:318-358).  out: R x (m_end - m_start)
- * complex128. */
+ * complex128.  Returns KPM_EDIVERGED (with out written) when a moment
+ * exceeds 1.001 mu_0 in magnitude or is not finite: the spectral bounds
+ * do not enclose the spectrum (|T_n| <= 1 holds only inside it). */
 KPM_API int kpm_block_dos_moments(kpm_block* blk, int64_t m_start, int64_t m_end,
                                   double* out);
 
@@ -194,7 +207,8 @@ KPM_API int kpm_op_apply(kpm_op* op, const double* bra, const double* ket,
  * moments (mean over vectors, /a, kernel) and reconstructs the density at
  * the 2M Chebyshev nodes on the device.  KPM_PREC_MIXED uses
  * KPM_FLAG_REORDER.  moments_out: R x M complex128 (may
- * be NULL); gammas_out / densities_out: 2M complex128 (may be NULL). */
+ * be NULL); gammas_out / densities_out: 2M complex128 (may be NULL).
+ * KPM_EDIVERGED as kpm_block_dos_moments, with every output written. */
 KPM_API int kpm_dos(const kpm_csr_desc* ham, double a, double b, int precision,
                     const double* vecs, int64_t R, int64_t M, int kernel,
                     double* moments_out, double* gammas_out, double* densities_out);

@@ -33,6 +33,8 @@ KERNEL_JACKSON = 1
 KERNEL_LORENTZ = 2
 FLAG_REORDER = 1
 FLAG_PLAIN_C64 = 2
+DEBUG_WAIT_NS = 1
+DEBUG_STALL_TMA = 2
 
 
 class KPMError(RuntimeError):
@@ -129,6 +131,7 @@ def _load():
         'kpm_profile': [P, I],
         'kpm_profile_read': [P, P, P],
         'kpm_launch_count': [P],
+        'kpm_debug_set': [I, I64],
         'kpm_family_set': [P, P, P, P, P],
         'kpm_family_point': [P, D, D, D],
         'kpm_mlp_create': [I, P, I, C.c_uint64, P],
@@ -175,6 +178,13 @@ def check(status):
 
 def ptr(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def debug_set(key, value):
+    """kpm_debug_set: process-wide diagnostics (DEBUG_WAIT_NS: bound of
+    the tensor-core kernels' mbarrier waits; DEBUG_STALL_TMA: tests only,
+    their TMA producers issue no loads)."""
+    check(lib.kpm_debug_set(int(key), int(value)))
 
 
 def device_count():
@@ -306,9 +316,18 @@ class Block:
         self._b = b
         handle._children.add(self)
 
-    def dos_moments(self, m_start, m_end):
+    def dos_moments(self, m_start, m_end, diverged='raise'):
+        """R x (m_end - m_start) DOS moments.  A recursion that diverged
+        (KPM_EDIVERGED: spectral bounds that leave eigenvalues outside)
+        raises KPMDiverged, or with diverged='return' returns the moments
+        and keeps the message in self.diverged."""
         out = np.empty((self.R, m_end - m_start), dtype=np.complex128)
-        check(lib.kpm_block_dos_moments(self._b, m_start, m_end, ptr(out)))
+        st = lib.kpm_block_dos_moments(self._b, m_start, m_end, ptr(out))
+        self.diverged = None
+        if st == KPM_EDIVERGED and diverged == 'return':
+            self.diverged = last_error()
+            return out
+        check(st)
         return out
 
     def op_moments(self, op, m_start, m_end):

@@ -27,11 +27,14 @@
 
 #include "kpm_common.cuh"
 #include "kpm_internal.cuh"
+#include "kpm_tc.cuh"
 
 namespace kpm {
 
 // ---------------------------------------------------------------- errors
 static thread_local char g_err[1024] = "";
+static std::atomic<uint64_t> g_wait_ns{2000000000ull};
+static std::atomic<int> g_stall_tma{0};
 static std::atomic<int64_t> g_launches{0};
 
 void set_error(const char* fmt, ...) {
@@ -42,6 +45,10 @@ void set_error(const char* fmt, ...) {
 }
 const char* last_error() { return g_err; }
 void count_launch(int n) { g_launches += n; }
+
+namespace tc {
+WaitCfg wait_cfg() { return WaitCfg{g_wait_ns.load(), g_stall_tma.load()}; }
+}  // namespace tc
 
 // ------------------------------------------------------------- allocation
 int dev_alloc(void** p, size_t bytes, cudaStream_t s) {
@@ -1102,6 +1109,20 @@ int kpm_device_count(int* count) {
   return KPM_OK;
 }
 
+int kpm_debug_set(int key, int64_t value) {
+  switch (key) {
+    case KPM_DEBUG_WAIT_NS:
+      KPM_REQUIRE(value > 0, "kpm_debug_set: wait limit must be positive");
+      g_wait_ns = (uint64_t)value;
+      return KPM_OK;
+    case KPM_DEBUG_STALL_TMA:
+      g_stall_tma = value != 0;
+      return KPM_OK;
+  }
+  set_error("kpm_debug_set: unknown key %d", key);
+  return KPM_EINVAL;
+}
+
 int kpm_launch_count(int64_t* count) {
   if (!count) return KPM_EINVAL;
   *count = g_launches.load();
@@ -1426,6 +1447,40 @@ int kpm_block_state(kpm_block* b, double* alpha_prev, double* alpha_cur) {
                              b->Rpad, alpha_cur);
 }
 
+// Failure detection for spectral bounds that do not enclose the spectrum:
+// with the rescaled spectrum inside [-1, 1], |T_n| <= 1 there and every DOS
+// moment of a vector obeys |mu_n| <= mu_0; eigenvalues left outside make
+// T_n grow exponentially.  The reference has no such check (its only guard
+// is the eigsh bound itself, kwant/kpm.py:1177-1180).  The moments are
+// written either way; KPM_EDIVERGED reports the first offending moment.
+static int check_divergence(kpm_block* b, int64_t m_start, int64_t count,
+                            const double* out) {
+  std::vector<double> mu01;
+  if (m_start > 0) {
+    mu01.resize((size_t)b->R * 4);
+    KPM_CUDA(cudaMemcpyAsync(mu01.data(), b->mu01,
+                             (size_t)b->R * 2 * sizeof(double2),
+                             cudaMemcpyDeviceToHost, b->h->stream));
+    KPM_CUDA(cudaStreamSynchronize(b->h->stream));
+  }
+  for (int64_t r = 0; r < b->R; ++r) {
+    const double* v = out + 2 * r * count;
+    const double mu0 = m_start == 0 ? v[0] : mu01[4 * r];
+    const double lim = 1.001 * fabs(mu0) + 1e-300;
+    for (int64_t m = 0; m < count; ++m) {
+      const double mag = hypot(v[2 * m], v[2 * m + 1]);
+      if (!(mag <= lim)) {
+        set_error("moment %lld of vector %lld: |mu| = %g exceeds mu_0 = %g: "
+                  "the spectral bounds do not enclose the spectrum and the "
+                  "recursion diverged", (long long)(m_start + m),
+                  (long long)r, mag, mu0);
+        return KPM_EDIVERGED;
+      }
+    }
+  }
+  return KPM_OK;
+}
+
 int kpm_block_dos_moments(kpm_block* b, int64_t m_start, int64_t m_end,
                           double* out) {
   KPM_REQUIRE(b && out, "kpm_block_dos_moments: null argument");
@@ -1477,6 +1532,7 @@ int kpm_block_dos_moments(kpm_block* b, int64_t m_start, int64_t m_end,
   if (st == KPM_OK) st = timed_end(h);
   if (st == KPM_OK) st = moments_to_host(h, mom, count, b->R, b->Rpad, 1, out);
   dev_free(mom, h->stream);
+  if (st == KPM_OK) st = check_divergence(b, m_start, count, out);
   return st;
 }
 

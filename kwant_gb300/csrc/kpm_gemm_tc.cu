@@ -19,9 +19,12 @@
 // epilogue.  Two pipeline stages of 32 K-elements (64-byte swizzle).  The
 // split partials (FP32) are summed in FP64 in a fixed order.
 //
-// Every wait on an mbarrier is bounded (about 2 s of GPU time); on expiry
-// the kernel records an error code, stops issuing work, releases its tensor
-// memory and returns, and the host reports KPM_ETIMEOUT.
+// Every wait on an mbarrier is bounded (2 s of GPU time by default,
+// KPM_DEBUG_WAIT_NS); on expiry the kernel records an error code and stops
+// issuing work; the producer waits for the loads it already issued, one
+// thread decides for the whole CTA whether the epilogue reads tensor memory
+// (all warps take the same branch), the CTA releases its tensor memory and
+// returns, and the host reports KPM_ETIMEOUT.
 
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -44,6 +47,8 @@ struct TcArgs {
   int tmem_cols;    // power of two >= 2 * nt
   float2* part;     // [split][M][M] (re, im) partials
   int* err;
+  uint64_t wait_ns; // bound of every mbarrier wait
+  int stall;        // test only: the producer issues no loads
 };
 
 template <int KC>
@@ -98,15 +103,18 @@ bf16x3_tc_kernel(const __grid_constant__ CUtensorMap map_a,
 
   if (warp == 0 && lane == 0) {
     // ---- TMA producer
-    for (int64_t i = 0; i < nk; ++i) {
+    int64_t issued = 0;
+    for (int64_t i = 0; i < nk && !args.stall; ++i) {
       const int s = (int)(i % STAGES);
       const uint32_t ph = (uint32_t)((i / STAGES) & 1);
-      if (!mbar_wait(&empty[s], ph ^ 1, args.err, 1)) break;
+      if (!mbar_wait(&empty[s], ph ^ 1, args.err, 1, args.wait_ns)) break;
       mbar_expect_tx(&full[s], a_bytes + b_bytes);
       const int kx = (int)((kc0 + i) * KC);
       tma_load_3d(sa + s * a_bytes, &map_a, &full[s], kx, tm * TM, 0);
       tma_load_3d(sb + s * b_bytes, &map_b, &full[s], kx, tn * nt, 0);
+      ++issued;
     }
+    drain_loads(full, STAGES, issued, args.err, args.wait_ns);
   } else if (warp == 1 && lane == 0) {
     // ---- MMA issuer
     const uint32_t id_pos = instr_desc(nt, false);
@@ -117,7 +125,7 @@ bf16x3_tc_kernel(const __grid_constant__ CUtensorMap map_a,
     for (int64_t i = 0; i < nk && ok; ++i) {
       const int s = (int)(i % STAGES);
       const uint32_t ph = (uint32_t)((i / STAGES) & 1);
-      if (!mbar_wait(&full[s], ph, args.err, 2)) {
+      if (!mbar_wait(&full[s], ph, args.err, 2, args.wait_ns)) {
         ok = false;
         break;
       }
@@ -157,11 +165,20 @@ bf16x3_tc_kernel(const __grid_constant__ CUtensorMap map_a,
     mma_commit(done);  // all MMAs of this thread
   }
 
-  // ---- epilogue: all four warps (the MMA thread always commits `done`)
-  __syncwarp();
-  const bool have = mbar_wait(done, 0, args.err, 3) && nk > 0;
+  // ---- epilogue: all four warps (the MMA thread always commits `done`);
+  // one thread decides for the CTA, so that every warp takes the same
+  // branch around the warp-collective tensor-memory loads
+  __shared__ int go;
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const bool ok = mbar_wait_all(done, 0, args.wait_ns);
+    if (!ok) atomicCAS(args.err, 0, 3);
+    go = ok && nk > 0 && *(volatile int*)args.err == 0;
+  }
+  __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
-  if (have && *(volatile int*)args.err == 0) {
+  if (go) {
     const int row = tm * TM + warp * 32 + lane;
     const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
     float2* dst = args.part + ((int64_t)split * args.M + row) * args.M;
@@ -295,7 +312,9 @@ static int gemm_bf16x3_tc_kc(kpm_handle* h, const Store* omega,
     if (e == cudaSuccess) e = cudaEventCreate(&h->ev_gemm1);
   }
   if (st == KPM_OK && e == cudaSuccess) {
-    TcArgs args{M, kchunks, splits, nt, ntiles_n, tmem_cols, part, err};
+    const WaitCfg wc = wait_cfg();
+    TcArgs args{M,    kchunks, splits, nt,      ntiles_n,
+                tmem_cols, part, err,  wc.ns,   wc.stall};
     cudaEventRecord(h->ev_gemm0, h->stream);
     bf16x3_tc_kernel<KC><<<(unsigned)(tiles * splits), THREADS, smem,
                            h->stream>>>(map_a, map_b, args);

@@ -36,6 +36,8 @@ struct TnArgs {
   float* C;
   int64_t ldc;
   int* err;
+  uint64_t wait_ns;  // bound of every mbarrier wait
+  int stall;         // test only: the producer issues no loads
 };
 
 // C[M][N] = A[M][K] * B[N][K]^T (BF16 in, FP32 out), one 128 x nt tile per
@@ -80,20 +82,23 @@ bf16_tn_kernel(const __grid_constant__ CUtensorMap map_a,
   const uint32_t tmem = *tmem_slot;
 
   if (warp == 0 && lane == 0) {
-    for (int64_t i = 0; i < nk; ++i) {
+    int64_t issued = 0;
+    for (int64_t i = 0; i < nk && !args.stall; ++i) {
       const int s = (int)(i % STAGES);
       const uint32_t ph = (uint32_t)((i / STAGES) & 1);
-      if (!mbar_wait(&empty[s], ph ^ 1, args.err, 1)) break;
+      if (!mbar_wait(&empty[s], ph ^ 1, args.err, 1, args.wait_ns)) break;
       mbar_expect_tx(&full[s], a_bytes + b_bytes);
       tma_load_2d(sa + s * a_bytes, &map_a, &full[s], (int)(i * KC), tm * TM);
       tma_load_2d(sb + s * b_bytes, &map_b, &full[s], (int)(i * KC), tn * nt);
+      ++issued;
     }
+    drain_loads(full, STAGES, issued, args.err, args.wait_ns);
   } else if (warp == 1 && lane == 0) {
     const uint32_t idesc = instr_desc(nt, false);
     for (int64_t i = 0; i < nk; ++i) {
       const int s = (int)(i % STAGES);
       const uint32_t ph = (uint32_t)((i / STAGES) & 1);
-      if (!mbar_wait(&full[s], ph, args.err, 2)) break;
+      if (!mbar_wait(&full[s], ph, args.err, 2, args.wait_ns)) break;
       asm volatile("tcgen05.fence::after_thread_sync;");
       const uint32_t a0 = smem_u32(sa + s * a_bytes);
       const uint32_t b0 = smem_u32(sb + s * b_bytes);
@@ -105,10 +110,18 @@ bf16_tn_kernel(const __grid_constant__ CUtensorMap map_a,
     }
     mma_commit(done);
   }
-  __syncwarp();
-  const bool have = mbar_wait(done, 0, args.err, 3) && nk > 0;
+  // one thread decides for the CTA (warp-uniform tensor-memory loads)
+  __shared__ int go;
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const bool ok = mbar_wait_all(done, 0, args.wait_ns);
+    if (!ok) atomicCAS(args.err, 0, 3);
+    go = ok && nk > 0 && *(volatile int*)args.err == 0;
+  }
+  __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
-  if (have && *(volatile int*)args.err == 0) {
+  if (go) {
     const int64_t row = (int64_t)tm * TM + warp * 32 + lane;
     const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
     for (int c = 0; c < nt; c += 16) {
@@ -364,7 +377,9 @@ int gemm_tn(kpm_mlp* net, const bf16* A, int64_t M, const bf16* B,
   KPM_TRY(make_map2d(&ma, A, M, K, tc::TM));
   KPM_TRY(make_map2d(&mb, B, N, K, nt));
   const size_t smem = gemm_smem(nt);   // attribute set at create
-  TnArgs args{M, N, K, nt, ntiles_n, tmem_cols, C, ldc, net->err};
+  const tc::WaitCfg wc = tc::wait_cfg();
+  TnArgs args{M, N, K, nt, ntiles_n, tmem_cols, C, ldc, net->err, wc.ns,
+              wc.stall};
   const int grid = (int)(ceil_div(M, tc::TM) * ntiles_n);
   bf16_tn_kernel<<<grid, tc::THREADS, smem, net->stream>>>(ma, mb, args);
   count_launch(1);

@@ -566,6 +566,10 @@ int kpm_dos(const kpm_csr_desc* ham, double a, double b, int precision,
     mom = moments_out ? moments_out : new double[2 * R * M];
     st = kpm_block_dos_moments(blk, 0, M, mom);
   }
+  // a diverged recursion still returns its moments and densities
+  const bool diverged = st == KPM_EDIVERGED;
+  std::string diverged_msg = diverged ? last_error() : "";
+  if (diverged) st = KPM_OK;
   if (st == KPM_OK && (gammas_out || densities_out)) {
     // real_if_close(tol=100): real when every |imag| < 100 * eps
     double mx = 0.0;
@@ -597,6 +601,10 @@ int kpm_dos(const kpm_csr_desc* ham, double a, double b, int precision,
   if (mom && mom != moments_out) delete[] mom;
   kpm_block_destroy(blk);
   kpm_destroy(h);
+  if (st == KPM_OK && diverged) {
+    set_error("kpm_dos: %s", diverged_msg.c_str());
+    return KPM_EDIVERGED;
+  }
   return st;
 }
 

@@ -13,7 +13,14 @@ namespace tc {
 
 constexpr int TM = 128;          // output rows per CTA (MMA M)
 constexpr int THREADS = 128;
-constexpr uint64_t WAIT_NS = 2000000000ull;  // bounded waits: 2 s
+
+// Limit of every bounded mbarrier wait (ns of GPU time, default 2 s) and
+// the test-only producer stall, set by kpm_debug_set (host side).
+struct WaitCfg {
+  uint64_t ns;
+  int stall;
+};
+WaitCfg wait_cfg();
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -50,18 +57,43 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait; returns false (and records err) when the deadline passes.
+// Bounded wait; returns false (and records err) when the deadline passes
+// or another thread has recorded an error.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
-                                          int* err, int code) {
+                                          int* err, int code,
+                                          uint64_t limit_ns) {
   const uint64_t t0 = global_ns();
   while (!mbar_try_wait(bar, parity)) {
     if (*(volatile int*)err) return false;
-    if (global_ns() - t0 > WAIT_NS) {
+    if (global_ns() - t0 > limit_ns) {
       atomicCAS(err, 0, code);
       return false;
     }
   }
   return true;
+}
+
+// Bounded wait that does not give up on another thread's error (for
+// copies and MMAs already in flight, which complete regardless).
+__device__ __forceinline__ bool mbar_wait_all(uint64_t* bar, uint32_t parity,
+                                              uint64_t limit_ns) {
+  const uint64_t t0 = global_ns();
+  while (!mbar_try_wait(bar, parity))
+    if (global_ns() - t0 > limit_ns) return false;
+  return true;
+}
+
+// The producer's last `issued` TMA loads (at most one pending phase per
+// stage) have landed in shared memory: called before the CTA releases its
+// resources, also after an error stopped the pipeline.
+__device__ __forceinline__ void drain_loads(uint64_t* full, int stages,
+                                            int64_t issued, int* err,
+                                            uint64_t limit_ns) {
+  for (int64_t i = issued > stages ? issued - stages : 0; i < issued; ++i) {
+    const int s = (int)(i % stages);
+    if (!mbar_wait_all(&full[s], (uint32_t)((i / stages) & 1), limit_ns))
+      atomicCAS(err, 0, 4);
+  }
 }
 
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map,

@@ -576,7 +576,9 @@ class SpectralDensity:
     # -- moments -------------------------------------------------------------
     def _block_moments(self, block, m_start, m_end):
         if self._op is None:
-            return block.dos_moments(m_start, m_end)
+            # divergence is reported by _check_divergence (a warning, as
+            # the reference returns its moments unchecked)
+            return block.dos_moments(m_start, m_end, diverged='return')
         return block.op_moments(self._op, m_start, m_end)
 
     def _update_moments_list(self, n_moments, num_vectors):

@@ -302,11 +302,36 @@ def test_mixed_operator_moments(kpm):
 def test_divergence_warning_on_tight_bounds(kpm):
     """Failure detection without a GPU fault: bounds that cut the spectrum
     make the recursion grow; the host flags it from the moments."""
+    from kwant_gb300 import _lib
     g = load('rmt20')
     with pytest.warns(RuntimeWarning, match='do not enclose'):
         kpm.SpectralDensity(g['ham'], bounds=(0.5 * g['lmin'],
                                               0.5 * g['lmax']),
                             num_moments=200, num_vectors=2, rng=1)
+    # the C ABI reports it as KPM_EDIVERGED, with the moments written
+    _, vecs = ref_vectors(g['seed'], 20, 2)
+    tight = kpm._rescale_ab(0.5 * g['lmin'], 0.5 * g['lmax'], 0.05)
+    good = kpm._rescale_ab(g['lmin'], g['lmax'], 0.05)
+    for prec in (_lib.PREC_FP64, _lib.PREC_MIXED):
+        h = _lib.Handle(g['ham'], *tight, prec)
+        blk = _lib.Block(h, vecs, keep_a0=True)
+        with pytest.raises(_lib.KPMDiverged, match='do not enclose'):
+            blk.dos_moments(0, 200)
+        blk.rewind()
+        mom = blk.dos_moments(0, 200, diverged='return')
+        big = np.abs(mom)          # grows until it overflows (complex64)
+        assert blk.diverged
+        assert not np.all(np.isfinite(big)) or \
+            np.nanmax(big) > 10 * big[:, 0].max()
+        blk.close()
+        h.close()
+        h = _lib.Handle(g['ham'], *good, prec)
+        blk = _lib.Block(h, vecs, keep_a0=True)
+        blk.dos_moments(0, 200)            # enclosing bounds: no error
+        blk.close()
+        h.close()
+    with pytest.raises(_lib.KPMDiverged, match='kpm_dos'):
+        _lib.dos(g['ham'], *tight, _lib.PREC_FP64, vecs, 200)
 
 
 
@@ -398,7 +423,42 @@ def test_conductivity_fp64(kpm):
     assert _rel(vals, g['values_add']) < 1e-9
 
 
+def _sigma_error_bound(dmu, a, b, M, mus, temps):
+    """Bound on |sigma(mu + dmu) - sigma(mu)| over a (mu, T) grid.  sigma is
+    linear in the moments matrix (kwant/kpm.py:720-760, :608-630):
+    sigma = pref * sum_k w_k f_k / (1 - e_k^2)^2 * sum_mn mu~_mn G_nm(e_k)
+    with mu~ = g g^T o mu (g[0] halved), Simpson weights w_k and
+    pref = 2 * 4^2 / (2a)^2, so
+    |d sigma| <= pref * sum_k |w_k| f_k / (1 - e_k^2)^2 *
+                 sum_mn |g_m g_n dmu_mn| |G_nm(e_k)|."""
+    from kwant_gb300.kpm import _simpson_weights
+    g = ko.jackson_kernel(np.ones(M))
+    g[0] /= 2
+    x = ko.chebyshev_nodes(2 * M)
+    m = np.arange(M)
+    A = np.abs(np.outer(g, g) * dmu)
+    per_node = np.empty(x.size)
+    for k, e in enumerate(x):
+        ex = np.exp(1j * np.arccos(e) * m)
+        ep = (e - 1j * np.sqrt(1 - e * e) * m) * ex
+        big = ep[None, :] * ex.real[:, None]
+        big = big + big.conj().T
+        per_node[k] = np.sum(A * np.abs(big.T))
+    w = np.abs(_simpson_weights(x)) / (1 - x ** 2) ** 2 * per_node
+    pref = 2 * 4 ** 2 / (2 * a) ** 2
+    E = a * x + b
+    return np.array([[pref * np.sum(w * ko.fermi_distribution(E, mu, T))
+                      for mu in mus] for T in temps])
+
+
 def test_conductivity_mixed_bf16x3(kpm):
+    """Mixed precision (complex64 recursions, BF16x3 tensor-core moments
+    matrix) against the reference's conductivity fixture.  The moments
+    matrix is held to 1e-4 relative; sigma, which weights the integrand by
+    (1 - e^2)^-2 (kwant/kpm.py:623) and so amplifies moment errors most at
+    the outermost nodes, must stay within the error that this moments-
+    matrix error implies through the (linear) integral, plus the FP64
+    post-processing tolerance of test_conductivity_fp64."""
     g = load('conductivity')
     ham = csr(g)
     pos = g['orb_positions']
@@ -410,12 +470,12 @@ def test_conductivity_mixed_bf16x3(kpm):
     assert _rel(cond.moments_matrix, g['mu_xy']) < 1e-4
     vals = np.array([[cond(mu=m, temperature=T) for m in g['mus']]
                      for T in g['temps']])
-    # sigma weights the integrand by (1 - e^2)^-2 (kwant/kpm.py:623), which
-    # amplifies moment errors ~1e7-fold at the outermost of the 2M nodes of
-    # this 48-moment expansion; the bound is the observed mixed-precision
-    # error with a margin, relative to the largest |sigma|.
-    err = np.max(np.abs(vals - g['values_xy']))
-    assert err < 2e-2 * max(1.0, np.max(np.abs(g['values_xy']))), err
+    ref = g['values_xy']
+    bound = _sigma_error_bound(cond.moments_matrix - g['mu_xy'], cond._a,
+                               cond._b, 48, g['mus'], g['temps'])
+    err = np.abs(vals - ref)
+    tol = bound * (1 + 1e-6) + 1e-9 * np.max(np.abs(ref))
+    assert np.all(err <= tol), np.max(err / tol)
 
 
 def test_tensor_core_contraction_matches_cuda_cores(kpm):
