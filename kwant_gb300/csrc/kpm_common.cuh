@@ -138,7 +138,7 @@ struct kpm_handle {
   // call); dg_ok: every row had a real diagonal entry (else the general
   // compensated kernel runs)
   int32_t* dg_idx = nullptr;
-  float2* dg_val = nullptr;
+  float4* dg_val = nullptr;   // (hr, hr, hi, hi) per entry
   int* dg_flag = nullptr;
   bool dg_ok = false;
   int device = 0;

@@ -32,14 +32,21 @@
 //     as complex128 (hi + lo, exact) uploads to the same hi and lo.
 // The fused dot products use the hi parts: mu_0 and mu_1 in FP64 from hi+lo
 // (once), then <a_n|a_n> and Re <a_n+1|a_n> with Ogita-Rump-Oishi Dot2
-// (TwoProd + TwoSum, flushed to FP64 every 32 rows) and Im <a_n+1|a_n> as a
-// plain FP32 sum.  Leaving out lo in these dots is a zero-mean error of
-// each moment alone, not a shift of all of them.
+// (TwoProd + TwoSum, flushed to FP64 every 128 rows) and Im <a_n+1|a_n> as
+// a plain FP32 sum.  Leaving out lo in these dots is a zero-mean error of
+// each moment alone, not a shift of all of them.  (An anchored sum with a
+// per-vector anchor >= 4 mu_0, which bounds every partial sum, was
+// measured too: the anchor is then far above a row's terms, their
+// fractional parts land in the FP32 residual sum, and its bias took the
+// per-orbital DOS error at the outermost node of the 2e6-orbital workload
+// from 2.6e-7 to 1.7e-5.)
 //
 // The H values themselves stay complex64 (2H/a): rounding them perturbs the
 // Hamiltonian, whose moments are still those of a Hermitian operator, and
 // leaves the reconstruction consistent (a ~1e-7 relative shift of the
 // spectrum, not noise).
+
+#include <type_traits>
 
 #include "kpm_common.cuh"
 #include "kpm_internal.cuh"
@@ -87,6 +94,10 @@ __device__ __forceinline__ void dot2(float2& s, float2& c, float2 a,
   s = t;
   c = __fadd2_rn(c, __fadd2_rn(e, pe));
 }
+// value of a compensated pair in FP64, both halves
+__device__ __forceinline__ double pair_sum(float2 s, float2 c) {
+  return ((double)s.x + (double)s.y) + ((double)c.x + (double)c.y);
+}
 // bfloat16 pair word (re in the low half) -> (re, im)
 __device__ __forceinline__ float2 lo_pair(uint32_t w) {
   return make_float2(__uint_as_float(w << 16),
@@ -129,9 +140,12 @@ template <int K, bool D0> struct HiloCfg {
   static constexpr int GATH = D0 ? 1 : 2;
   static constexpr int NW = THREADS / 32;
   static constexpr int NSLOT = THREADS / 8;
+  // ELL values: D0 copies hold them pre-broadcast, (hr, hr, hi, hi), so
+  // that the packed products need no register moves
+  using VT = typename std::conditional<D0, float4, float2>::type;
   static constexpr size_t SMEM =
       2 * ITEMS * THREADS * (sizeof(float4) + sizeof(uint2)) +
-      NW * 3 * 4 * K * (sizeof(int32_t) + sizeof(float2)) +
+      NW * 3 * 4 * K * (sizeof(int32_t) + sizeof(VT)) +
       NSLOT * 48 * sizeof(double);
 };
 
@@ -161,16 +175,17 @@ __global__ void __launch_bounds__(HiloCfg<K, D0>::THREADS,
                                   HiloCfg<K, D0>::MIN_BLOCKS)
 cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
                       const int32_t* __restrict__ eidx,
-                      const float2* __restrict__ eval) {
+                      const typename HiloCfg<K, D0>::VT* __restrict__ eval) {
   using Cfg = HiloCfg<K, D0>;
+  using VT = typename Cfg::VT;
   constexpr int OWN = Cfg::OWN, PREV = Cfg::PREV, GATH = Cfg::GATH;
   constexpr int T = Cfg::THREADS, ITEMS = Cfg::ITEMS, NSLOT = Cfg::NSLOT;
-  constexpr int SW = 8, G = 16, SPW = 4, FLUSH = 32;
+  constexpr int SW = 8, G = 16, SPW = 4, FLUSH = 128;
   extern __shared__ __align__(16) unsigned char smem[];
   float4* vhi = reinterpret_cast<float4*>(smem);              // [2][ITEMS][T]
   uint2* vlo = reinterpret_cast<uint2*>(vhi + 2 * ITEMS * T);  // [2][ITEMS][T]
   int32_t* sidx = reinterpret_cast<int32_t*>(vlo + 2 * ITEMS * T);
-  float2* sval = reinterpret_cast<float2*>(sidx + Cfg::NW * 3 * 4 * K);
+  VT* sval = reinterpret_cast<VT*>(sidx + Cfg::NW * 3 * 4 * K);
   double* red = reinterpret_cast<double*>(sval + Cfg::NW * 3 * 4 * K);
 
   const int tid = threadIdx.x;
@@ -178,7 +193,7 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
   const int slot = tid / SW;
   const int wq = slot / SPW, half = slot % SPW, wl = tid & 31;
   int32_t* widx = sidx + wq * 3 * 4 * K;   // this warp's ring: [3][SPW * K]
-  float2* wval = sval + wq * 3 * 4 * K;
+  VT* wval = sval + wq * 3 * 4 * K;
 
   const float4* __restrict__ x = reinterpret_cast<const float4*>(p.x);
   const float4* prev = reinterpret_cast<const float4*>(p.prev);
@@ -200,15 +215,17 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
 
   // ELL entries of the warp's rows r0 .. r0 + 3 into ring buffer b
   auto stage_ell = [&](int r0, int b) {
-    constexpr int IC = SPW * K / 4, VC = SPW * K / 2;
+    constexpr int EPC = 16 / (int)sizeof(VT);   // values per 16-byte chunk
+    constexpr int IC = SPW * K / 4, VC = SPW * K / EPC;
     for (int c = wl; c < IC + VC; c += 32) {
       if (c < IC) {
         if (r0 + (4 * c) / K < rows)
           cp_async16(widx + b * 4 * K + 4 * c, eidx + (int64_t)r0 * K + 4 * c);
       } else {
         const int e = c - IC;
-        if (r0 + (2 * e) / K < rows)
-          cp_async16(wval + b * 4 * K + 2 * e, eval + (int64_t)r0 * K + 2 * e);
+        if (r0 + (EPC * e) / K < rows)
+          cp_async16(wval + b * 4 * K + EPC * e,
+                     eval + (int64_t)r0 * K + EPC * e);
       }
     }
   };
@@ -298,11 +315,19 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
             LP[k] = __fmul2_rn(shift, lo_pair(xlw[k]));
           }
         }
-        const float2* hv = wval + e0 * 4 * K + half * K;
+        const VT* hv = wval + e0 * 4 * K + half * K;
 #pragma unroll
         for (int t = 0; t < K; ++t) {
-          const float2 h = hv[t];
-          const float2 hr = f2(h.x), hi = f2(h.y);
+          float2 hr, hi;
+          if constexpr (D0) {
+            const float4 h = hv[t];
+            hr = make_float2(h.x, h.y);
+            hi = make_float2(h.z, h.w);
+          } else {
+            const float2 h = hv[t];
+            hr = f2(h.x);
+            hi = f2(h.y);
+          }
           const float4 gx = sh[(GATH + t) * T];
           const uint2 gl = sl[(GATH + t) * T];
           const float2 gk[2] = {make_float2(gx.x, gx.y),
@@ -380,10 +405,8 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
           if (++pending == FLUSH) {
 #pragma unroll
             for (int k = 0; k < 2; ++k) {
-              my[k * 3 + 0] += ((double)dns[k].x + (double)dns[k].y) +
-                               ((double)dnc[k].x + (double)dnc[k].y);
-              my[k * 3 + 1] += ((double)drs[k].x + (double)drs[k].y) +
-                               ((double)drc[k].x + (double)drc[k].y);
+              my[k * 3 + 0] += pair_sum(dns[k], dnc[k]);
+              my[k * 3 + 1] += pair_sum(drs[k], drc[k]);
               my[k * 3 + 2] += (double)fim[k];
               dns[k] = dnc[k] = drs[k] = drc[k] = make_float2(0.f, 0.f);
               fim[k] = 0.f;
@@ -403,10 +426,8 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
     if constexpr (MODE == STEP_RECUR) {
 #pragma unroll
       for (int k = 0; k < 2; ++k) {
-        my[k * 3 + 0] += ((double)dns[k].x + (double)dns[k].y) +
-                         ((double)dnc[k].x + (double)dnc[k].y);
-        my[k * 3 + 1] += ((double)drs[k].x + (double)drs[k].y) +
-                         ((double)drc[k].x + (double)drc[k].y);
+        my[k * 3 + 0] += pair_sum(dns[k], dnc[k]);
+        my[k * 3 + 1] += pair_sum(drs[k], drc[k]);
         my[k * 3 + 2] += (double)fim[k];
       }
     }
@@ -455,7 +476,9 @@ static int launch_hilo_t(kpm_handle* h, const StepArgs& a,
   }
   cheb_step_hilo_kernel<K, MODE, D0>
       <<<(unsigned)grid, Cfg::THREADS, Cfg::SMEM, h->stream>>>(
-          a, q, D0 ? h->dg_idx : h->H.ell_idx, D0 ? h->dg_val : h->H.ell_val);
+          a, q, D0 ? h->dg_idx : h->H.ell_idx,
+          reinterpret_cast<const typename Cfg::VT*>(
+              D0 ? (const void*)h->dg_val : (const void*)h->H.ell_val));
   count_launch(1);
   KPM_CHECK_LAUNCH();
   if (e1) KPM_CUDA(cudaEventRecord(e1, h->stream));
@@ -481,7 +504,7 @@ __global__ void diag_first_kernel(int64_t n, int K,
                                   const int32_t* __restrict__ eidx,
                                   const float2* __restrict__ eval,
                                   float shift, int32_t* __restrict__ oidx,
-                                  float2* __restrict__ oval, int* bad) {
+                                  float4* __restrict__ oval, int* bad) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n) return;
   const int32_t* ri = eidx + r * K;
@@ -499,13 +522,14 @@ __global__ void diag_first_kernel(int64_t n, int K,
   int o = 0;
   if (d >= 0) {
     oidx[r * K] = (int32_t)r;
-    oval[r * K] = make_float2(__fadd_rn(rv[d].x, shift), 0.f);
+    const float dv = __fadd_rn(rv[d].x, shift);
+    oval[r * K] = make_float4(dv, dv, 0.f, 0.f);
     o = 1;
   }
   for (int t = 0; t < K; ++t) {
     if (t == d) continue;
     oidx[r * K + o] = ri[t];
-    oval[r * K + o] = rv[t];
+    oval[r * K + o] = make_float4(rv[t].x, rv[t].x, rv[t].y, rv[t].y);
     ++o;
   }
 }
@@ -517,7 +541,7 @@ int prepare_hilo(kpm_handle* h) {
   const size_t cnt = (size_t)n * K;
   if (!h->dg_idx) {
     KPM_TRY(dev_alloc((void**)&h->dg_idx, cnt * sizeof(int32_t), h->stream));
-    KPM_TRY(dev_alloc((void**)&h->dg_val, cnt * sizeof(float2), h->stream));
+    KPM_TRY(dev_alloc((void**)&h->dg_val, cnt * sizeof(float4), h->stream));
     KPM_TRY(dev_alloc((void**)&h->dg_flag, sizeof(int), h->stream));
   }
   KPM_CUDA(cudaMemsetAsync(h->dg_flag, 0, sizeof(int), h->stream));
