@@ -950,6 +950,21 @@ def run_surrogate(args):
     pv = sweep.moments(Xte[:16], per_vector=True).real
     noise = (np.std(pv @ A.T, axis=1, ddof=1) / np.sqrt(R)).max(axis=1)
     n = len(Xte)
+    # the smallest tolerance at which surrogate + KPM check beats the plain
+    # sweep with >= 95 % of the accepted points really within it
+    wins = [c['tol'] for c in curve if c['sweep_s_model'] < plain_s and
+            c['accepted'] > 0 and c['frac_accepted_within_tol'] >= 0.95]
+    verdict = {
+        'configured_tol': args.sur_tol,
+        'hybrid_beats_plain_at_configured_tol': hybrid_s < plain_s,
+        'first_winning_tol': min(wins) if wins else None,
+        'kpm_noise_linf_median': float(np.median(noise)),
+        'configured_tol_below_kpm_noise':
+            args.sur_tol < float(np.median(noise)),
+        'note': 'the plain sweep (R vectors) is itself uncertain by its '
+                'stochastic DOS error; a tolerance below it cannot be '
+                'certified by the R-vector KPM check that judges the '
+                'surrogate'}
     line = {
         'metric': 'held-out sweep points/s at DOS Linf error <= tol '
                   '(surrogate + KPM fallback)',
@@ -982,6 +997,7 @@ def run_surrogate(args):
                            'estimate_scale': sur.scale,
                            'estimate_median': float(np.median(est))},
         'tolerance_curve': curve,
+        'tolerance_verdict': verdict,
         'kpm_noise_linf_median': float(np.median(noise)),
         'costs_s': {'setup': setup_s, 'dataset': gen_s, 'train': train_s,
                     'train_loss': [float(x) for x in losses]},

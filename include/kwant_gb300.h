@@ -5,7 +5,7 @@
  * (kwant/kpm.py: SpectralDensity, Correlator, conductivity; with
  * kwant/operator.pyx Density/Current as local operators).  The Python
  * package kwant_gb300 binds it through ctypes; any other host language
- * binds the same symbols (see INTEGRATION.md).
+ * binds the same symbols.
  *
  * Conventions
  *  - Every function returns an int status: KPM_OK (0) or a negative error
@@ -111,6 +111,11 @@ KPM_API int kpm_device_count(int* count);
 #define KPM_DEBUG_WAIT_NS 1
 #define KPM_DEBUG_STALL_TMA 2
 KPM_API int kpm_debug_set(int key, int64_t value);
+/* 1 if this library was built with -DKPM_CHECK: its Chebyshev step kernels
+ * validate every gathered column index, and the moment calls return
+ * KPM_EINVAL naming the first index out of range (no reference
+ * counterpart; the reference's Cython loops run with boundscheck off). */
+KPM_API int kpm_build_checks(int* enabled);
 
 /* ---- Hamiltonian handle ---------------------------------------------------
  * Replaces the rescaled LinearOperator of _rescale (kwant/kpm.py:1145-1187):

@@ -12,7 +12,10 @@ import os
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, 'libkwant_gb300.so')
+# KWANT_GB300_LIB may name another build of the library (the bounds-checked
+# variant of kwant_gb300.build)
+LIB_PATH = os.environ.get('KWANT_GB300_LIB') or \
+    os.path.join(_HERE, 'libkwant_gb300.so')
 
 KPM_OK = 0
 KPM_EINVAL = -1
@@ -132,6 +135,7 @@ def _load():
         'kpm_profile_read': [P, P, P],
         'kpm_launch_count': [P],
         'kpm_debug_set': [I, I64],
+        'kpm_build_checks': [P],
         'kpm_family_set': [P, P, P, P, P],
         'kpm_family_point': [P, D, D, D],
         'kpm_mlp_create': [I, P, I, C.c_uint64, P],
@@ -185,6 +189,13 @@ def debug_set(key, value):
     the tensor-core kernels' mbarrier waits; DEBUG_STALL_TMA: tests only,
     their TMA producers issue no loads)."""
     check(lib.kpm_debug_set(int(key), int(value)))
+
+
+def build_checks():
+    """True when the loaded library is the bounds-checked build."""
+    on = C.c_int(0)
+    check(lib.kpm_build_checks(C.byref(on)))
+    return bool(on.value)
 
 
 def device_count():

@@ -4,6 +4,11 @@ Compiles every ``csrc/*.cu`` translation unit with nvcc in parallel and links
 ``kwant_gb300/libkwant_gb300.so`` (CUDA runtime linked statically, so the
 library only needs the driver at run time).  Object files go to
 ``kwant_gb300/_build/``.  Rebuilds only what changed.
+
+``build(variant='check')`` builds the bounds-checked debug library
+(``-DKPM_CHECK``: the step kernels validate every gathered column index)
+into ``kwant_gb300/_build_check/libkwant_gb300.so``; the package loads it
+when the environment variable ``KWANT_GB300_LIB`` names it.
 """
 
 import concurrent.futures as cf
@@ -48,7 +53,17 @@ def _compile(nvcc, src, obj, extra):
     return r.stderr
 
 
-def build(verbose=False, extra_flags=()):
+def build(verbose=False, extra_flags=(), variant=None):
+    if variant == 'check':
+        return _build(os.path.join(HERE, '_build_check'),
+                      os.path.join(HERE, '_build_check', 'libkwant_gb300.so'),
+                      verbose, list(extra_flags) + ['-DKPM_CHECK'])
+    if variant is not None:
+        raise ValueError('unknown build variant %r' % (variant,))
+    return _build(BUILD, LIB, verbose, extra_flags)
+
+
+def _build(BUILD, LIB, verbose, extra_flags):
     nvcc = _nvcc()
     os.makedirs(BUILD, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, '*.cu')))

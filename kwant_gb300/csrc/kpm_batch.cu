@@ -1428,6 +1428,7 @@ int kpm_batch_add_wilson_dirac(kpm_batch* bt, int64_t L, double m, double W,
 }
 
 int kpm_batch_run(kpm_batch* bt, double* out) {
+  NvtxRange nvtx("kpm_batch_run");
   KPM_REQUIRE(bt && out, "kpm_batch_run: null argument");
   if (!bt->ready) KPM_TRY(prepare(bt));
   KPM_CUDA(cudaEventRecord(bt->e0, bt->stream));

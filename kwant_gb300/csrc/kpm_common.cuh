@@ -9,6 +9,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/kwant_gb300.h"
 
 namespace kpm {
@@ -42,6 +44,15 @@ const char* last_error();
     int st__ = (expr);                                                      \
     if (st__ != KPM_OK) return st__;                                        \
   } while (0)
+
+// NVTX range over an API call (named in Nsight Systems / Compute
+// timelines; a no-op unless a tool is attached)
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // --- launch geometry -------------------------------------------------------
 // A "slot" is LANES consecutive threads that together own one matrix row for
@@ -133,6 +144,9 @@ struct kpm_handle {
   // complex64 element and step with the compensated kernel (cleared by
   // KPM_FLAG_PLAIN_C64; needs the complex64 ELL copy)
   bool compensated = false;
+  // bounds-checked builds (-DKPM_CHECK): first out-of-range column index a
+  // step kernel met, plus one (0: none)
+  unsigned long long* check = nullptr;
   // compensated DOS: ELL copy with every row's diagonal entry first and the
   // diagonal shift -2b/a folded into it (rebuilt on the device by each DOS
   // call); dg_ok: every row had a real diagonal entry (else the general

@@ -621,8 +621,8 @@ cheb_step_kernel(StepArgs p) {
         double ar = 0.0, ai = 0.0;
         int jj = beg;
         for (; jj + 4 <= end; jj += 4) {
-          int c0 = __ldg(indices + jj), c1 = __ldg(indices + jj + 1);
-          int c2 = __ldg(indices + jj + 2), c3 = __ldg(indices + jj + 3);
+          int c0 = col_index(p, __ldg(indices + jj)), c1 = col_index(p, __ldg(indices + jj + 1));
+          int c2 = col_index(p, __ldg(indices + jj + 2)), c3 = col_index(p, __ldg(indices + jj + 3));
           double2 h0 = vals[jj], h1 = vals[jj + 1];
           double2 h2 = vals[jj + 2], h3 = vals[jj + 3];
           double2 x0 = x[(int64_t)c0 * p.rp + col];
@@ -635,7 +635,7 @@ cheb_step_kernel(StepArgs p) {
           cmul_acc_exact(ar, ai, h3, x3);
         }
         for (; jj < end; ++jj) {
-          int c = __ldg(indices + jj);
+          int c = col_index(p, __ldg(indices + jj));
           cmul_acc_exact(ar, ai, vals[jj], x[(int64_t)c * p.rp + col]);
         }
         // (H v - b v) * (1/a): numpy's order (kwant/kpm.py:1183; complex
@@ -674,7 +674,7 @@ cheb_step_kernel(StepArgs p) {
           PT xx[4];
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
-            c[u] = __ldg(indices + jj + u);
+            c[u] = col_index(p, __ldg(indices + jj + u));
             h[u] = vals[jj + u];
           }
 #pragma unroll
@@ -683,7 +683,7 @@ cheb_step_kernel(StepArgs p) {
           for (int u = 0; u < 4; ++u) mac(h[u], xx[u]);
         }
         for (; jj < end; ++jj) {
-          int c = __ldg(indices + jj);
+          int c = col_index(p, __ldg(indices + jj));
           mac(vals[jj], x[(int64_t)c * p.rp + col]);
         }
         float orr[VPL], oii[VPL];
@@ -902,11 +902,32 @@ StepArgs step_args(kpm_block* b, const void* x, const void* prev, void* out) {
   a.groups = b->groups;
   a.xitems = xitems_for_rows(b->N, h->num_sms);
   a.partials = h->partials;
+  a.check = h->check;
   return a;
 }
 
 // Advance the block's recursion by one matvec.  On the first call alpha_1 =
 // H~ alpha_0; afterwards alpha_{n+1} = 2 H~ alpha_n - alpha_{n-1}.
+int check_bounds(kpm_handle* h, const char* where) {
+#ifdef KPM_CHECK
+  if (!h->check) return KPM_OK;
+  unsigned long long v = 0;
+  KPM_CUDA(cudaMemcpyAsync(&v, h->check, sizeof(v), cudaMemcpyDeviceToHost,
+                           h->stream));
+  KPM_CUDA(cudaStreamSynchronize(h->stream));
+  if (v) {
+    KPM_CUDA(cudaMemsetAsync(h->check, 0, sizeof(v), h->stream));
+    set_error("%s: bounds check: column index %llu outside [0, %lld)", where,
+              v - 1, (long long)h->H.rows);
+    return KPM_EINVAL;
+  }
+#else
+  (void)h;
+  (void)where;
+#endif
+  return KPM_OK;
+}
+
 int block_advance(kpm_block* b, bool dots) {
   void* x = b->p_cur;
   if (b->steps_done == 0) {
@@ -1123,6 +1144,16 @@ int kpm_debug_set(int key, int64_t value) {
   return KPM_EINVAL;
 }
 
+int kpm_build_checks(int* enabled) {
+  KPM_REQUIRE(enabled, "kpm_build_checks: null argument");
+#ifdef KPM_CHECK
+  *enabled = 1;
+#else
+  *enabled = 0;
+#endif
+  return KPM_OK;
+}
+
 int kpm_launch_count(int64_t* count) {
   if (!count) return KPM_EINVAL;
   *count = g_launches.load();
@@ -1168,6 +1199,17 @@ int kpm_create_ex(const kpm_csr_desc* ham, double a, double b, int precision,
   h->own_stream = true;
   h->compensated =
       precision == KPM_PREC_MIXED && !(flags & KPM_FLAG_PLAIN_C64);
+#ifdef KPM_CHECK
+  st = dev_alloc((void**)&h->check, sizeof(unsigned long long), h->stream);
+  if (st == KPM_OK &&
+      cudaMemsetAsync(h->check, 0, sizeof(unsigned long long), h->stream) !=
+          cudaSuccess)
+    st = KPM_ECUDA;
+  if (st != KPM_OK) {
+    kpm_destroy(h);
+    return st;
+  }
+#endif
   if (const char* kc = getenv("KPM_TC_KC")) h->tc_kc = atoi(kc) == 32 ? 32 : 16;
   const double scale = h->precision == KPM_PREC_MIXED ? 2.0 / a : 0.0;
   if (flags & KPM_FLAG_REORDER) {
@@ -1216,6 +1258,7 @@ int kpm_destroy(kpm_handle* h) {
   dev_free(h->vec_staging, h->stream);
   dev_free(h->partials, h->stream);
   dev_free(h->perm, h->stream);
+  dev_free(h->check, h->stream);
   dev_free(h->dg_idx, h->stream);
   dev_free(h->dg_val, h->stream);
   dev_free(h->dg_flag, h->stream);
@@ -1483,6 +1526,7 @@ static int check_divergence(kpm_block* b, int64_t m_start, int64_t count,
 
 int kpm_block_dos_moments(kpm_block* b, int64_t m_start, int64_t m_end,
                           double* out) {
+  NvtxRange nvtx("kpm_block_dos_moments");
   KPM_REQUIRE(b && out, "kpm_block_dos_moments: null argument");
   KPM_REQUIRE(m_end >= 2 && m_start >= 0 && m_start < m_end,
               "kpm_block_dos_moments: need 0 <= m_start < m_end, m_end >= 2 "
@@ -1532,6 +1576,7 @@ int kpm_block_dos_moments(kpm_block* b, int64_t m_start, int64_t m_end,
   if (st == KPM_OK) st = timed_end(h);
   if (st == KPM_OK) st = moments_to_host(h, mom, count, b->R, b->Rpad, 1, out);
   dev_free(mom, h->stream);
+  if (st == KPM_OK) st = check_bounds(h, "kpm_block_dos_moments");
   if (st == KPM_OK) st = check_divergence(b, m_start, count, out);
   return st;
 }

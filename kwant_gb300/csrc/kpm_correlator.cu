@@ -274,6 +274,7 @@ int kpm_correlator_moments(kpm_handle* h, double a2, double b2,
                            const kpm_csr_desc* v_beta, const double* vecs,
                            int64_t R, int64_t M, int gemm, int per_vector,
                            double* mu_out) {
+  NvtxRange nvtx("kpm_correlator_moments");
   KPM_REQUIRE(h && v_alpha && v_beta && vecs && mu_out,
               "kpm_correlator_moments: null argument");
   KPM_REQUIRE(R > 0 && M >= 2, "kpm_correlator_moments: need R > 0, M >= 2");
@@ -399,6 +400,7 @@ int kpm_correlator_moments(kpm_handle* h, double a2, double b2,
   }
   if (ready) cudaEventDestroy(ready);
   if (done) cudaEventDestroy(done);
+  if (st == KPM_OK) st = check_bounds(h, "kpm_correlator_moments");
   return st;
 }
 

@@ -23,7 +23,26 @@ struct StepArgs {
   int groups;
   int xitems;
   double* partials; // [group][vector*3 + component][xitems]
+  unsigned long long* check;  // KPM_CHECK builds: first bad index + 1
 };
+
+// Column index of a gathered row.  Bounds-checked builds (-DKPM_CHECK)
+// validate it: an index outside [0, rows) is recorded in p.check and row 0
+// is read instead; other builds use it as is.
+__device__ __forceinline__ int col_index(const StepArgs& p, int c) {
+#ifdef KPM_CHECK
+  if ((uint32_t)c >= (uint32_t)p.rows) {
+    if (p.check)
+      atomicCAS(p.check, 0ull, 1ull + (unsigned long long)(uint32_t)c);
+    return 0;
+  }
+#endif
+  return c;
+}
+
+// KPM_CHECK builds: KPM_EINVAL if a step kernel of h met a bad index
+// (then cleared); KPM_OK otherwise and in other builds
+int check_bounds(kpm_handle* h, const char* where);
 
 // Fused store of alpha_n's row (the correlator's recursions, ELL step,
 // BF16x3 store): smode 0 none, 1 alpha_n itself, 2 V alpha_n with V's values

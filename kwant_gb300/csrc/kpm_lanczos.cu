@@ -217,6 +217,7 @@ extern "C" {
 
 int kpm_bounds(const kpm_csr_desc* ham, const double* v0, double tol,
                int max_iter, double* lmin, double* lmax, int* iterations) {
+  NvtxRange nvtx("kpm_bounds");
   KPM_REQUIRE(ham && v0 && lmin && lmax, "kpm_bounds: null argument");
   KPM_REQUIRE(tol > 0 && max_iter >= 2, "kpm_bounds: invalid tol/max_iter");
   kpm_handle* h = nullptr;

@@ -297,6 +297,7 @@ int kpm_op_destroy(kpm_op* op) {
 
 int kpm_block_op_moments(kpm_block* b, kpm_op* op, int64_t m_start,
                          int64_t m_end, double* out) {
+  NvtxRange nvtx("kpm_block_op_moments");
   KPM_REQUIRE(b && op && out, "kpm_block_op_moments: null argument");
   KPM_REQUIRE(op->h == b->h, "kpm_block_op_moments: operator of another "
               "handle");
@@ -353,6 +354,7 @@ int kpm_block_op_moments(kpm_block* b, kpm_op* op, int64_t m_start,
   if (st == KPM_OK) st = moments_to_host(h, mom, count, b->R, b->Rpad, W, out);
   dev_free(mom, h->stream);
   dev_free(part, h->stream);
+  if (st == KPM_OK) st = check_bounds(h, "kpm_block_op_moments");
   return st;
 }
 

@@ -383,6 +383,7 @@ int kpm_reconstruct(int64_t R, int64_t M, int64_t W, const double* moments,
                     int mean, int is_real, double a, int kernel,
                     double lorentz_l, const double* nodes, double* gammas_out,
                     double* densities_out) {
+  NvtxRange nvtx("kpm_reconstruct");
   KPM_REQUIRE(R > 0 && M > 0 && W > 0 && moments && nodes && a > 0,
               "kpm_reconstruct: invalid argument");
   KPM_REQUIRE(kernel >= KPM_KERNEL_NONE && kernel <= KPM_KERNEL_LORENTZ,
@@ -408,6 +409,7 @@ int kpm_reconstruct(int64_t R, int64_t M, int64_t W, const double* moments,
 int kpm_fermi_sums(int64_t n, const double* energies, const double* weights,
                    int64_t W, const double* values, int64_t P,
                    const double* mu, const double* temperature, double* out) {
+  NvtxRange nvtx("kpm_fermi_sums");
   KPM_REQUIRE(n > 0 && W > 0 && P > 0 && energies && weights && values &&
                   out && (mu == nullptr) == (temperature == nullptr) &&
                   (mu != nullptr || P == 1),
@@ -469,6 +471,7 @@ int kpm_fermi_sums(int64_t n, const double* energies, const double* weights,
 
 int kpm_integral_factor(int64_t M, const double* mu, const double* g,
                         const double* nodes, double* factor_out) {
+  NvtxRange nvtx("kpm_integral_factor");
   KPM_REQUIRE(M > 0 && mu && g && nodes && factor_out,
               "kpm_integral_factor: invalid argument");
   int dev, sms;
@@ -522,6 +525,7 @@ int kpm_integral_factor(int64_t M, const double* mu, const double* g,
 int kpm_dos(const kpm_csr_desc* ham, double a, double b, int precision,
             const double* vecs, int64_t R, int64_t M, int kernel,
             double* moments_out, double* gammas_out, double* densities_out) {
+  NvtxRange nvtx("kpm_dos");
   KPM_REQUIRE(ham && vecs && R > 0 && M >= 2, "kpm_dos: invalid argument");
   KPM_REQUIRE(ham->rows > 0, "kpm_dos: invalid CSR descriptor");
   // Copy the vectors to the device on a stream of their own first, so that

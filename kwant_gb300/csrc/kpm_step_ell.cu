@@ -195,7 +195,8 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
             : nullptr;
 #pragma unroll
         for (int q = 0; q < KQ; ++q) {
-          const int cc[4] = {c4[u][q].x, c4[u][q].y, c4[u][q].z, c4[u][q].w};
+          const int cc[4] = {col_index(p, c4[u][q].x), col_index(p, c4[u][q].y),
+                             col_index(p, c4[u][q].z), col_index(p, c4[u][q].w)};
           PT xx[4];
 #pragma unroll
           for (int t = 0; t < 4; ++t) xx[t] = x[(int64_t)cc[t] * p.rp + col];

@@ -247,7 +247,7 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
     const int32_t* ci = widx + eb * 4 * K + half * K;
 #pragma unroll
     for (int t = 0; t < K; ++t) {
-      const int64_t oc = off(ci[t], col);
+      const int64_t oc = off(col_index(p, ci[t]), col);
       cp_async16_ca(dh + (GATH + t) * T, x + oc);
       cp_async8(dl + (GATH + t) * T, xl + oc);
     }

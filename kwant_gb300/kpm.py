@@ -33,6 +33,7 @@ post-processing (``__call__`` at arbitrary energies, ``integrate``,
 ``Correlator.__call__``).
 """
 
+import itertools
 import math
 from collections.abc import Iterable
 
@@ -235,6 +236,20 @@ class _RescaledHamiltonian(LinearOperator):
 # --------------------------------------------------------------------------
 # vector factories (kwant/kpm.py:850-985)
 # --------------------------------------------------------------------------
+
+class _SequenceTail:
+    """A sequence of vectors resumed after its first ``start`` elements:
+    its length is the sequence's, its iteration starts at ``start``."""
+
+    def __init__(self, seq, start):
+        self.seq, self.start = seq, start
+
+    def __len__(self):
+        return len(self.seq)
+
+    def __iter__(self):
+        return itertools.islice(iter(self.seq), self.start, None)
+
 
 class _VectorFactory:
     """kwant/kpm.py:850-929."""
@@ -814,9 +829,12 @@ class SpectralDensity:
         """A SpectralDensity resumed from ``save``'s checkpoint, on the same
         ``hamiltonian`` (and ``operator``, ``params``).  ``add_moments``
         continues the saved recursion; ``add_vectors`` continues the saved
-        random-vector stream (or draws from ``vector_factory`` when the
-        vectors were user-supplied).  ``kernel`` is needed when a custom
-        kernel was used."""
+        random-vector stream, or draws from ``vector_factory`` when the
+        vectors were user-supplied: a sequence (with ``len()``) is taken to
+        be the same vectors as before, and its first ``num_vectors`` (the
+        saved ones) are skipped; an iterator without ``len()`` must yield
+        only the vectors that come after the checkpoint.  ``kernel`` is
+        needed when a custom kernel was used."""
         z = np.load(file, allow_pickle=False)
         if int(z['version']) != 1:
             raise ValueError('unknown checkpoint version')
@@ -839,7 +857,11 @@ class SpectralDensity:
         nvec = sum(len(a) for a in a0s)
         self._rng = None
         if vector_factory is not None:
-            source = vector_factory
+            try:
+                len(vector_factory)
+                source = _SequenceTail(vector_factory, nvec)
+            except TypeError:
+                source = vector_factory
         elif 'rng_keys' in z.files:
             rng = np.random.RandomState()
             rng.set_state(('MT19937', z['rng_keys'], int(z['rng_pos']),

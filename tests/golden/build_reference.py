@@ -1,8 +1,9 @@
 """Build the reference Kwant package from its sources for fixture generation.
 
-Test infrastructure only.  The reference lives at ``/root/reference`` in the
-development container (read-only); this script copies its ``kwant/`` package
-into ``tests/golden/_refbuild/`` (git-ignored, never shipped) and compiles the
+Test infrastructure only.  The reference's source tree is named by the
+environment variable ``KWANT_REFERENCE_SRC`` (a read-only checkout of
+kwant-project/kwant); this script copies its ``kwant/`` package into
+``tests/golden/_refbuild/`` (git-ignored, never shipped) and compiles the
 Cython extension modules the KPM path imports, with our own minimal
 setuptools invocation (not the reference's ``setup.py``).  The numpy-backed
 ``tinyarray`` stand-in in ``tests/golden/tinyarray_standin`` replaces the
@@ -10,7 +11,7 @@ absent ``tinyarray`` dependency.
 
 Usage::
 
-    python tests/golden/build_reference.py        # builds once, then no-op
+    KWANT_REFERENCE_SRC=<kwant checkout> python tests/golden/build_reference.py
     python -c "import sys; sys.path[:0] = [...]; import kwant"
 
 ``reference_paths()`` returns the two ``sys.path`` entries that make
@@ -22,7 +23,7 @@ import shutil
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE = os.environ.get('KWANT_REFERENCE_SRC', '/root/reference')
+REFERENCE = os.environ.get('KWANT_REFERENCE_SRC')
 BUILD_DIR = os.path.join(HERE, '_refbuild')
 STANDIN = os.path.join(HERE, 'tinyarray_standin')
 
@@ -48,6 +49,9 @@ def _built():
 def build(force=False):
     if _built() and not force:
         return BUILD_DIR
+    if not REFERENCE:
+        raise RuntimeError('set KWANT_REFERENCE_SRC to a kwant source '
+                           'checkout to build the reference')
     if not os.path.isdir(os.path.join(REFERENCE, 'kwant')):
         raise RuntimeError('reference sources not found at %s' % REFERENCE)
     import numpy as np

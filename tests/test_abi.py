@@ -82,3 +82,28 @@ def test_argument_checks_and_missing_device_fail_cleanly():
         assert st == -2                                  # KPM_ECUDA
         assert 'CUDA' in _lib.last_error()
         assert lib.kpm_batch_create(4, 24, 0, ctypes.byref(out)) == -2
+
+
+def _query_checks(lib_file):
+    """kpm_build_checks of a library, in a fresh process that loads it
+    through the package (KWANT_GB300_LIB)."""
+    env = dict(os.environ, KWANT_GB300_LIB=lib_file)
+    out = subprocess.run(
+        ['python', '-c', 'from kwant_gb300 import _lib; '
+         'print(int(_lib.build_checks()))'],
+        cwd=ROOT, env=env, capture_output=True, text=True, check=True)
+    return int(out.stdout.strip())
+
+
+def test_bounds_checked_build(lib_path):
+    """The -DKPM_CHECK debug build (in-kernel index validation) compiles,
+    links, exports the same symbols and reports itself; the default
+    library does not check."""
+    from kwant_gb300 import build
+    checked = build.build(variant='check')
+    assert os.path.abspath(checked) != os.path.abspath(lib_path)
+    lib = ctypes.CDLL(checked)
+    for name in _declared():
+        assert hasattr(lib, name), name
+    assert _query_checks(checked) == 1
+    assert _query_checks(lib_path) == 0

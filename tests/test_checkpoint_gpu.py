@@ -43,6 +43,26 @@ def test_save_load_resumes_exactly(tmp_path, precision, with_op):
         kpm.SpectralDensity.load(f, lattices.square(11, seed=4))
 
 
+def test_load_continues_a_user_vector_list(tmp_path):
+    """A checkpoint of a run on user-supplied vectors, loaded with the same
+    list: add_vectors continues with the list's next vectors (the saved
+    ones are skipped), as an uninterrupted run does."""
+    from kwant_gb300 import kpm, lattices
+    syst = lattices.square(10, seed=2)
+    n = syst.hamiltonian_submatrix(sparse=True).shape[0]
+    vecs = list(np.exp(2j * np.pi * np.random.RandomState(4)
+                       .random_sample((6, n))))
+    kw = dict(num_moments=24, bounds=(-4.6, 4.6))
+    sd = kpm.SpectralDensity(syst, vector_factory=vecs, num_vectors=3, **kw)
+    f = tmp_path / 'ckpt.npz'
+    sd.save(f)
+    sd2 = kpm.SpectralDensity.load(f, syst, vector_factory=vecs)
+    sd2.add_vectors(3)
+    full = kpm.SpectralDensity(syst, vector_factory=vecs, num_vectors=6, **kw)
+    assert np.array_equal(np.array(sd2._moments_list),
+                          np.array(full._moments_list))
+
+
 def test_checkpoint_needs_accumulated_vectors(tmp_path):
     from kwant_gb300 import kpm, lattices
     syst = lattices.square(8, seed=1)
