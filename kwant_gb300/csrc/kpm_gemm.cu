@@ -97,7 +97,6 @@ gemm_bf16x3_simt_kernel(const __nv_bfloat16* __restrict__ A,
   const int64_t chunk = ceil_div(K, splits);
   const int64_t ks = sp * chunk;
   const int64_t ke = ks + chunk < K ? ks + chunk : K;
-  const int64_t plane = M * Kp;
   __shared__ float As[4][GT][GK + 1], Bs[4][GT][GK + 1];
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
   float ar[2][2] = {{0, 0}, {0, 0}}, ai[2][2] = {{0, 0}, {0, 0}};
@@ -108,10 +107,10 @@ gemm_bf16x3_simt_kernel(const __nv_bfloat16* __restrict__ A,
       const int64_t ma = tm * GT + r, nb = tn * GT + r;
       for (int q = 0; q < 4; ++q) {
         As[q][r][c] = (kk < ke && ma < M)
-                          ? __bfloat162float(A[q * plane + ma * Kp + kk])
+                          ? __bfloat162float(A[store_index(M, q, ma, kk)])
                           : 0.f;
         Bs[q][r][c] = (kk < ke && nb < M)
-                          ? __bfloat162float(B[q * plane + nb * Kp + kk])
+                          ? __bfloat162float(B[store_index(M, q, nb, kk)])
                           : 0.f;
       }
     }

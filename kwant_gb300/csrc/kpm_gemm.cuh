@@ -11,23 +11,36 @@ enum { STORE_C128 = 0, STORE_BF16X3 = 1 };
 
 // K padding of the BF16x3 planes: a multiple of the tensor-core K tile.
 constexpr int64_t STORE_KPAD = 128;
+// BF16x3 planes are K-blocked: [K / KB][plane][row][K % KB].  A tensor-core
+// pipeline stage (KB or KB/2 K-elements of 128 rows and 4 planes) is then
+// four contiguous runs of 128 x 64 bytes, instead of 512 pieces of 64 bytes
+// one row stride (the whole K extent, 2.5 MB on the Kubo workload) apart.
+constexpr int64_t STORE_KB = 32;
+
+__host__ __device__ inline int64_t store_index(int64_t M, int q, int64_t n,
+                                               int64_t k) {
+  return ((k / STORE_KB) * 4 * M + q * M + n) * STORE_KB + (k % STORE_KB);
+}
 
 struct StoreRow {
   double2* c128;            // STORE_C128 row
-  __nv_bfloat16* p[4];      // STORE_BF16X3 row: re_hi, re_lo, im_hi, im_lo
+  __nv_bfloat16* planes;    // STORE_BF16X3: the store's planes (re_hi,
+  int64_t M, n;             //   re_lo, im_hi, im_lo) and the row n
 };
 
 struct Store {
   int kind = STORE_C128;
-  int64_t M = 0, K = 0, Kp = 0;  // rows, logical K, padded K (row stride)
+  int64_t M = 0, K = 0, Kp = 0;  // rows, logical K, padded K
   double2* c128 = nullptr;
-  __nv_bfloat16* planes = nullptr;  // 4 planes of M x Kp
+  __nv_bfloat16* planes = nullptr;  // 4 K-blocked planes of M x Kp
   StoreRow row(int64_t n) const {
     StoreRow r{};
     if (kind == STORE_C128) {
       r.c128 = c128 + n * K;
     } else {
-      for (int q = 0; q < 4; ++q) r.p[q] = planes + (q * M + n) * Kp;
+      r.planes = planes;
+      r.M = M;
+      r.n = n;
     }
     return r;
   }
@@ -46,12 +59,14 @@ __device__ __forceinline__ void store_put(const StoreRow& r, int64_t k, S re,
     r.c128[k] = make_double2((double)re, (double)im);
   } else {
     __nv_bfloat16 h, l;
+    const int64_t i = store_index(r.M, 0, r.n, k);
+    const int64_t ps = r.M * STORE_KB;    // plane step within a K block
     split_bf16((float)re, h, l);
-    r.p[0][k] = h;
-    r.p[1][k] = l;
+    r.planes[i] = h;
+    r.planes[i + ps] = l;
     split_bf16((float)im, h, l);
-    r.p[2][k] = h;
-    r.p[3][k] = l;
+    r.planes[i + 2 * ps] = h;
+    r.planes[i + 3 * ps] = l;
   }
 }
 

@@ -14,9 +14,10 @@
 //
 // One CTA computes a 128 x NT output tile of both Re and Im (2*NT <= 512
 // TMEM columns) over one K range (split-K); 4 warps: warp 0 allocates TMEM
-// and issues the TMA loads (one 3D box per operand = its four planes),
-// warp 1 issues the MMAs from one thread, all four warps drain TMEM in the
-// epilogue.  Two pipeline stages of 32 K-elements (64-byte swizzle).  The
+// and issues the TMA loads (one 4D box per operand = its four planes of one
+// K block of the K-blocked store), warp 1 issues the MMAs from one thread,
+// all four warps drain TMEM in the epilogue.  Pipeline stages of 32
+// K-elements (64-byte swizzle), as many as the shared memory holds.  The
 // split partials (FP32) are summed in FP64 in a fixed order.
 //
 // Every wait on an mbarrier is bounded (2 s of GPU time by default,
@@ -51,11 +52,10 @@ struct TcArgs {
   int stall;        // test only: the producer issues no loads
 };
 
-template <int KC>
+template <int KC, int STAGES>
 __global__ void __launch_bounds__(THREADS, 1)
 bf16x3_tc_kernel(const __grid_constant__ CUtensorMap map_a,
                  const __grid_constant__ CUtensorMap map_b, TcArgs args) {
-  constexpr int STAGES = Stage<KC>::STAGES;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   // align the dynamic shared memory to 1024 bytes (swizzle atoms)
   uint8_t* smem = reinterpret_cast<uint8_t*>(
@@ -109,9 +109,11 @@ bf16x3_tc_kernel(const __grid_constant__ CUtensorMap map_a,
       const uint32_t ph = (uint32_t)((i / STAGES) & 1);
       if (!mbar_wait(&empty[s], ph ^ 1, args.err, 1, args.wait_ns)) break;
       mbar_expect_tx(&full[s], a_bytes + b_bytes);
+      // K-blocked planes: element kx is (kx % KB) of block kx / KB
       const int kx = (int)((kc0 + i) * KC);
-      tma_load_3d(sa + s * a_bytes, &map_a, &full[s], kx, tm * TM, 0);
-      tma_load_3d(sb + s * b_bytes, &map_b, &full[s], kx, tn * nt, 0);
+      const int kb = kx / (int)STORE_KB, ki = kx % (int)STORE_KB;
+      tma_load_4d(sa + s * a_bytes, &map_a, &full[s], ki, tm * TM, 0, kb);
+      tma_load_4d(sb + s * b_bytes, &map_b, &full[s], ki, tn * nt, 0, kb);
       ++issued;
     }
     drain_loads(full, STAGES, issued, args.err, args.wait_ns);
@@ -236,8 +238,10 @@ __global__ void tc_reduce_kernel(const float2* __restrict__ part, int splits,
   out[i] = make_double2(r * scale, im * scale);
 }
 
-// 3D map over the four planes of a store: dims {Kp, M, 4}, box {KC, rows, 4},
-// swizzled over the 2*KC-byte rows.
+// 4D map over the four K-blocked planes of a store: dims {KB, M, 4,
+// Kp / KB}, box {KC, rows, 4, 1}, swizzled over the 2*KC-byte rows (the box
+// lands in shared memory as [plane][row][KC], as a 3D box over row-major
+// planes would).
 template <int KC>
 static int make_map(CUtensorMap* map, const Store* s, int box_rows) {
   auto fn = encode_fn();
@@ -245,12 +249,14 @@ static int make_map(CUtensorMap* map, const Store* s, int box_rows) {
     set_error("cuTensorMapEncodeTiled unavailable");
     return KPM_ECUDA;
   }
-  cuuint64_t dims[3] = {(cuuint64_t)s->Kp, (cuuint64_t)s->M, 4};
-  cuuint64_t strides[2] = {(cuuint64_t)s->Kp * 2,
-                           (cuuint64_t)s->M * s->Kp * 2};
-  cuuint32_t box[3] = {(cuuint32_t)KC, (cuuint32_t)box_rows, 4};
-  cuuint32_t estr[3] = {1, 1, 1};
-  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, s->planes, dims,
+  cuuint64_t dims[4] = {(cuuint64_t)STORE_KB, (cuuint64_t)s->M, 4,
+                        (cuuint64_t)(s->Kp / STORE_KB)};
+  cuuint64_t strides[3] = {(cuuint64_t)STORE_KB * 2,
+                           (cuuint64_t)s->M * STORE_KB * 2,
+                           (cuuint64_t)4 * s->M * STORE_KB * 2};
+  cuuint32_t box[4] = {(cuuint32_t)KC, (cuuint32_t)box_rows, 4, 1};
+  cuuint32_t estr[4] = {1, 1, 1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, s->planes, dims,
                   strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                   KC == 32 ? CU_TENSOR_MAP_SWIZZLE_64B
                            : CU_TENSOR_MAP_SWIZZLE_32B,
@@ -265,18 +271,16 @@ static int make_map(CUtensorMap* map, const Store* s, int box_rows) {
 
 }  // namespace tc
 
-template <int KC>
+template <int KC, int STAGES>
 static int gemm_bf16x3_tc_kc(kpm_handle* h, const Store* omega,
-                             const Store* psi, int64_t M, int64_t R,
+                             const Store* psi, int64_t M, int64_t R, int nt,
                              double* mu_host) {
   using namespace tc;
-  constexpr int STAGES = Stage<KC>::STAGES;
   KPM_REQUIRE(omega->kind == STORE_BF16X3 && psi->kind == STORE_BF16X3,
               "tensor-core contraction needs BF16x3 stores");
   KPM_REQUIRE(omega->Kp % KC == 0 && omega->Kp == psi->Kp,
               "store K padding mismatch");
   KPM_REQUIRE(M < (1 << 20), "too many moments");
-  int nt = (int)round_up(M < 256 ? M : 256, 16);
   const int ntiles_n = (int)ceil_div(M, nt);
   int tmem_cols = 32;
   while (tmem_cols < 2 * nt) tmem_cols *= 2;
@@ -297,7 +301,7 @@ static int gemm_bf16x3_tc_kc(kpm_handle* h, const Store* omega,
   const size_t a_bytes = 4 * TM * KC * 2, b_bytes = (size_t)4 * nt * KC * 2;
   const size_t smem = 1024 + STAGES * (a_bytes + b_bytes) +
                       (2 * STAGES + 1) * 8 + 16;
-  KPM_CUDA(cudaFuncSetAttribute(bf16x3_tc_kernel<KC>,
+  KPM_CUDA(cudaFuncSetAttribute(bf16x3_tc_kernel<KC, STAGES>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem));
   float2* part = nullptr;
@@ -316,7 +320,7 @@ static int gemm_bf16x3_tc_kc(kpm_handle* h, const Store* omega,
     TcArgs args{M,    kchunks, splits, nt,      ntiles_n,
                 tmem_cols, part, err,  wc.ns,   wc.stall};
     cudaEventRecord(h->ev_gemm0, h->stream);
-    bf16x3_tc_kernel<KC><<<(unsigned)(tiles * splits), THREADS, smem,
+    bf16x3_tc_kernel<KC, STAGES><<<(unsigned)(tiles * splits), THREADS, smem,
                            h->stream>>>(map_a, map_b, args);
     count_launch(1);
     e = cudaGetLastError();
@@ -361,12 +365,32 @@ static int gemm_bf16x3_tc_kc(kpm_handle* h, const Store* omega,
   return KPM_OK;
 }
 
+// Output tile width nt (MMA N, <= 256; KPM_TC_NT=128 narrows it) and as
+// many pipeline stages as the shared memory holds (at most 4): a 128 x 256
+// tile has 96 KB stages (2), a 128 x 128 tile 64 KB (3).  Measured on the
+// Kubo workload (M = 256, K = 1.28e6, K-blocked stores): 1.11 ms either
+// way (0.95 of the measured BF16 peak); the 256-wide tiles split K over
+// twice as many CTAs, so each FP32 accumulator sums half as many products
+// (moments-matrix error 1.0e-4 against 2.0e-4 relative).  Before the
+// stores were K-blocked the same kernel took 3.09 ms (row-major planes: a
+// stage gathered 512 pieces of 64 bytes, each a 2.5 MB row stride apart).
 int gemm_bf16x3(kpm_handle* h, const Store* omega, const Store* psi,
                 int64_t M, int64_t K, int64_t R, double* mu_host) {
   (void)K;
-  if (h->tc_kc == 32)
-    return gemm_bf16x3_tc_kc<32>(h, omega, psi, M, R, mu_host);
-  return gemm_bf16x3_tc_kc<16>(h, omega, psi, M, R, mu_host);
+  int nt_max = 256;
+  if (const char* e = getenv("KPM_TC_NT")) nt_max = atoi(e) >= 256 ? 256 : 128;
+  const int nt = (int)round_up(M < nt_max ? M : nt_max, 16);
+  if (h->tc_kc != 32)
+    return gemm_bf16x3_tc_kc<16, tc::Stage<16>::STAGES>(h, omega, psi, M, R,
+                                                        nt, mu_host);
+  const size_t stage = (size_t)4 * (tc::TM + nt) * 32 * 2;
+  const size_t budget = 227 * 1024 - 2048;
+  const size_t stages = budget / stage;
+  if (stages >= 4)
+    return gemm_bf16x3_tc_kc<32, 4>(h, omega, psi, M, R, nt, mu_host);
+  if (stages == 3)
+    return gemm_bf16x3_tc_kc<32, 3>(h, omega, psi, M, R, nt, mu_host);
+  return gemm_bf16x3_tc_kc<32, 2>(h, omega, psi, M, R, nt, mu_host);
 }
 
 }  // namespace kpm
