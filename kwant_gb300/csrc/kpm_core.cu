@@ -810,6 +810,24 @@ __global__ void moments_to_host_order_kernel(const double2* __restrict__ in,
 }
 
 // --------------------------------------------------------------- dispatch
+
+// Per-launch profiling (kpm_profile): an event pair around the next
+// step launch on the handle's stream; *e1 = the closing event, or nullptr
+// when profiling is off.
+int prof_begin(kpm_handle* h, cudaEvent_t* e1) {
+  *e1 = nullptr;
+  if (!h->profiling) return KPM_OK;
+  while (h->prof_events.size() < h->prof_used + 2) {
+    cudaEvent_t e;
+    KPM_CUDA(cudaEventCreate(&e));
+    h->prof_events.push_back(e);
+  }
+  KPM_CUDA(cudaEventRecord(h->prof_events[h->prof_used], h->stream));
+  *e1 = h->prof_events[h->prof_used + 1];
+  h->prof_used += 2;
+  return KPM_OK;
+}
+
 template <bool MIXED, int MODE, bool DOTS, int VPL = (MIXED ? 2 : 1)>
 static int launch_step_t(kpm_handle* h, const StepArgs& a) {
   static int occ = -1;
@@ -822,18 +840,8 @@ static int launch_step_t(kpm_handle* h, const StepArgs& a) {
   int64_t work = (int64_t)a.xitems * a.groups;
   int64_t grid = (int64_t)occ * h->num_sms;
   if (grid > work) grid = work;
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
-  if (h->profiling) {
-    while (h->prof_events.size() < h->prof_used + 2) {
-      cudaEvent_t e;
-      KPM_CUDA(cudaEventCreate(&e));
-      h->prof_events.push_back(e);
-    }
-    e0 = h->prof_events[h->prof_used];
-    e1 = h->prof_events[h->prof_used + 1];
-    h->prof_used += 2;
-    KPM_CUDA(cudaEventRecord(e0, h->stream));
-  }
+  cudaEvent_t e1 = nullptr;
+  KPM_TRY(prof_begin(h, &e1));
   cheb_step_kernel<MIXED, MODE, DOTS, VPL>
       <<<(unsigned)grid, STEP_THREADS, 0, h->stream>>>(a);
   count_launch(1);
@@ -906,8 +914,6 @@ StepArgs step_args(kpm_block* b, const void* x, const void* prev, void* out) {
   return a;
 }
 
-// Advance the block's recursion by one matvec.  On the first call alpha_1 =
-// H~ alpha_0; afterwards alpha_{n+1} = 2 H~ alpha_n - alpha_{n-1}.
 int check_bounds(kpm_handle* h, const char* where) {
 #ifdef KPM_CHECK
   if (!h->check) return KPM_OK;
@@ -928,26 +934,37 @@ int check_bounds(kpm_handle* h, const char* where) {
   return KPM_OK;
 }
 
-int block_advance(kpm_block* b, bool dots) {
-  void* x = b->p_cur;
+// The output buffer of the step that advances a block from p_cur, its
+// alpha_{n-1} input and the step mode: alpha_1 goes to buf[0]; afterwards
+// alpha_{n+1} overwrites alpha_{n-1} in place, except a kept alpha_0.
+static void* next_out(kpm_block* b, const void** prev, int* mode) {
   if (b->steps_done == 0) {
-    void* out = b->buf[0];
-    StepArgs a = step_args(b, x, nullptr, out);
-    KPM_TRY(launch_step(b->h, STEP_FIRST, dots, a));
-    b->p_prev = b->p_cur;
-    b->p_cur = out;
-  } else {
-    void* out;
-    if (b->p_prev == b->a0 && b->keep_a0)
-      out = (b->p_cur == b->buf[0]) ? b->buf[1] : b->buf[0];
-    else
-      out = b->p_prev;  // in place: alpha_{n+1} overwrites alpha_{n-1}
-    StepArgs a = step_args(b, x, b->p_prev, out);
-    KPM_TRY(launch_step(b->h, STEP_RECUR, dots, a));
-    b->p_prev = b->p_cur;
-    b->p_cur = out;
+    *prev = nullptr;
+    *mode = STEP_FIRST;
+    return b->buf[0];
   }
+  *prev = b->p_prev;
+  *mode = STEP_RECUR;
+  if (b->p_prev == b->a0 && b->keep_a0)
+    return (b->p_cur == b->buf[0]) ? b->buf[1] : b->buf[0];
+  return b->p_prev;
+}
+
+static void rotate(kpm_block* b, void* out) {
+  b->p_prev = b->p_cur;
+  b->p_cur = out;
   b->steps_done += 1;
+}
+
+// Advance the block's recursion by one matvec.  On the first call alpha_1 =
+// H~ alpha_0; afterwards alpha_{n+1} = 2 H~ alpha_n - alpha_{n-1}.
+int block_advance(kpm_block* b, bool dots) {
+  const void* prev;
+  int mode;
+  void* out = next_out(b, &prev, &mode);
+  StepArgs a = step_args(b, b->p_cur, prev, out);
+  KPM_TRY(launch_step(b->h, mode, dots, a));
+  rotate(b, out);
   return KPM_OK;
 }
 
@@ -962,34 +979,20 @@ uint32_t* block_lo(const kpm_block* b, const void* hi) {
 // block_advance on hi + lo vectors: the same buffer rotation, with each lo
 // part following its hi part.
 int block_advance_hilo(kpm_block* b) {
-  void* x = b->p_cur;
-  void* out;
-  const void* prev = nullptr;
+  const void* prev;
   int mode;
-  if (b->steps_done == 0) {
-    out = b->buf[0];
-    mode = STEP_FIRST;
-  } else {
-    if (b->p_prev == b->a0 && b->keep_a0)
-      out = (b->p_cur == b->buf[0]) ? b->buf[1] : b->buf[0];
-    else
-      out = b->p_prev;
-    prev = b->p_prev;
-    mode = STEP_RECUR;
-  }
+  void* out = next_out(b, &prev, &mode);
   HiloArgs q{};
-  q.xlo = block_lo(b, x);
+  q.xlo = block_lo(b, b->p_cur);
   q.plo = block_lo(b, prev);
   q.olo = block_lo(b, out);
   if (!q.xlo || !q.olo || (mode == STEP_RECUR && !q.plo)) {
     set_error("compensated step: block has no lo part for its buffers");
     return KPM_ESTATE;
   }
-  StepArgs a = step_args(b, x, prev, out);
+  StepArgs a = step_args(b, b->p_cur, prev, out);
   KPM_TRY(launch_step_hilo(b->h, mode, a, q));
-  b->p_prev = b->p_cur;
-  b->p_cur = out;
-  b->steps_done += 1;
+  rotate(b, out);
   return KPM_OK;
 }
 
@@ -1000,27 +1003,13 @@ int block_advance_store(kpm_block* b, int smode, const float2* vell,
     set_error("fused store needs a complex64 ELL handle");
     return KPM_EUNSUPPORTED;
   }
-  void* x = b->p_cur;
-  void* out;
-  const void* prev = nullptr;
+  const void* prev;
   int mode;
-  if (b->steps_done == 0) {
-    out = b->buf[0];
-    mode = STEP_FIRST;
-  } else {
-    if (b->p_prev == b->a0 && b->keep_a0)
-      out = (b->p_cur == b->buf[0]) ? b->buf[1] : b->buf[0];
-    else
-      out = b->p_prev;
-    prev = b->p_prev;
-    mode = STEP_RECUR;
-  }
-  StepArgs a = step_args(b, x, prev, out);
+  void* out = next_out(b, &prev, &mode);
+  StepArgs a = step_args(b, b->p_cur, prev, out);
   StoreArgs sa{smode, vell, row, R};
   KPM_TRY(launch_step_ell(h, mode, false, a, &sa));
-  b->p_prev = b->p_cur;
-  b->p_cur = out;
-  b->steps_done += 1;
+  rotate(b, out);
   return KPM_OK;
 }
 

@@ -65,6 +65,8 @@ struct HiloArgs {
 };
 
 void count_launch(int n);
+// event pair around the next launch when profiling (*e1: closing event)
+int prof_begin(kpm_handle* h, cudaEvent_t* e1);
 int dev_alloc(void** p, size_t bytes, cudaStream_t s);
 void dev_free(void* p, cudaStream_t s);
 int init_device(int* device, int* num_sms);

@@ -462,18 +462,8 @@ static int launch_hilo_t(kpm_handle* h, const StepArgs& a,
   const int64_t work = (int64_t)a.xitems * a.groups;
   int64_t grid = (int64_t)occ * h->num_sms;
   if (grid > work) grid = work;
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
-  if (h->profiling) {
-    while (h->prof_events.size() < h->prof_used + 2) {
-      cudaEvent_t e;
-      KPM_CUDA(cudaEventCreate(&e));
-      h->prof_events.push_back(e);
-    }
-    e0 = h->prof_events[h->prof_used];
-    e1 = h->prof_events[h->prof_used + 1];
-    h->prof_used += 2;
-    KPM_CUDA(cudaEventRecord(e0, h->stream));
-  }
+  cudaEvent_t e1 = nullptr;
+  KPM_TRY(prof_begin(h, &e1));
   cheb_step_hilo_kernel<K, MODE, D0>
       <<<(unsigned)grid, Cfg::THREADS, Cfg::SMEM, h->stream>>>(
           a, q, D0 ? h->dg_idx : h->H.ell_idx,
