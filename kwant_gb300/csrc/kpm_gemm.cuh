@@ -70,6 +70,23 @@ __device__ __forceinline__ void store_put(const StoreRow& r, int64_t k, S re,
   }
 }
 
+// Two K-adjacent complex values (k even) into a BF16x3 store row: each
+// plane gets one 4-byte bf16x2 write; the same roundings as store_put.
+__device__ __forceinline__ void store_put2_bf16x3(const StoreRow& r, int64_t k,
+                                                  float re0, float im0,
+                                                  float re1, float im1) {
+  const int64_t i = store_index(r.M, 0, r.n, k);
+  const int64_t ps = r.M * STORE_KB;
+  __nv_bfloat162* p = reinterpret_cast<__nv_bfloat162*>(r.planes + i);
+  const int64_t ps2 = ps / 2;
+  const __nv_bfloat162 hr = __floats2bfloat162_rn(re0, re1);
+  const __nv_bfloat162 hi = __floats2bfloat162_rn(im0, im1);
+  p[0] = hr;
+  p[ps2] = __floats2bfloat162_rn(re0 - __low2float(hr), re1 - __high2float(hr));
+  p[2 * ps2] = hi;
+  p[3 * ps2] = __floats2bfloat162_rn(im0 - __low2float(hi), im1 - __high2float(hi));
+}
+
 int store_alloc(Store* s, int kind, int64_t M, int64_t K, cudaStream_t st);
 void store_free(Store* s, cudaStream_t st);
 

@@ -9,7 +9,8 @@
 //
 // A slot is 8 lanes with two (16-vector groups) or four (32-vector groups)
 // complex64 vectors per lane: 128 or 256 bytes per row, and four rows in
-// flight per warp.  The column indices and values of a warp's next four
+// flight per warp (the correlator's store steps on 16-vector blocks: 4
+// lanes of four vectors, eight rows per warp).  The column indices and values of a warp's next four
 // rows are copied into shared memory with cp.async (16-byte chunks, no
 // row-pointer load) while the current ones compute, so a row's gathers go
 // out together with its own vector entry and its alpha_{n-1} entry: one
@@ -29,6 +30,16 @@ namespace kpm {
 #ifndef KPM_ELL_MIN_BLOCKS
 #define KPM_ELL_MIN_BLOCKS 4
 #endif
+// Lanes per row of the store steps of 16-vector blocks: 4 (four vectors
+// per lane, eight rows per warp) or 8 (two vectors per lane, four rows).
+// Measured on the Kubo workload (Rashba square 200 x 200 x 2 orbitals,
+// R = 16, M = 256): 9.19 ms per conductivity with 4, 9.62 ms with 8; a
+// grid of one block per row group instead of resident blocks looping over
+// them: 9.37 and 10.59 ms.
+#ifndef KPM_STORE_SW
+#define KPM_STORE_SW 4
+#endif
+
 template <int K, int RPI>
 constexpr int ell_min_blocks() {
   return RPI != 1 ? 1 : KPM_ELL_MIN_BLOCKS;
@@ -79,7 +90,7 @@ __global__ void __launch_bounds__(STEP_THREADS, ell_min_blocks<K, RPI>())
 cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
                      const float2* __restrict__ eval, StoreArgs sa) {
   static_assert(SM == 0 || (!DOTS && RPI == 1), "store fusion: no dots");
-  static_assert(SW == 8 || SW == 16, "8- or 16-lane slots");
+  static_assert(SW == 4 || SW == 8 || SW == 16, "4-, 8- or 16-lane slots");
   using Pay = EllPay<VPL>;
   using PT = typename Pay::T;
   constexpr int G = SW * VPL;
@@ -230,15 +241,22 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
           }
         }
         if constexpr (SM != 0) {
-          // store row of alpha_n: K index row * R + vector, real vectors only
+          // store row of alpha_n: K index row * R + vector, real vectors
+          // only; pairs of K-adjacent vectors as bf16x2 writes when R is even
 #pragma unroll
-          for (int k = 0; k < VPL; ++k) {
+          for (int k = 0; k < VPL; k += 2) {
             const int64_t vec = (int64_t)g * G + (int64_t)lane * VPL + k;
-            if (vec < sa.R) {
-              const float re = SM == 2 ? sr[k] : Pay::re(xv[u], k);
-              const float im = SM == 2 ? si[k] : Pay::im(xv[u], k);
-              store_put<STORE_BF16X3>(sa.store, (int64_t)row[u] * sa.R + vec,
-                                      re, im);
+            const int64_t kk = (int64_t)row[u] * sa.R + vec;
+            const float re0 = SM == 2 ? sr[k] : Pay::re(xv[u], k);
+            const float im0 = SM == 2 ? si[k] : Pay::im(xv[u], k);
+            const float re1 = SM == 2 ? sr[k + 1] : Pay::re(xv[u], k + 1);
+            const float im1 = SM == 2 ? si[k + 1] : Pay::im(xv[u], k + 1);
+            if ((sa.R & 1) == 0) {
+              if (vec < sa.R) store_put2_bf16x3(sa.store, kk, re0, im0, re1, im1);
+            } else {
+              if (vec < sa.R) store_put<STORE_BF16X3>(sa.store, kk, re0, im0);
+              if (vec + 1 < sa.R)
+                store_put<STORE_BF16X3>(sa.store, kk + 1, re1, im1);
             }
           }
         }
@@ -326,15 +344,34 @@ static int launch_ell_t(kpm_handle* h, const StepArgs& a,
 }
 
 // Store steps (no dot products).  Blocks of 16 vectors (one complex64
-// vector per lane in 16-lane slots) run as 8-lane slots of two vectors per
-// lane: the same 128 bytes per row, twice the rows in flight per warp, and
-// each vector's arithmetic unchanged.
-template <int K, int VPL, int SM>
+// vector per lane in 16-lane slots) run as KPM_STORE_SW-lane slots of
+// 16 / KPM_STORE_SW vectors per lane: the same 128 bytes per row, more rows
+// in flight per warp, and each vector's arithmetic unchanged.
+template <int K, int VPL, int SM, int SW = 8>
 static int dispatch_store_mode(kpm_handle* h, int mode, const StepArgs& a,
                                const StoreArgs& sa) {
   return mode == STEP_FIRST
-             ? launch_ell_t<K, STEP_FIRST, false, 1, VPL, SM>(h, a, sa)
-             : launch_ell_t<K, STEP_RECUR, false, 1, VPL, SM>(h, a, sa);
+             ? launch_ell_t<K, STEP_FIRST, false, 1, VPL, SM, SW>(h, a, sa)
+             : launch_ell_t<K, STEP_RECUR, false, 1, VPL, SM, SW>(h, a, sa);
+}
+
+template <int SW>
+static int dispatch_store_16(kpm_handle* h, int mode, const StepArgs& a,
+                             const StoreArgs& sa) {
+  constexpr int VPL = 16 / SW;
+  switch (h->H.ell_k) {
+#define KPM_STORE_CASE(KK)                                                 \
+  case KK:                                                                 \
+    return sa.smode == 2 ? dispatch_store_mode<KK, VPL, 2, SW>(h, mode, a, sa) \
+                         : dispatch_store_mode<KK, VPL, 1, SW>(h, mode, a, sa);
+    KPM_STORE_CASE(4)
+    KPM_STORE_CASE(8)
+    KPM_STORE_CASE(12)
+    KPM_STORE_CASE(16)
+#undef KPM_STORE_CASE
+  }
+  set_error("ELL width %d not supported", h->H.ell_k);
+  return KPM_EUNSUPPORTED;
 }
 
 template <int K, int VPL>
@@ -371,6 +408,12 @@ static int dispatch_k(kpm_handle* h, int mode, bool dots, const StepArgs& a,
 int launch_step_ell(kpm_handle* h, int mode, bool dots, const StepArgs& a,
                     const StoreArgs* sa) {
   StepArgs w = a;
+  if (sa && sa->smode && a.vpl == 1 && KPM_STORE_SW != 8) {
+    constexpr int SW = KPM_STORE_SW;
+    w.vpl = 16 / SW;
+    w.rp = a.rp / w.vpl;
+    return dispatch_store_16<SW>(h, mode, w, *sa);
+  }
   w.vpl = 2 * a.vpl;
   w.rp = a.rp / 2;
   return a.vpl == 1 ? dispatch_k<2>(h, mode, dots, w, sa)
