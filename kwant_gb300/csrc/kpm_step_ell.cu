@@ -111,6 +111,10 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
   const PT* prev = reinterpret_cast<const PT*>(p.prev);
   PT* out = reinterpret_cast<PT*>(p.out);
   const int work = p.xitems * p.groups;
+  // the next store step may launch now: its blocks take the SM slots this
+  // grid frees and stage their first rows while this grid finishes
+  if constexpr (SM != 0)
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   // row counters in 32 bits (CSR indices are int32); addresses in 64
   const int rows = (int)p.rows;
   const int stride = p.xitems * NSLOT;
@@ -157,6 +161,10 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
     const int wb0 = xi * NSLOT + SPW * wq;
     if (wb0 < rows) stage(wb0, 0);
     cp_async_commit();
+    // store steps run as programmatic dependent launches: H's entries above
+    // are constant, everything below reads or overwrites the vectors of
+    // the previous step, which this wait sees completed
+    if constexpr (SM != 0) asm volatile("griddepcontrol.wait;" ::: "memory");
     int sb = 0;
     for (int wb = wb0; wb < rows; wb += RPI * stride) {
       if (wb + RPI * stride < rows) stage(wb + RPI * stride, sb ^ 1);
@@ -334,9 +342,27 @@ static int launch_ell_t(kpm_handle* h, const StepArgs& a,
   if (grid > work) grid = work;
   cudaEvent_t e1 = nullptr;
   KPM_TRY(prof_begin(h, &e1));
-  cheb_step_ell_kernel<K, MODE, DOTS, RPI, VPL, SM, SW>
-      <<<(unsigned)grid, STEP_THREADS, 0, h->stream>>>(a, h->H.ell_idx,
-                                                        h->H.ell_val, sa);
+  if constexpr (SM != 0) {
+    // programmatic dependent launch (the kernel waits for its predecessor
+    // in griddepcontrol.wait)
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(STEP_THREADS);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = h->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    KPM_CUDA(cudaLaunchKernelEx(
+        &cfg, cheb_step_ell_kernel<K, MODE, DOTS, RPI, VPL, SM, SW>, a,
+        h->H.ell_idx, h->H.ell_val, sa));
+  } else {
+    cheb_step_ell_kernel<K, MODE, DOTS, RPI, VPL, SM, SW>
+        <<<(unsigned)grid, STEP_THREADS, 0, h->stream>>>(a, h->H.ell_idx,
+                                                          h->H.ell_val, sa);
+  }
   count_launch(1);
   KPM_CHECK_LAUNCH();
   if (e1) KPM_CUDA(cudaEventRecord(e1, h->stream));
