@@ -350,12 +350,17 @@ def run_ours(args):
     avg_step_ms = step_ms / max(n_step, 1)
     achieved = B / (avg_step_ms / 1e3) / 1e9
     # DRAM bytes per step launch: ncu dram__bytes_read + dram__bytes_write
-    # of one cheb_step_ell launch on the 500 x 500-cell, R = 64 case (774.5
-    # MB against 794.0 MB algorithmic; the workload here is too large for a
-    # multi-pass capture), scaled to this launch by its algorithmic bytes
+    # of one step launch on the 500 x 500-cell, R = 64 case (the workload
+    # here is too large for a multi-pass capture), scaled to this launch by
+    # its algorithmic bytes: cheb_step_hilo_kernel 884.2 + 354.7 MB against
+    # 1178.0 MB ('mixed'), cheb_step_ell_kernel 774.5 MB against 794.0 MB
+    # ('single')
     traffic = None
-    if args.precision == 'single' and args.reorder and R == 64:
-        traffic = B * (774.5 / 794.0)
+    if args.reorder and R == 64:
+        if args.precision == 'mixed':
+            traffic = B * ((884.2 + 354.7) / 1178.0)
+        elif args.precision == 'single':
+            traffic = B * (774.5 / 794.0)
 
     # ---- accuracy vs the FP64 path (untimed) -------------------------------
     accuracy = None
@@ -722,9 +727,10 @@ def kubo_record(args, steps, warmup, cpu=True, accuracy=True):
         'roofline': {'bound': 'tensor', 'achieved': achieved, 'peak': tpeak,
                      'unit': 'TFLOP/s', 'frac': achieved / tpeak,
                      # ncu dram bytes of one launch on the 60 x 60 x 2,
-                     # R = 16 case: 475.9 MB against 472.0 MB of operands
-                     # (4 BF16 planes x M x K_pad x 2 operands), scaled
-                     'traffic': (475.9 / 472.0) * 16.0 * M * g_fl /
+                     # R = 16 case: 472.4 + 4.1 MB against 472.0 MB of
+                     # operands (4 BF16 planes x M x K_pad x 2 operands),
+                     # scaled
+                     'traffic': (476.5 / 472.0) * 16.0 * M * g_fl /
                                 (24.0 * M * M) if g_fl else None,
                      'kernel': 'bf16x3_tc_kernel',
                      'mma_flops_per_launch': g_fl, 'avg_launch_ms': g_ms,
