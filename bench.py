@@ -589,7 +589,8 @@ def run_ldos(args):
     if os.path.exists(pk):
         peaks = json.load(open(pk))
     hbm = float(peaks.get('hbm_gbs', 6800.0))
-    B = step_bytes(nnz, n, R, 'mixed')
+    # the operator path advances plain complex64 vectors (8 B per element)
+    B = step_bytes(nnz, n, R, 'single')
     avg = step_ms / max(n_step, 1)
     achieved = B / (avg / 1e3) / 1e9
     line = {

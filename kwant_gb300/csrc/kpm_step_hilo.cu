@@ -31,10 +31,15 @@
 //     most half an ulp of hi, so the split is unique and a vector downloaded
 //     as complex128 (hi + lo, exact) uploads to the same hi and lo.
 // The fused dot products use the hi parts: mu_0 and mu_1 in FP64 from hi+lo
-// (once), then <a_n|a_n> and Re <a_n+1|a_n> with Ogita-Rump-Oishi Dot2
-// (TwoProd + TwoSum, flushed to FP64 every 128 rows) and Im <a_n+1|a_n> as
-// a plain FP32 sum.  Leaving out lo in these dots is a zero-mean error of
-// each moment alone, not a shift of all of them.  (An anchored sum with a
+// (once), then <a_n|a_n> with Ogita-Rump-Oishi Dot2 (TwoProd + TwoSum) and
+// Re and Im <a_n+1|a_n> as plain FP32 sums, all flushed to FP64 every 128
+// rows.  Leaving out lo in these dots is a zero-mean error of each moment
+// alone, not a shift of all of them.  The sums of |a_i|^2 need the
+// compensation: their terms are all positive, and plain FP32 partials
+// (flushed every 128 or 32 rows) took the per-orbital DOS error at the
+// outermost node of the 2e6-orbital workload to 1.0e-4 or 1.0e-5 (2.6e-7
+// with Dot2).  The terms of <a_n+1|a_n> change sign, and a plain sum there
+// left the error at 2.6e-7 and saved 0.7 % of the step.  (An anchored sum with a
 // per-vector anchor >= 4 mu_0, which bounds every partial sum, was
 // measured too: the anchor is then far above a row's terms, their
 // fractional parts land in the FP32 residual sum, and its bias took the
@@ -109,14 +114,6 @@ __device__ __forceinline__ uint32_t lo_pack_rz(float2 v) {
 }
 __device__ __forceinline__ void cp_async8(void* dst, const void* src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(
-                   static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
-               "l"(src)
-               : "memory");
-}
-// 16-byte asynchronous global -> shared copy through L1 (gathered rows:
-// the rows of a warp share neighbours)
-__device__ __forceinline__ void cp_async16_ca(void* dst, const void* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(
                    static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
                "l"(src)
                : "memory");
@@ -248,7 +245,7 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
 #pragma unroll
     for (int t = 0; t < K; ++t) {
       const int64_t oc = off(col_index(p, ci[t]), col);
-      cp_async16_ca(dh + (GATH + t) * T, x + oc);
+      cp_async16(dh + (GATH + t) * T, x + oc);
       cp_async8(dl + (GATH + t) * T, xl + oc);
     }
   };
@@ -257,7 +254,10 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
   // side by side (they share the partition's ELL rows in L2).  Measured on
   // the 2e6-orbital graphene workload, R = 64: 1.08 ms per step against
   // 1.12 ms sub-group-major; blocks of 192 or 160 threads (3 or 4 per SM)
-  // were slower still (1.15-1.22 ms)
+  // were slower still (1.15-1.22 ms), and so were blocks of 128 threads at
+  // 4 or 5 per SM (1.03 and 1.33 ms against 1.01 ms).  The gathered hi
+  // slices are copied through L2 only (cp.async.cg): 1.026 -> 1.010 ms
+  // against copies that also allocate in L1 (15 % L1 hit rate)
   for (int w = blockIdx.x; w < work; w += gridDim.x) {
     const int xi = w / p.groups;
     const int g = w - xi * p.groups;
@@ -265,13 +265,13 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
     double* my = red + slot * (G * 3) + lane * 6;   // vectors 2 lane, +1
 #pragma unroll
     for (int e = 0; e < 6; ++e) my[e] = 0.0;
-    // compensated FP32 dots (STEP_RECUR): <a_n|a_n> as (xr^2, xi^2) sums,
-    // Re <a_n+1|a_n> as (or xr, oi xi) sums, Im plain
-    float2 dns[2], dnc[2], drs[2], drc[2];
+    // FP32 dots (STEP_RECUR): <a_n|a_n> as compensated (xr^2, xi^2) sums,
+    // Re <a_n+1|a_n> as plain (or xr, oi xi) sums, Im plain
+    float2 dns[2], dnc[2], drs[2];
     float fim[2];
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
-      dns[k] = dnc[k] = drs[k] = drc[k] = make_float2(0.f, 0.f);
+      dns[k] = dnc[k] = drs[k] = make_float2(0.f, 0.f);
       fim[k] = 0.f;
     }
     int pending = 0;
@@ -399,16 +399,16 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
 #pragma unroll
           for (int k = 0; k < 2; ++k) {
             dot2(dns[k], dnc[k], xk[k], xk[k]);
-            dot2(drs[k], drc[k], ohi[k], xk[k]);
+            drs[k] = __ffma2_rn(ohi[k], xk[k], drs[k]);
             fim[k] = fmaf(ohi[k].x, xk[k].y, fmaf(-ohi[k].y, xk[k].x, fim[k]));
           }
           if (++pending == FLUSH) {
 #pragma unroll
             for (int k = 0; k < 2; ++k) {
               my[k * 3 + 0] += pair_sum(dns[k], dnc[k]);
-              my[k * 3 + 1] += pair_sum(drs[k], drc[k]);
+              my[k * 3 + 1] += (double)drs[k].x + (double)drs[k].y;
               my[k * 3 + 2] += (double)fim[k];
-              dns[k] = dnc[k] = drs[k] = drc[k] = make_float2(0.f, 0.f);
+              dns[k] = dnc[k] = drs[k] = make_float2(0.f, 0.f);
               fim[k] = 0.f;
             }
             pending = 0;
@@ -427,7 +427,7 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
 #pragma unroll
       for (int k = 0; k < 2; ++k) {
         my[k * 3 + 0] += pair_sum(dns[k], dnc[k]);
-        my[k * 3 + 1] += pair_sum(drs[k], drc[k]);
+        my[k * 3 + 1] += (double)drs[k].x + (double)drs[k].y;
         my[k * 3 + 2] += (double)fim[k];
       }
     }
