@@ -30,8 +30,9 @@
 //   * hi = RN(v), lo = RZ_bf16(RZ(v - hi)): round toward zero keeps |lo| at
 //     most half an ulp of hi, so the split is unique and a vector downloaded
 //     as complex128 (hi + lo, exact) uploads to the same hi and lo.
-// The fused dot products use the hi parts: mu_0 and mu_1 in FP64 from hi+lo
-// (once), then <a_n|a_n> with Ogita-Rump-Oishi Dot2 (TwoProd + TwoSum) and
+// The fused dot products use the hi parts: mu_0 and mu_1 from hi + lo
+// (once, compensated; FP64 products per row took 4.6x a recursion step on
+// GB300's narrow FP64 pipe), then <a_n|a_n> with Ogita-Rump-Oishi Dot2 (TwoProd + TwoSum) and
 // Re and Im <a_n+1|a_n> as plain FP32 sums, all flushed to FP64 every 128
 // rows.  Leaving out lo in these dots is a zero-mean error of each moment
 // alone, not a shift of all of them.  The sums of |a_i|^2 need the
@@ -154,7 +155,7 @@ template <int K, bool D0> struct HiloCfg {
 // row from the previous copies, and the warp's ELL entries are staged two
 // iterations ahead (their column indices address those copies), so a row's
 // memory latency overlaps the previous row's arithmetic.  MODE STEP_FIRST:
-// a_1 = H~ a_0 with the FP64 dots mu_0 = <a_0|a_0> and <a_1|a_0>;
+// a_1 = H~ a_0 with the dots mu_0 = <a_0|a_0> and <a_1|a_0> of hi + lo;
 // STEP_RECUR: a_{n+1} = 2 H~ a_n - a_{n-1} with the compensated dots
 // <a_n|a_n>, <a_n+1|a_n>.
 //
@@ -267,13 +268,34 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
     for (int e = 0; e < 6; ++e) my[e] = 0.0;
     // FP32 dots (STEP_RECUR): <a_n|a_n> as compensated (xr^2, xi^2) sums,
     // Re <a_n+1|a_n> as plain (or xr, oi xi) sums, Im plain
-    float2 dns[2], dnc[2], drs[2];
+    // (STEP_FIRST: all three compensated, the products with lo parts added
+    // to the compensation terms)
+    float2 dns[2], dnc[2], drs[2], drc[2], dis[2], dic[2];
     float fim[2];
+    auto clear_dots = [&]() {
 #pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      dns[k] = dnc[k] = drs[k] = make_float2(0.f, 0.f);
-      fim[k] = 0.f;
-    }
+      for (int k = 0; k < 2; ++k) {
+        dns[k] = dnc[k] = drs[k] = drc[k] = dis[k] = dic[k] =
+            make_float2(0.f, 0.f);
+        fim[k] = 0.f;
+      }
+    };
+    // add the FP32 partials to the slot's FP64 accumulators
+    auto flush_dots = [&]() {
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        my[k * 3 + 0] += pair_sum(dns[k], dnc[k]);
+        if constexpr (MODE == STEP_FIRST) {
+          my[k * 3 + 1] += pair_sum(drs[k], drc[k]);
+          my[k * 3 + 2] += pair_sum(dis[k], dic[k]);
+        } else {
+          my[k * 3 + 1] += (double)drs[k].x + (double)drs[k].y;
+          my[k * 3 + 2] += (double)fim[k];
+        }
+      }
+      clear_dots();
+    };
+    clear_dots();
     int pending = 0;
 
     const int wb0 = xi * NSLOT + SPW * wq;
@@ -383,17 +405,27 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
         out[o] = make_float4(ohi[0].x, ohi[0].y, ohi[1].x, ohi[1].y);
         ol[o] = make_uint2(olw[0], olw[1]);
         if constexpr (MODE == STEP_FIRST) {
-          // mu_0 and <a_1|a_0> in FP64 from hi + lo
+          // mu_0 and <a_1|a_0> of a = hi + lo: Dot2 on the hi products, the
+          // products with a lo part (2^-8 of them, relative) as FP32 sums
+          // into the compensation terms
 #pragma unroll
           for (int k = 0; k < 2; ++k) {
             const float2 al = lo_pair(xlw[k]), bl = lo_pair(olw[k]);
-            const double ar = (double)xk[k].x + (double)al.x;
-            const double ai = (double)xk[k].y + (double)al.y;
-            const double br = (double)ohi[k].x + (double)bl.x;
-            const double bi = (double)ohi[k].y + (double)bl.y;
-            my[k * 3 + 0] += ar * ar + ai * ai;
-            my[k * 3 + 1] += br * ar + bi * ai;
-            my[k * 3 + 2] += br * ai - bi * ar;
+            dot2(dns[k], dnc[k], xk[k], xk[k]);
+            dnc[k] = __ffma2_rn(__fmul2_rn(f2(2.f), xk[k]), al, dnc[k]);
+            dnc[k] = __ffma2_rn(al, al, dnc[k]);
+            // Re <a_1|a_0> = br ar + bi ai
+            dot2(drs[k], drc[k], ohi[k], xk[k]);
+            drc[k] = __ffma2_rn(ohi[k], al, drc[k]);
+            drc[k] = __ffma2_rn(bl, __fadd2_rn(xk[k], al), drc[k]);
+            // Im <a_1|a_0> = br ai - bi ar
+            const float2 u = make_float2(ohi[k].x, -ohi[k].y);
+            const float2 ul = make_float2(bl.x, -bl.y);
+            const float2 v = make_float2(xk[k].y, xk[k].x);
+            const float2 vl = make_float2(al.y, al.x);
+            dot2(dis[k], dic[k], u, v);
+            dic[k] = __ffma2_rn(u, vl, dic[k]);
+            dic[k] = __ffma2_rn(ul, __fadd2_rn(v, vl), dic[k]);
           }
         } else {
 #pragma unroll
@@ -402,17 +434,10 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
             drs[k] = __ffma2_rn(ohi[k], xk[k], drs[k]);
             fim[k] = fmaf(ohi[k].x, xk[k].y, fmaf(-ohi[k].y, xk[k].x, fim[k]));
           }
-          if (++pending == FLUSH) {
-#pragma unroll
-            for (int k = 0; k < 2; ++k) {
-              my[k * 3 + 0] += pair_sum(dns[k], dnc[k]);
-              my[k * 3 + 1] += (double)drs[k].x + (double)drs[k].y;
-              my[k * 3 + 2] += (double)fim[k];
-              dns[k] = dnc[k] = drs[k] = make_float2(0.f, 0.f);
-              fim[k] = 0.f;
-            }
-            pending = 0;
-          }
+        }
+        if (++pending == FLUSH) {
+          flush_dots();
+          pending = 0;
         }
       }
       __syncwarp();
@@ -423,14 +448,7 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
       vb ^= 1;
     }
     cp_async_wait<0>();
-    if constexpr (MODE == STEP_RECUR) {
-#pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        my[k * 3 + 0] += pair_sum(dns[k], dnc[k]);
-        my[k * 3 + 1] += (double)drs[k].x + (double)drs[k].y;
-        my[k * 3 + 2] += (double)fim[k];
-      }
-    }
+    flush_dots();
     __syncthreads();
     // partials are addressed by vector: [vector*3 + component][xitems]
     double* dst = p.partials + (int64_t)g * (G * 3) * p.xitems + xi;
