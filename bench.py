@@ -896,8 +896,71 @@ def run_batch(args):
                      'algorithmic_bytes_per_step': B,
                      'avg_step_ms': ms / steps},
     }
+    if args.accuracy:
+        line['accuracy'] = batch_accuracy(bd, bd.moments(), Ls, Ws, R, M)
+    if args.batch_mixed:
+        # the compensated mode on the same systems and vectors (one warm-up
+        # and one timed run: ~1 min each), after freeing the 'single' batch
+        bd._b.close()
+        del bd
+        bm = batch.BatchedDOS(R, M, seed=1, precision='mixed')
+        for s in range(S):
+            bm.add_wilson_dirac(int(Ls[s]), m=1.5, W=float(Ws[s]),
+                                seed=100 + s)
+        bm.moments()
+        mom = bm.moments()
+        mms, launches, _ = bm.stats()
+        Bm = int(mat_ell_mixed(Ls) + 3 * orbs * Rpad * 12)
+        rec = {'precision': 'mixed (compensated single-system step, system '
+                            'after system)',
+               'value': nnz * R * M / (mms / 1e3), 'unit': UNIT,
+               'ms_per_step': mms, 'gpu_launches_per_step': launches,
+               'roofline': {'bound': 'hbm',
+                            'achieved': Bm * steps / (mms / 1e3) / 1e9,
+                            'peak': hbm, 'unit': 'GB/s',
+                            'frac': Bm * steps / (mms / 1e3) / 1e9 / hbm,
+                            'traffic': None,
+                            'kernel': 'cheb_step_hilo_kernel (ELL width 16)',
+                            'algorithmic_bytes_per_step': Bm}}
+        if args.accuracy:
+            rec['accuracy'] = batch_accuracy(bm, mom, Ls, Ws, R, M)
+        bm.close()
+        line['mixed'] = rec
     print(json.dumps(line))
     return 0
+
+
+def mat_ell_mixed(Ls):
+    """Matrix bytes of one compensated ELL step over the batch: 16
+    entries per orbital row (13 non-zeros padded), 4 + 8 bytes each."""
+    return int(sum(4 * int(L) ** 3 for L in Ls)) * 16 * 12
+
+
+def batch_accuracy(bd, mom, Ls, Ws, R, M):
+    """Per-orbital DOS of the smallest system of the batch against the
+    FP64 GPU path (parity-tested against the reference fixtures) on the
+    same Hamiltonian (the device generator's disorder assembled on the
+    host), the same device-generated vectors and the same bounds, at all
+    2M Chebyshev nodes (untimed)."""
+    from kwant_gb300 import _lib, batch
+    from kwant_gb300.kpm import _chebyshev_nodes as kpm_nodes
+    s = int(np.argmin(Ls))
+    L, W = int(Ls[s]), float(Ws[s])
+    H = batch.wilson_dirac_matrix(L, 1.5, W, 100 + s)
+    n = H.shape[0]
+    a, b = bd.scales[s]
+    vecs = batch.random_phase_vectors(1, s, R, n)
+    mom64 = _lib.dos(H, a, b, _lib.PREC_FP64, vecs, M)[0].mean(axis=0)
+    ref = mom.copy()
+    ref[s] = mom64
+    _, rho = bd.densities(mom)
+    _, rho64 = bd.densities(ref)
+    err = np.abs(rho[s] - rho64[s]) / n
+    return {'dos_linf_per_orbital_vs_fp64': float(err.max()),
+            'argmax_node_x': float(kpm_nodes(2 * M)[np.argmax(err)]),
+            'system': {'L': L, 'W': W, 'orbitals': int(n)},
+            'reference': 'FP64 GPU path, same vectors and bounds, all 2M '
+                         'nodes'}
 
 
 def run_surrogate(args):
@@ -1033,6 +1096,9 @@ def main():
     p.add_argument('--batch-vectors', type=int, default=256)
     p.add_argument('--batch-moments', type=int, default=1024)
     p.add_argument('--batch-seed', type=int, default=0)
+    p.add_argument('--no-batch-mixed', dest='batch_mixed',
+                   action='store_false',
+                   help='leave the compensated batch sub-record out')
     p.add_argument('--kubo-l', type=int, default=200)
     p.add_argument('--kubo-vectors', type=int, default=16)
     p.add_argument('--kubo-moments', type=int, default=256)

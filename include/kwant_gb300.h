@@ -151,6 +151,8 @@ KPM_API int kpm_destroy(kpm_handle* h);
 /* ---- vector blocks ---------------------------------------------------------
  * R starting vectors |r> (host, R x N complex128, one vector after another:
  * the stacked output of the reference's vector factory, kwant/kpm.py:437).
+ * vecs == NULL allocates the block with zero vectors, for a following
+ * kpm_block_randomize (no host upload).
  * keep_a0 keeps |r> resident (needed for operators and for rewinding). */
 KPM_API int kpm_block_create(kpm_handle* h, const double* vecs, int64_t R,
                              int keep_a0, kpm_block** out);

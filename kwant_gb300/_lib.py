@@ -315,14 +315,24 @@ class Handle:
 class Block:
     """R vectors and their recursion state on the device."""
 
-    def __init__(self, handle, vecs, keep_a0=True):
-        vecs = c128(np.atleast_2d(vecs))
+    def __init__(self, handle, vecs, keep_a0=True, num_vectors=None):
+        """vecs: (R, N) starting vectors, or None with num_vectors = R
+        for a block of zero vectors on the device (then `randomize`)."""
         self.handle = handle
-        self.R = vecs.shape[0]
-        if vecs.shape[1] != handle.N:
-            raise ValueError('vector length does not match the Hamiltonian')
+        if vecs is None:
+            if num_vectors is None or int(num_vectors) <= 0:
+                raise ValueError('num_vectors must be positive')
+            self.R = int(num_vectors)
+            vp = None
+        else:
+            vecs = c128(np.atleast_2d(vecs))
+            self.R = vecs.shape[0]
+            if vecs.shape[1] != handle.N:
+                raise ValueError('vector length does not match the '
+                                 'Hamiltonian')
+            vp = ptr(vecs)
         b = C.c_void_p()
-        check(lib.kpm_block_create(handle.ptr, ptr(vecs), self.R,
+        check(lib.kpm_block_create(handle.ptr, vp, self.R,
                                    1 if keep_a0 else 0, C.byref(b)))
         self._b = b
         handle._children.add(self)

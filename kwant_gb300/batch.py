@@ -4,13 +4,26 @@ in a CUDA graph (``kpm_batch_*`` in include/kwant_gb300.h).
 
 This replaces looping ``kwant.kpm.SpectralDensity`` (kwant/kpm.py:163-252)
 over realisations.  Matrices are block-sparse with 4 x 4 blocks (4-orbital
-models such as the Wilson-Dirac topological insulator); the recursion is
-complex64 with FP64 moment accumulation; the random-phase vectors are drawn
-on the device from a counter-based generator whose stream
+models such as the Wilson-Dirac topological insulator).  The random-phase
+vectors are drawn on the device from a counter-based generator whose stream
 ``random_phase_vectors`` reproduces on the host.
+
+Two precisions:
+
+* ``'single'``: plain complex64 vectors with FP64 moment accumulation; every
+  system advances in one launch per step, and the whole run is one CUDA
+  graph.  On the 32-system Wilson-Dirac workload (M = 1024) the per-orbital
+  DOS is 5e-5 off the FP64 path at the outermost Chebyshev node.
+* ``'mixed'``: the compensated single-system step (complex64 plus bfloat16
+  corrections, error-free FP32 sums; the DOS gate of 1e-5), one resident
+  handle and block per system, advanced system after system, with the same
+  starting vectors as ``'single'``.
 """
 
+import time
+
 import numpy as np
+import scipy.sparse as sp
 
 from . import _lib
 
@@ -76,35 +89,82 @@ class BatchedDOS:
     num_vectors, num_moments : int (num_moments even)
     seed : int, seed of the device vector generator
     eps : float, spectral margin as in kwant.kpm (kwant/kpm.py:1174)
+    precision : 'single' (default) or 'mixed' (see the module docstring)
     """
 
-    def __init__(self, num_vectors=256, num_moments=1024, seed=0, eps=0.05):
+    def __init__(self, num_vectors=256, num_moments=1024, seed=0, eps=0.05,
+                 precision='single'):
+        if precision not in ('single', 'mixed'):
+            raise ValueError("precision must be 'single' or 'mixed'")
+        if int(num_moments) <= 0 or int(num_moments) % 2:
+            raise ValueError('num_moments must be a positive even integer')
         self.num_vectors = int(num_vectors)
         self.num_moments = int(num_moments)
         self.eps = eps
-        self._b = _lib.Batch(num_vectors, num_moments, seed)
+        self.precision = precision
+        self.seed = int(seed)
         self.scales = []
+        if precision == 'single':
+            self._b = _lib.Batch(num_vectors, num_moments, seed)
+        else:
+            self._mats = []        # host CSR per system
+            self._sys = []         # (handle, block) per system, on first run
+            self._last = (0.0, 0)
 
     def add_matrix(self, ham, bounds):
         """A system given as a (4-orbital) sparse matrix and its spectral
         bounds (lmin, lmax)."""
         a, b = _rescale(bounds[0], bounds[1], self.eps)
-        self._b.add_bsr(ham, a, b)
+        if self.precision == 'single':
+            self._b.add_bsr(ham, a, b)
+        else:
+            self._add_host(sp.csr_matrix(ham))
         self.scales.append((a, b))
 
     def add_wilson_dirac(self, L, m=1.5, W=0.0, seed=0, bounds=None):
-        """An L^3 Wilson-Dirac system generated on the device.  Default
-        bounds: the Gershgorin bound |E| <= |m - 3| + W/2 + 6."""
+        """An L^3 Wilson-Dirac system, generated on the device ('single')
+        or assembled on the host with the device generator's disorder
+        ('mixed').  Default bounds: the Gershgorin bound
+        |E| <= |m - 3| + W/2 + 6."""
         if bounds is None:
             g = abs(m - 3) + W / 2 + 6.0
             bounds = (-g, g)
         a, b = _rescale(bounds[0], bounds[1], self.eps)
-        self._b.add_wilson_dirac(L, m, W, seed, a, b)
+        if self.precision == 'single':
+            self._b.add_wilson_dirac(L, m, W, seed, a, b)
+        else:
+            self._add_host(wilson_dirac_matrix(L, m, W, seed))
         self.scales.append((a, b))
+
+    def _add_host(self, ham):
+        if self._sys:
+            raise RuntimeError('BatchedDOS: batch already run')
+        if ham.shape[0] % 4:
+            raise ValueError('the batch holds 4-orbital systems')
+        self._mats.append(ham.tocsr())
 
     def moments(self):
         """(systems, M) complex128 moments, mean over the vectors."""
-        return self._b.run()
+        if self.precision == 'single':
+            return self._b.run()
+        t0 = time.perf_counter()
+        launches0 = _lib.launch_count()
+        if not self._sys:
+            for s, H in enumerate(self._mats):
+                a, b = self.scales[s]
+                h = _lib.Handle(H, a, b, _lib.PREC_MIXED)
+                self._sys.append((h, _lib.Block(h, None,
+                                                num_vectors=self.num_vectors)))
+        out = np.empty((len(self._sys), self.num_moments), complex)
+        for s, (h, blk) in enumerate(self._sys):
+            # the device generator of 'single' with this system's key: the
+            # block keys its stream by mix64(seed ^ 0x5EEDB10C), the batch
+            # by mix64(seed ^ (system << 32)); storage order = orbital order
+            blk.randomize(self.seed ^ (s << 32) ^ 0x5EEDB10C)
+            out[s] = blk.dos_moments(0, self.num_moments).mean(axis=0)
+        self._last = ((time.perf_counter() - t0) * 1e3,
+                      _lib.launch_count() - launches0)
+        return out
 
     def densities(self, moments=None):
         """Densities at the 2M Chebyshev nodes of every system (Jackson
@@ -123,13 +183,38 @@ class BatchedDOS:
         return np.array(en), np.array(rho)
 
     def stats(self):
-        """(device ms of the last run, graph kernel nodes, vectors per
-        lane chosen by the autotuner)."""
+        """'single': (device ms of the last run, graph kernel nodes,
+        vectors per lane chosen by the autotuner); 'mixed': (wall ms of the
+        last run, kernel launches of that run, 2)."""
+        if self.precision == 'mixed':
+            return self._last[0], self._last[1], 2
         return self._b.stats()
 
     def step_format(self):
         """Step kernel chosen by the autotuner at the first run:
         ``(format, ell_width)`` with format 0 = dense 4 x 4 blocks, 1 =
         orbital-row ELL of width ell_width, 2 = sparse blocks staged in
-        shared memory."""
+        shared memory; 'mixed': ``(3, 0)``, the compensated ELL step."""
+        if self.precision == 'mixed':
+            return 3, 0
         return self._b.step_format()
+
+    def close(self):
+        """Free the device state of a 'mixed' batch."""
+        if self.precision == 'mixed':
+            for h, blk in self._sys:
+                blk.close()
+                h.close()
+            self._sys = []
+
+
+def wilson_dirac_matrix(L, m=1.5, W=0.0, seed=0):
+    """Host CSR of the L^3 Wilson-Dirac system that
+    ``add_wilson_dirac(L, m, W, seed)`` generates on the device (the
+    lattices builder's hoppings and onsite mass, the device generator's
+    disorder)."""
+    from . import lattices
+    H = lattices.wilson_dirac_cubic(L, m=m, W=0.0).hamiltonian_submatrix(
+        sparse=True).tocsr()
+    w = wilson_dirac_disorder(seed, L, W)
+    return (H + sp.diags(np.repeat(w, 4))).tocsr()

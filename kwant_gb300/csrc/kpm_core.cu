@@ -1305,7 +1305,7 @@ int kpm_last_kernel_ms(kpm_handle* h, double* ms) {
 
 int kpm_block_create(kpm_handle* h, const double* vecs, int64_t R,
                      int keep_a0, kpm_block** out) {
-  KPM_REQUIRE(h && vecs && out, "kpm_block_create: null argument");
+  KPM_REQUIRE(h && out, "kpm_block_create: null argument");
   KPM_REQUIRE(R > 0, "kpm_block_create: num_vectors must be positive");
   *out = nullptr;
   auto* b = new kpm_block();
@@ -1335,8 +1335,20 @@ int kpm_block_create(kpm_handle* h, const double* vecs, int64_t R,
       st = dev_alloc((void**)&b->lo_a0, lbytes, h->stream);
     if (st == KPM_OK && !b->keep_a0) b->lo_a0 = b->lo_buf[1];
   }
-  if (st == KPM_OK)
+  if (st == KPM_OK && vecs) {
     st = upload_vectors_lo(h, vecs, R, b->N, b->Rpad, b->a0, b->lo_a0);
+  } else if (st == KPM_OK) {
+    // no host vectors: zero, until kpm_block_randomize sets them
+    cudaError_t e = cudaMemsetAsync(b->a0, 0, vbytes, h->stream);
+    if (e == cudaSuccess && b->lo_a0)
+      e = cudaMemsetAsync(b->lo_a0, 0,
+                          (size_t)b->N * b->Rpad * sizeof(uint32_t),
+                          h->stream);
+    if (e != cudaSuccess) {
+      set_error("kpm_block_create: %s", cudaGetErrorString(e));
+      st = KPM_ECUDA;
+    }
+  }
   if (st == KPM_OK) {
     cudaError_t e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) {

@@ -54,6 +54,40 @@ def test_batch_matches_oracle_uneven_sizes():
     assert rho.shape == (3, 2 * M) and np.all(np.isfinite(rho))
 
 
+def test_batch_mixed_matches_oracle_and_single_vectors():
+    """precision='mixed' runs every system through the compensated step
+    with the starting vectors of the 'single' batch (the device stream of
+    random_phase_vectors): the moments match the oracle on those vectors,
+    a rerun repeats them bit for bit, and wilson_dirac_matrix is the host
+    twin of the device-generated system."""
+    from kwant_gb300 import batch
+    R, M, seed = 8, 40, 11
+    mats = [_host_wilson_dirac(3, 1.5, 1.0, 7), _host_wilson_dirac(5, 1.5, 3.0, 8)]
+    bd = batch.BatchedDOS(R, M, seed=seed, precision='mixed')
+    for H in mats:
+        bd.add_matrix(H, _gershgorin(H))
+    bd.add_wilson_dirac(4, m=1.5, W=0.5, seed=9)
+    mats.append(batch.wilson_dirac_matrix(4, 1.5, 0.5, 9))
+    assert np.array_equal(mats[-1].toarray(),
+                          _host_wilson_dirac(4, 1.5, 0.5, 9).toarray())
+    mom = bd.moments()
+    assert mom.shape == (3, M)
+    for s, H in enumerate(mats):
+        a, b = bd.scales[s]
+        vecs = batch.random_phase_vectors(seed, s, R, H.shape[0])
+        ref = _oracle_mean(H, a, b, vecs, M)
+        err = np.max(np.abs(mom[s] - ref)) / np.max(np.abs(ref))
+        # complex64 values of 2H/a: a consistent ~6e-8 perturbation of H
+        assert err < 2e-6, (s, err)
+    assert np.array_equal(bd.moments(), mom)     # rerun: same vectors
+    ms, launches, _ = bd.stats()
+    assert ms > 0 and launches >= 3 * M // 2
+    assert bd.step_format() == (3, 0)
+    bd.close()
+    with pytest.raises(ValueError):
+        batch.BatchedDOS(4, 24, precision='fp64')
+
+
 def test_device_generated_wilson_dirac_equals_host_matrix():
     from kwant_gb300 import batch
     R, M, seed = 4, 24, 5
