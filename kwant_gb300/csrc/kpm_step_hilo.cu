@@ -124,14 +124,19 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-// Block size by ELL width: each thread stages a row's own x (unless it is
-// the first gathered row, D0), alpha_{n-1} and K gathered rows (24 bytes
-// each, hi and lo), double-buffered; the block must leave room for two or
-// three blocks per SM (K = 4: two blocks of 256, 78 KB each).
+// Block shape: each thread stages, per chunk of four ELL entries of a row,
+// the four gathered rows (24 bytes each, hi and lo), plus alpha_{n-1} with
+// the last chunk and the row's own x with the first (unless it is the
+// first gathered row, D0), double-buffered.  The staging does not grow with
+// the ELL width, so every width runs two blocks of 256 threads per SM
+// (16 warps).  When every slice of a row was staged at once, an ELL width
+// of 16 left room for 6 warps per SM and the step took 2.8x the time per
+// orbital and vector of the 4-wide graphene rows.
 template <int K, bool D0> struct HiloCfg {
-  static constexpr int THREADS = K <= 4 ? 256 : (K <= 12 ? 128 : 64);
-  static constexpr int MIN_BLOCKS = K <= 4 ? 2 : 2;
-  static constexpr int ITEMS = K + (D0 ? 1 : 2);
+  static constexpr int THREADS = 256;
+  static constexpr int MIN_BLOCKS = 2;
+  static constexpr int CHUNKS = K / 4;          // ELL entries in groups of 4
+  static constexpr int ITEMS = 4 + (D0 ? 1 : 2);
   // staged item indices: the row's own x, alpha_{n-1}, first gathered row
   static constexpr int OWN = D0 ? 1 : 0;
   static constexpr int PREV = D0 ? 0 : 1;
@@ -149,12 +154,13 @@ template <int K, bool D0> struct HiloCfg {
 
 // The step over 16-vector sub-groups in 8-lane slots whose lanes hold two
 // complex64 vectors each (a float4 of hi parts, a uint2 of lo parts).  A
-// warp's four slots walk adjacent rows.  Per row iteration each thread
-// copies its next row's slices (own x, alpha_{n-1} and the K gathered rows,
-// hi and lo) into shared memory with cp.async while it computes the current
-// row from the previous copies, and the warp's ELL entries are staged two
-// iterations ahead (their column indices address those copies), so a row's
-// memory latency overlaps the previous row's arithmetic.  MODE STEP_FIRST:
+// warp's four slots walk adjacent rows.  A row is computed in chunks of
+// four ELL entries; while a thread computes one chunk it copies the slices
+// of its next chunk (the next row's first chunk after the last) into shared
+// memory with cp.async, and the warp's ELL entries are staged two rows
+// ahead (their column indices address those copies), so the memory latency
+// of a chunk overlaps the previous chunk's arithmetic.  The entries of a row
+// are summed in ELL order whatever the chunking.  MODE STEP_FIRST:
 // a_1 = H~ a_0 with the dots mu_0 = <a_0|a_0> and <a_1|a_0> of hi + lo;
 // STEP_RECUR: a_{n+1} = 2 H~ a_n - a_{n-1} with the compensated dots
 // <a_n|a_n>, <a_n+1|a_n>.
@@ -177,6 +183,7 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
   using Cfg = HiloCfg<K, D0>;
   using VT = typename Cfg::VT;
   constexpr int OWN = Cfg::OWN, PREV = Cfg::PREV, GATH = Cfg::GATH;
+  constexpr int CHUNKS = Cfg::CHUNKS;
   constexpr int T = Cfg::THREADS, ITEMS = Cfg::ITEMS, NSLOT = Cfg::NSLOT;
   constexpr int SW = 8, G = 16, SPW = 4, FLUSH = 128;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -227,24 +234,29 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
       }
     }
   };
-  // this thread's slices of row r (ELL entries in ring buffer eb) into
-  // vector buffer vb
-  auto stage_vec = [&](int r, int vb, int eb, int col) {
+  // this thread's slices of chunk c of row r (ELL entries in ring buffer
+  // eb) into vector buffer vb: the four gathered rows, the own x with the
+  // first chunk (unless D0) and alpha_{n-1} with the last
+  auto stage_vec = [&](int r, int vb, int eb, int col, int c) {
     if (r >= rows) return;
     float4* dh = vhi + vb * ITEMS * T + tid;
     uint2* dl = vlo + vb * ITEMS * T + tid;
     const int64_t o = off(r, col);
     if constexpr (!D0) {
-      cp_async16(dh + OWN * T, x + o);
-      cp_async8(dl + OWN * T, xl + o);
+      if (c == 0) {
+        cp_async16(dh + OWN * T, x + o);
+        cp_async8(dl + OWN * T, xl + o);
+      }
     }
     if constexpr (MODE == STEP_RECUR) {
-      cp_async16(dh + PREV * T, prev + o);
-      cp_async8(dl + PREV * T, pl + o);
+      if (c == CHUNKS - 1) {
+        cp_async16(dh + PREV * T, prev + o);
+        cp_async8(dl + PREV * T, pl + o);
+      }
     }
-    const int32_t* ci = widx + eb * 4 * K + half * K;
+    const int32_t* ci = widx + eb * 4 * K + half * K + 4 * c;
 #pragma unroll
-    for (int t = 0; t < K; ++t) {
+    for (int t = 0; t < 4; ++t) {
       const int64_t oc = off(col_index(p, ci[t]), col);
       cp_async16(dh + (GATH + t) * T, x + oc);
       cp_async8(dl + (GATH + t) * T, xl + oc);
@@ -305,147 +317,164 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
     cp_async_commit();
     cp_async_wait<1>();
     __syncwarp();
-    stage_vec(wb0 + half, 0, 0, col);
+    stage_vec(wb0 + half, 0, 0, col, 0);
     cp_async_commit();
     int e0 = 0, e1 = 1, e2 = 2, vb = 0;   // ring positions of rows it, +1, +2
     for (int wb = wb0; wb < rows; wb += stride) {
-      stage_ell(wb + 2 * stride, e2);
-      cp_async_commit();
-      // pending groups: ELL(it + 1), vectors(it), ELL(it + 2)
-      cp_async_wait<1>();
-      __syncwarp();
-      stage_vec(wb + stride + half, vb ^ 1, e1, col);
-      cp_async_commit();
       const int r = wb + half;
-      if (r < rows) {
-        const float4* sh = vhi + vb * ITEMS * T + tid;
-        const uint2* sl = vlo + vb * ITEMS * T + tid;
-        const float4 xo = sh[OWN * T];
-        const uint2 xol = sl[OWN * T];
-        const float2 xk[2] = {make_float2(xo.x, xo.y),
-                              make_float2(xo.z, xo.w)};
-        const uint32_t xlw[2] = {xol.x, xol.y};
-        float2 Ps[2], Pc[2], Qs[2], Qc[2], LP[2], LQ[2];
+      // the row's state across its chunks
+      float2 xk[2], Ps[2], Pc[2], Qs[2], Qc[2], LP[2], LQ[2];
+      uint32_t xlw[2];
 #pragma unroll
-        for (int k = 0; k < 2; ++k) {
-          Ps[k] = Qs[k] = f2(C);
-          Pc[k] = Qc[k] = LQ[k] = make_float2(0.f, 0.f);
-          if constexpr (D0) {
-            LP[k] = make_float2(0.f, 0.f);
-          } else {
-            acc_fma(Ps[k], Pc[k], shift, xk[k]);
-            LP[k] = __fmul2_rn(shift, lo_pair(xlw[k]));
-          }
+      for (int c = 0; c < CHUNKS; ++c) {
+        if (c == 0) {
+          stage_ell(wb + 2 * stride, e2);
+          cp_async_commit();
+          // pending groups: ELL(it + 1), vectors(it, 0), ELL(it + 2)
+          cp_async_wait<1>();
+        } else {
+          cp_async_wait<0>();          // vectors(it, c), ELL(it + 2)
         }
-        const VT* hv = wval + e0 * 4 * K + half * K;
+        __syncwarp();
+        if (c + 1 < CHUNKS)
+          stage_vec(r, vb ^ 1, e0, col, c + 1);
+        else
+          stage_vec(wb + stride + half, vb ^ 1, e1, col, 0);
+        cp_async_commit();
+        if (r < rows) {
+          const float4* sh = vhi + vb * ITEMS * T + tid;
+          const uint2* sl = vlo + vb * ITEMS * T + tid;
+          if (c == 0) {
+            const float4 xo = sh[OWN * T];
+            const uint2 xol = sl[OWN * T];
+            xk[0] = make_float2(xo.x, xo.y);
+            xk[1] = make_float2(xo.z, xo.w);
+            xlw[0] = xol.x;
+            xlw[1] = xol.y;
 #pragma unroll
-        for (int t = 0; t < K; ++t) {
-          float2 hr, hi;
-          if constexpr (D0) {
-            const float4 h = hv[t];
-            hr = make_float2(h.x, h.y);
-            hi = make_float2(h.z, h.w);
-          } else {
-            const float2 h = hv[t];
-            hr = f2(h.x);
-            hi = f2(h.y);
+            for (int k = 0; k < 2; ++k) {
+              Ps[k] = Qs[k] = f2(C);
+              Pc[k] = Qc[k] = LQ[k] = make_float2(0.f, 0.f);
+              if constexpr (D0) {
+                LP[k] = make_float2(0.f, 0.f);
+              } else {
+                acc_fma(Ps[k], Pc[k], shift, xk[k]);
+                LP[k] = __fmul2_rn(shift, lo_pair(xlw[k]));
+              }
+            }
           }
-          const float4 gx = sh[(GATH + t) * T];
-          const uint2 gl = sl[(GATH + t) * T];
-          const float2 gk[2] = {make_float2(gx.x, gx.y),
-                                make_float2(gx.z, gx.w)};
-          const uint32_t glw[2] = {gl.x, gl.y};
+          const VT* hv = wval + e0 * 4 * K + half * K + 4 * c;
 #pragma unroll
-          for (int k = 0; k < 2; ++k) {
-            acc_fma(Ps[k], Pc[k], hr, gk[k]);
-            const float2 l = lo_pair(glw[k]);
-            LP[k] = __ffma2_rn(hr, l, LP[k]);
-            if (!D0 || t > 0) {    // a D0 row's first entry is real
-              acc_fma(Qs[k], Qc[k], hi, gk[k]);
-              LQ[k] = __ffma2_rn(hi, l, LQ[k]);
+          for (int t = 0; t < 4; ++t) {
+            float2 hr, hi;
+            if constexpr (D0) {
+              const float4 h = hv[t];
+              hr = make_float2(h.x, h.y);
+              hi = make_float2(h.z, h.w);
+            } else {
+              const float2 h = hv[t];
+              hr = f2(h.x);
+              hi = f2(h.y);
+            }
+            const float4 gx = sh[(GATH + t) * T];
+            const uint2 gl = sl[(GATH + t) * T];
+            const float2 gk[2] = {make_float2(gx.x, gx.y),
+                                  make_float2(gx.z, gx.w)};
+            const uint32_t glw[2] = {gl.x, gl.y};
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+              acc_fma(Ps[k], Pc[k], hr, gk[k]);
+              const float2 l = lo_pair(glw[k]);
+              LP[k] = __ffma2_rn(hr, l, LP[k]);
+              if (!D0 || c > 0 || t > 0) {   // a D0 row's first entry is real
+                acc_fma(Qs[k], Qc[k], hi, gk[k]);
+                LQ[k] = __ffma2_rn(hi, l, LQ[k]);
+              }
+            }
+          }
+          if (c == CHUNKS - 1) {
+            if constexpr (MODE == STEP_RECUR) {
+              const float4 pv = sh[PREV * T];
+              const uint2 plv = sl[PREV * T];
+              const float2 pk[2] = {make_float2(pv.x, pv.y),
+                                    make_float2(pv.z, pv.w)};
+              const uint32_t plw[2] = {plv.x, plv.y};
+#pragma unroll
+              for (int k = 0; k < 2; ++k) {
+                acc_sub(Ps[k], Pc[k], pk[k]);
+                LP[k] = sub2(LP[k], lo_pair(plw[k]));
+              }
+            }
+            float2 ohi[2];
+            uint32_t olw[2];
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+              // v = (re, im) of the anchored sums (exact), cc = their
+              // compensation plus the lo bracket
+              const float2 v = make_float2(
+                  __fsub_rn(Ps[k].x, Qs[k].y),
+                  __fadd_rn(__fsub_rn(Ps[k].y, C), __fsub_rn(Qs[k].x, C)));
+              const float2 cc = make_float2(
+                  __fadd_rn(__fsub_rn(Pc[k].x, Qc[k].y),
+                            __fsub_rn(LP[k].x, LQ[k].y)),
+                  __fadd_rn(__fadd_rn(Pc[k].y, Qc[k].x),
+                            __fadd_rn(LP[k].y, LQ[k].x)));
+              float2 h = __fadd2_rn(v, cc);                 // hi = RN(v)
+              float2 l = __fadd2_rz(sub2(v, h), cc);        // lo = RZ(v - hi)
+              if constexpr (MODE == STEP_FIRST) {           // a_1 = (2 H~ a_0) / 2
+                h = __fmul2_rn(h, f2(0.5f));
+                l = __fmul2_rn(l, f2(0.5f));
+              }
+              ohi[k] = h;
+              olw[k] = lo_pack_rz(l);
+            }
+            const int64_t o = off(r, col);
+            out[o] = make_float4(ohi[0].x, ohi[0].y, ohi[1].x, ohi[1].y);
+            ol[o] = make_uint2(olw[0], olw[1]);
+            if constexpr (MODE == STEP_FIRST) {
+              // mu_0 and <a_1|a_0> of a = hi + lo: Dot2 on the hi products, the
+              // products with a lo part (2^-8 of them, relative) as FP32 sums
+              // into the compensation terms
+#pragma unroll
+              for (int k = 0; k < 2; ++k) {
+                const float2 al = lo_pair(xlw[k]), bl = lo_pair(olw[k]);
+                dot2(dns[k], dnc[k], xk[k], xk[k]);
+                dnc[k] = __ffma2_rn(__fmul2_rn(f2(2.f), xk[k]), al, dnc[k]);
+                dnc[k] = __ffma2_rn(al, al, dnc[k]);
+                // Re <a_1|a_0> = br ar + bi ai
+                dot2(drs[k], drc[k], ohi[k], xk[k]);
+                drc[k] = __ffma2_rn(ohi[k], al, drc[k]);
+                drc[k] = __ffma2_rn(bl, __fadd2_rn(xk[k], al), drc[k]);
+                // Im <a_1|a_0> = br ai - bi ar
+                const float2 u = make_float2(ohi[k].x, -ohi[k].y);
+                const float2 ul = make_float2(bl.x, -bl.y);
+                const float2 v = make_float2(xk[k].y, xk[k].x);
+                const float2 vl = make_float2(al.y, al.x);
+                dot2(dis[k], dic[k], u, v);
+                dic[k] = __ffma2_rn(u, vl, dic[k]);
+                dic[k] = __ffma2_rn(ul, __fadd2_rn(v, vl), dic[k]);
+              }
+            } else {
+#pragma unroll
+              for (int k = 0; k < 2; ++k) {
+                dot2(dns[k], dnc[k], xk[k], xk[k]);
+                drs[k] = __ffma2_rn(ohi[k], xk[k], drs[k]);
+                fim[k] = fmaf(ohi[k].x, xk[k].y, fmaf(-ohi[k].y, xk[k].x, fim[k]));
+              }
+            }
+            if (++pending == FLUSH) {
+              flush_dots();
+              pending = 0;
             }
           }
         }
-        if constexpr (MODE == STEP_RECUR) {
-          const float4 pv = sh[PREV * T];
-          const uint2 plv = sl[PREV * T];
-          const float2 pk[2] = {make_float2(pv.x, pv.y),
-                                make_float2(pv.z, pv.w)};
-          const uint32_t plw[2] = {plv.x, plv.y};
-#pragma unroll
-          for (int k = 0; k < 2; ++k) {
-            acc_sub(Ps[k], Pc[k], pk[k]);
-            LP[k] = sub2(LP[k], lo_pair(plw[k]));
-          }
-        }
-        float2 ohi[2];
-        uint32_t olw[2];
-#pragma unroll
-        for (int k = 0; k < 2; ++k) {
-          // v = (re, im) of the anchored sums (exact), cc = their
-          // compensation plus the lo bracket
-          const float2 v = make_float2(
-              __fsub_rn(Ps[k].x, Qs[k].y),
-              __fadd_rn(__fsub_rn(Ps[k].y, C), __fsub_rn(Qs[k].x, C)));
-          const float2 cc = make_float2(
-              __fadd_rn(__fsub_rn(Pc[k].x, Qc[k].y),
-                        __fsub_rn(LP[k].x, LQ[k].y)),
-              __fadd_rn(__fadd_rn(Pc[k].y, Qc[k].x),
-                        __fadd_rn(LP[k].y, LQ[k].x)));
-          float2 h = __fadd2_rn(v, cc);                 // hi = RN(v)
-          float2 l = __fadd2_rz(sub2(v, h), cc);        // lo = RZ(v - hi)
-          if constexpr (MODE == STEP_FIRST) {           // a_1 = (2 H~ a_0) / 2
-            h = __fmul2_rn(h, f2(0.5f));
-            l = __fmul2_rn(l, f2(0.5f));
-          }
-          ohi[k] = h;
-          olw[k] = lo_pack_rz(l);
-        }
-        const int64_t o = off(r, col);
-        out[o] = make_float4(ohi[0].x, ohi[0].y, ohi[1].x, ohi[1].y);
-        ol[o] = make_uint2(olw[0], olw[1]);
-        if constexpr (MODE == STEP_FIRST) {
-          // mu_0 and <a_1|a_0> of a = hi + lo: Dot2 on the hi products, the
-          // products with a lo part (2^-8 of them, relative) as FP32 sums
-          // into the compensation terms
-#pragma unroll
-          for (int k = 0; k < 2; ++k) {
-            const float2 al = lo_pair(xlw[k]), bl = lo_pair(olw[k]);
-            dot2(dns[k], dnc[k], xk[k], xk[k]);
-            dnc[k] = __ffma2_rn(__fmul2_rn(f2(2.f), xk[k]), al, dnc[k]);
-            dnc[k] = __ffma2_rn(al, al, dnc[k]);
-            // Re <a_1|a_0> = br ar + bi ai
-            dot2(drs[k], drc[k], ohi[k], xk[k]);
-            drc[k] = __ffma2_rn(ohi[k], al, drc[k]);
-            drc[k] = __ffma2_rn(bl, __fadd2_rn(xk[k], al), drc[k]);
-            // Im <a_1|a_0> = br ai - bi ar
-            const float2 u = make_float2(ohi[k].x, -ohi[k].y);
-            const float2 ul = make_float2(bl.x, -bl.y);
-            const float2 v = make_float2(xk[k].y, xk[k].x);
-            const float2 vl = make_float2(al.y, al.x);
-            dot2(dis[k], dic[k], u, v);
-            dic[k] = __ffma2_rn(u, vl, dic[k]);
-            dic[k] = __ffma2_rn(ul, __fadd2_rn(v, vl), dic[k]);
-          }
-        } else {
-#pragma unroll
-          for (int k = 0; k < 2; ++k) {
-            dot2(dns[k], dnc[k], xk[k], xk[k]);
-            drs[k] = __ffma2_rn(ohi[k], xk[k], drs[k]);
-            fim[k] = fmaf(ohi[k].x, xk[k].y, fmaf(-ohi[k].y, xk[k].x, fim[k]));
-          }
-        }
-        if (++pending == FLUSH) {
-          flush_dots();
-          pending = 0;
-        }
+        __syncwarp();
+        vb ^= 1;
       }
-      __syncwarp();
       const int e_old = e0;
       e0 = e1;
       e1 = e2;
       e2 = e_old;
-      vb ^= 1;
     }
     cp_async_wait<0>();
     flush_dots();
