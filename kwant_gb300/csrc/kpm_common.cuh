@@ -72,7 +72,10 @@ constexpr int GROUP_FP32 = 2 * LANES;
 // kernel: its persistent grid then gets exactly one long run of rows per
 // vector group and block (the per-item pipeline start and block reduction
 // are amortised over many rows, and no block idles in a last round).
-constexpr int XITEMS_PER_SM = 4;
+#ifndef KPM_XITEMS_PER_SM
+#define KPM_XITEMS_PER_SM 4
+#endif
+constexpr int XITEMS_PER_SM = KPM_XITEMS_PER_SM;
 
 inline int group_size(int precision) {
   return precision == KPM_PREC_MIXED ? GROUP_FP32 : GROUP_FP64;
@@ -115,9 +118,10 @@ __device__ __forceinline__ void cp_async_wait_prev() {
   asm volatile("cp.async.wait_group 1;" ::: "memory");
 }
 
-inline int xitems_for_rows(int64_t rows, int num_sms) {
+inline int xitems_for_rows(int64_t rows, int num_sms,
+                           int per_sm = XITEMS_PER_SM) {
   int64_t x = ceil_div(rows, (int64_t)SLOTS);
-  const int64_t cap = (int64_t)XITEMS_PER_SM * (num_sms > 0 ? num_sms : 1);
+  const int64_t cap = (int64_t)per_sm * (num_sms > 0 ? num_sms : 1);
   if (x > cap) x = cap;
   if (x < 1) x = 1;
   return (int)x;

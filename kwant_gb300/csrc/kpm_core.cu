@@ -814,6 +814,12 @@ __global__ void moments_to_host_order_kernel(const double2* __restrict__ in,
 // Per-launch profiling (kpm_profile): an event pair around the next
 // step launch on the handle's stream; *e1 = the closing event, or nullptr
 // when profiling is off.
+int dos_xitems(const kpm_handle* h, int64_t rows) {
+  return xitems_for_rows(rows, h->num_sms,
+                         h->compensated && h->H.ell_k > 0 ? 2
+                                                          : XITEMS_PER_SM);
+}
+
 int prof_begin(kpm_handle* h, cudaEvent_t* e1) {
   *e1 = nullptr;
   if (!h->profiling) return KPM_OK;
@@ -908,7 +914,7 @@ StepArgs step_args(kpm_block* b, const void* x, const void* prev, void* out) {
   a.vpl = h->precision == KPM_PREC_MIXED ? b->G / GROUP_FP64 : 1;
   a.rp = b->Rpad / a.vpl;
   a.groups = b->groups;
-  a.xitems = xitems_for_rows(b->N, h->num_sms);
+  a.xitems = dos_xitems(h, b->N);
   a.partials = h->partials;
   a.check = h->check;
   return a;
@@ -1022,7 +1028,7 @@ int finalize(kpm_block* b, int mode, double2* mom, int64_t slot_even,
              int64_t slot_odd) {
   kpm_handle* h = b->h;
   dos_finalize_kernel<<<(unsigned)b->Rpad, 128, 0, h->stream>>>(
-      h->partials, b->G, xitems_for_rows(b->N, h->num_sms), b->Rpad,
+      h->partials, b->G, dos_xitems(h, b->N), b->Rpad,
       mode, (double2*)b->mu01, mom, b->Rpad, slot_even, slot_odd);
   count_launch(1);
   KPM_CHECK_LAUNCH();
@@ -1547,7 +1553,7 @@ int kpm_block_dos_moments(kpm_block* b, int64_t m_start, int64_t m_end,
   b->mode = 0;
   const int64_t count = m_end - m_start;
   const int G = group_size(h->precision);
-  KPM_TRY(ensure_partials(h, b->groups, xitems_for_rows(b->N, h->num_sms)));
+  KPM_TRY(ensure_partials(h, b->groups, dos_xitems(h, b->N)));
   double2* mom = nullptr;
   KPM_TRY(dev_alloc((void**)&mom, (size_t)count * b->Rpad * sizeof(double2),
                     h->stream));

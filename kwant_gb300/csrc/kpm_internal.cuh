@@ -65,6 +65,14 @@ struct HiloArgs {
 };
 
 void count_launch(int n);
+// Row partitions of the steps that write moment dot partials (the DOS dots
+// and norms, and their finalize): fixed for a handle and its row count, so
+// the reduction order never depends on R or on the launch shape.  The
+// compensated step runs two 256-thread blocks per SM, and 2 partitions per
+// SM give each block half as many pipeline starts and block reductions as 4
+// (graphene, 2e6 orbitals, R = 64: 1.000 -> 0.985 ms per step); the other
+// steps keep 4.
+int dos_xitems(const kpm_handle* h, int64_t rows);
 // event pair around the next launch when profiling (*e1: closing event)
 int prof_begin(kpm_handle* h, cudaEvent_t* e1);
 int dev_alloc(void** p, size_t bytes, cudaStream_t s);

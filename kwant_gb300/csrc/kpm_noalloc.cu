@@ -131,7 +131,7 @@ int kpm_dos_moments_noalloc(const kpm_device_csr* ham, double a, double b,
   const int64_t N = ham->rows;
   const int64_t Rpad = round_up(R, G);
   const int groups = (int)(Rpad / G);
-  const int xitems = xitems_for_rows(N, sms);
+  const int xitems = xitems_for_rows(N, sms);   // plain steps: 4 per SM
   const size_t partials = (size_t)groups * xitems * G * 3;  // doubles
   const size_t need = partials + (size_t)Rpad * 4;          // + mu0, mu1
   const size_t cap = KPM_NOALLOC_SCRATCH_BYTES / sizeof(double);

@@ -434,6 +434,8 @@ static int dispatch_k(kpm_handle* h, int mode, bool dots, const StepArgs& a,
 int launch_step_ell(kpm_handle* h, int mode, bool dots, const StepArgs& a,
                     const StoreArgs* sa) {
   StepArgs w = a;
+  // steps without dot partials: every resident block gets a partition
+  if (!dots) w.xitems = xitems_for_rows(a.rows, h->num_sms);
   if (sa && sa->smode && a.vpl == 1 && KPM_STORE_SW != 8) {
     constexpr int SW = KPM_STORE_SW;
     w.vpl = 16 / SW;
