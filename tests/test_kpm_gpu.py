@@ -200,6 +200,40 @@ def test_mixed_dos_all_nodes_long_expansion(kpm):
     assert err.max() < 1e-5, (err.max(), sd.energies[np.argmax(err)])
 
 
+@pytest.mark.parametrize('model', ['rashba', 'wilson_dirac'])
+def test_mixed_dos_wide_rows(kpm, model):
+    """The compensated step on wider ELL rows, which it computes in
+    chunks of four entries: the two-orbital Rashba square (width 12, three
+    chunks) and the four-orbital Wilson-Dirac cube (13 entries, width 16,
+    four chunks) against the oracle at every node of an M = 400 expansion,
+    and add_vectors across a 16-vector and a 32-vector group bit-identical
+    to one run."""
+    from kwant_gb300 import lattices
+    if model == 'rashba':
+        syst = lattices.rashba_square(40, seed=2)
+    else:
+        syst = lattices.wilson_dirac_cubic(8, m=1.5, W=1.0, seed=2)
+    ham = syst.hamiltonian_submatrix(sparse=True).tocsr()
+    n, R, M = ham.shape[0], 6, 400
+    v0, vecs = ref_vectors(3, n, R)
+    lmin, lmax = ko.spectral_bounds(ham, 0.05, v0)
+    ref = ko.spectral_density(ham, vecs, lmin, lmax, M)
+    sd = kpm.SpectralDensity(ham, bounds=(lmin, lmax),
+                             vector_factory=list(vecs), num_vectors=R,
+                             num_moments=M, precision='mixed')
+    err = np.abs(sd.densities.real - ref['densities'].real) / n
+    assert err.max() < 1e-5, err.max()
+    small = kpm.SpectralDensity(ham, bounds=(lmin, lmax), rng=5,
+                                num_vectors=10, num_moments=60,
+                                precision='mixed')
+    small.add_vectors(30)
+    fresh = kpm.SpectralDensity(ham, bounds=(lmin, lmax), rng=5,
+                                num_vectors=40, num_moments=60,
+                                precision='mixed')
+    assert np.array_equal(np.array(small._moments_list),
+                          np.array(fresh._moments_list))
+
+
 # --------------------------------------------------------------- operators
 def test_ldos_density_where(kpm):
     from kwant_gb300.system import LatticeSystem
