@@ -18,7 +18,7 @@ path on the device:
   the device (``csrc/kpm_correlator.cu``, ``csrc/kpm_gemm*.cu``).
 
 Extra keyword-only arguments: ``precision`` ('fp64': complex128 recursion in
-the reference's operation order; 'mixed': complex64 recursion, which for
+the reference's CSR order, with fused multiply-adds; 'mixed': complex64 recursion, which for
 the DOS keeps a bfloat16 correction next to every complex64 element and
 steps with error-free FP32 transformations, so the per-orbital DOS stays
 within ~1e-6 of FP64 at every Chebyshev node; 'single': the plain complex64
