@@ -352,13 +352,13 @@ def run_ours(args):
     # DRAM bytes per step launch: ncu dram__bytes_read + dram__bytes_write
     # of one step launch on the 500 x 500-cell, R = 64 case (the workload
     # here is too large for a multi-pass capture), scaled to this launch by
-    # its algorithmic bytes: cheb_step_hilo_kernel 884.2 + 354.7 MB against
+    # its algorithmic bytes: cheb_step_hilo_kernel 913.2 + 353.1 MB against
     # 1178.0 MB ('mixed'), cheb_step_ell_kernel 774.5 MB against 794.0 MB
     # ('single')
     traffic = None
     if args.reorder and R == 64:
         if args.precision == 'mixed':
-            traffic = B * ((884.2 + 354.7) / 1178.0)
+            traffic = B * ((913.2 + 353.1) / 1178.0)
         elif args.precision == 'single':
             traffic = B * (774.5 / 794.0)
 
