@@ -84,6 +84,24 @@ def test_argument_checks_and_missing_device_fail_cleanly():
         assert lib.kpm_batch_create(4, 24, 0, ctypes.byref(out)) == -2
 
 
+def test_batch_arguments_checked_on_the_host():
+    """BatchedDOS rejects an unknown precision and an odd moment count
+    before any device work, in both precisions."""
+    import pytest
+    from kwant_gb300 import batch
+    with pytest.raises(ValueError):
+        batch.BatchedDOS(4, 24, precision='fp64')
+    for prec in ('single', 'mixed'):
+        with pytest.raises(ValueError):
+            batch.BatchedDOS(4, 25, precision=prec)
+    bd = batch.BatchedDOS(4, 24, precision='mixed')   # nothing on the device
+    assert bd.stats()[0] == 0.0 and bd.step_format() == (3, 0)
+    H = batch.wilson_dirac_matrix(3, 1.5, 1.0, 7)
+    assert H.shape == (108, 108) and abs(H - H.conj().T).max() == 0
+    with pytest.raises(ValueError):
+        bd.add_matrix(H[:107, :107], (-10.0, 10.0))    # not 4-orbital
+
+
 def _query_checks(lib_file):
     """kpm_build_checks of a library, in a fresh process that loads it
     through the package (KWANT_GB300_LIB)."""
