@@ -546,8 +546,8 @@ template <> struct C64Pay<1> {
 // add, so this is half the instructions of scipy's separately rounded
 // (hr xr - hi xi) + i (hr xi + hi xr): the FP64 step is FP64-pipe bound, and
 // the fused form took it from 11.7 to 7.1 ms per step on the 2e6-orbital
-// graphene workload (R = 64).  Results stay within 1e-15 relative of the reference's
-// arithmetic per step.
+// graphene workload (R = 64).  Results stay within 1e-15 relative of the
+// reference's arithmetic per step.
 __device__ __forceinline__ void cmul_acc_fma(double& ar, double& ai,
                                              double2 h, double2 x) {
   ar = fma(h.x, x.x, fma(-h.y, x.y, ar));

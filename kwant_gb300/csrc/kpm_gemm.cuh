@@ -84,7 +84,8 @@ __device__ __forceinline__ void store_put2_bf16x3(const StoreRow& r, int64_t k,
   p[0] = hr;
   p[ps2] = __floats2bfloat162_rn(re0 - __low2float(hr), re1 - __high2float(hr));
   p[2 * ps2] = hi;
-  p[3 * ps2] = __floats2bfloat162_rn(im0 - __low2float(hi), im1 - __high2float(hi));
+  p[3 * ps2] =
+      __floats2bfloat162_rn(im0 - __low2float(hi), im1 - __high2float(hi));
 }
 
 int store_alloc(Store* s, int kind, int64_t M, int64_t K, cudaStream_t st);

@@ -10,10 +10,11 @@
 // A slot is 8 lanes with two (16-vector groups) or four (32-vector groups)
 // complex64 vectors per lane: 128 or 256 bytes per row, and four rows in
 // flight per warp (the correlator's store steps on 16-vector blocks: 4
-// lanes of four vectors, eight rows per warp).  The column indices and values of a warp's next four
-// rows are copied into shared memory with cp.async (16-byte chunks, no
-// row-pointer load) while the current ones compute, so a row's gathers go
-// out together with its own vector entry and its alpha_{n-1} entry: one
+// lanes of four vectors, eight rows per warp).  The column indices and
+// values of a warp's next rows are copied into shared memory with cp.async
+// (16-byte chunks, no row-pointer load) while the current ones compute, so
+// a row's gathers go out together with its own vector entry and its
+// alpha_{n-1} entry: one
 // dependent memory round trip per row (a CSR row costs four).  The FP64
 // dot-product accumulators live in shared memory to keep registers (and so
 // occupancy) low.
@@ -260,7 +261,8 @@ cheb_step_ell_kernel(StepArgs p, const int32_t* __restrict__ eidx,
             const float re1 = SM == 2 ? sr[k + 1] : Pay::re(xv[u], k + 1);
             const float im1 = SM == 2 ? si[k + 1] : Pay::im(xv[u], k + 1);
             if ((sa.R & 1) == 0) {
-              if (vec < sa.R) store_put2_bf16x3(sa.store, kk, re0, im0, re1, im1);
+              if (vec < sa.R)
+                store_put2_bf16x3(sa.store, kk, re0, im0, re1, im1);
             } else {
               if (vec < sa.R) store_put<STORE_BF16X3>(sa.store, kk, re0, im0);
               if (vec + 1 < sa.R)

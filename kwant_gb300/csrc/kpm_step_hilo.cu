@@ -30,22 +30,21 @@
 //   * hi = RN(v), lo = RZ_bf16(RZ(v - hi)): round toward zero keeps |lo| at
 //     most half an ulp of hi, so the split is unique and a vector downloaded
 //     as complex128 (hi + lo, exact) uploads to the same hi and lo.
-// The fused dot products use the hi parts: mu_0 and mu_1 from hi + lo
-// (once, compensated; FP64 products per row took 4.6x a recursion step on
-// GB300's narrow FP64 pipe), then <a_n|a_n> with Ogita-Rump-Oishi Dot2 (TwoProd + TwoSum) and
-// Re and Im <a_n+1|a_n> as plain FP32 sums, all flushed to FP64 every 128
-// rows.  Leaving out lo in these dots is a zero-mean error of each moment
-// alone, not a shift of all of them.  The sums of |a_i|^2 need the
-// compensation: their terms are all positive, and plain FP32 partials
-// (flushed every 128 or 32 rows) took the per-orbital DOS error at the
-// outermost node of the 2e6-orbital workload to 1.0e-4 or 1.0e-5 (2.6e-7
-// with Dot2).  The terms of <a_n+1|a_n> change sign, and a plain sum there
-// left the error at 2.6e-7 and saved 0.7 % of the step.  (An anchored sum with a
-// per-vector anchor >= 4 mu_0, which bounds every partial sum, was
-// measured too: the anchor is then far above a row's terms, their
-// fractional parts land in the FP32 residual sum, and its bias took the
+// The fused dot products use the hi parts.  mu_0 and mu_1 come from hi + lo
+// once, as compensated sums (FP64 products per row took 4.6x a recursion
+// step on GB300's narrow FP64 pipe).  Then <a_n|a_n> is summed with
+// Ogita-Rump-Oishi Dot2 (TwoProd + TwoSum), Re and Im <a_n+1|a_n> as plain
+// FP32 sums, all flushed to FP64 every 128 rows.  Leaving out lo in these
+// dots is a zero-mean error of each moment alone, not a shift of all of
+// them.  The sums of |a_i|^2 need the compensation: their terms are all
+// positive, and plain FP32 partials (flushed every 128 or 32 rows) took the
 // per-orbital DOS error at the outermost node of the 2e6-orbital workload
-// from 2.6e-7 to 1.7e-5.)
+// to 1.0e-4 or 1.0e-5 (2.6e-7 with Dot2).  The terms of <a_n+1|a_n> change
+// sign; a plain sum there left the error at 2.6e-7 and saved 0.7 % of the
+// step.  (An anchored sum with a per-vector anchor >= 4 mu_0, which bounds
+// every partial sum, was measured too: the anchor is then far above a
+// row's terms, their fractional parts land in the FP32 residual sum, and
+// its bias took the outer-node error from 2.6e-7 to 1.7e-5.)
 //
 // The H values themselves stay complex64 (2H/a): rounding them perturbs the
 // Hamiltonian, whose moments are still those of a Hermitian operator, and
@@ -421,7 +420,7 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
                             __fadd_rn(LP[k].y, LQ[k].x)));
               float2 h = __fadd2_rn(v, cc);                 // hi = RN(v)
               float2 l = __fadd2_rz(sub2(v, h), cc);        // lo = RZ(v - hi)
-              if constexpr (MODE == STEP_FIRST) {           // a_1 = (2 H~ a_0) / 2
+              if constexpr (MODE == STEP_FIRST) {   // a_1 = (2 H~ a_0) / 2
                 h = __fmul2_rn(h, f2(0.5f));
                 l = __fmul2_rn(l, f2(0.5f));
               }
@@ -459,7 +458,8 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
               for (int k = 0; k < 2; ++k) {
                 dot2(dns[k], dnc[k], xk[k], xk[k]);
                 drs[k] = __ffma2_rn(ohi[k], xk[k], drs[k]);
-                fim[k] = fmaf(ohi[k].x, xk[k].y, fmaf(-ohi[k].y, xk[k].x, fim[k]));
+                fim[k] = fmaf(ohi[k].x, xk[k].y,
+                              fmaf(-ohi[k].y, xk[k].x, fim[k]));
               }
             }
             if (++pending == FLUSH) {
