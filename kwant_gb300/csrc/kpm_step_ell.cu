@@ -14,8 +14,8 @@
 // values of a warp's next rows are copied into shared memory with cp.async
 // (16-byte chunks, no row-pointer load) while the current ones compute, so
 // a row's gathers go out together with its own vector entry and its
-// alpha_{n-1} entry: one
-// dependent memory round trip per row (a CSR row costs four).  The FP64
+// alpha_{n-1} entry: one dependent memory round trip per row (a CSR row
+// costs four).  The FP64
 // dot-product accumulators live in shared memory to keep registers (and so
 // occupancy) low.
 
