@@ -146,3 +146,42 @@ def test_edge_sizes_match_oracle(kpm, precision, N, R, M):
     tol = 1e-12 if precision == 'fp64' else 1e-5
     assert np.max(np.abs(got - ref)) <= tol * N
     assert s.densities.shape == (2 * M,)
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'mixed'])
+def test_doubling_dos_equals_identity_operator(kpm, precision):
+    """kwant/tests/test_kpm.py:342-353: the DOS from the doubling identities
+    (operator=None) and from the identity operator (one moment per step,
+    no doubling) agree: 1e-12 in FP64; in mixed precision the compensated
+    DOS step and the plain complex64 operator path agree within the
+    latter's rounding (1e-6 of the DOS maximum)."""
+    from kwant_gb300 import lattices
+    syst = lattices.honeycomb(30, t=1.0, flux=1e-2, W=0.5, seed=1)
+    ham = syst.hamiltonian_submatrix(sparse=True).tocsr()
+    n = ham.shape[0]
+    g = float(np.max(np.asarray(abs(ham).sum(axis=1))))
+    kw = dict(num_moments=120, num_vectors=6, rng=3, bounds=(-g, g),
+              precision=precision)
+    dos = kpm.SpectralDensity(ham, **kw)
+    ident = kpm.SpectralDensity(ham, operator=sp.identity(n, format='csr'),
+                                **kw)
+    tol = 1e-12 if precision == 'fp64' else 1e-6
+    assert np.array_equal(dos.energies, ident.energies)
+    scale = np.max(np.abs(dos.densities))
+    assert np.max(np.abs(dos.densities - ident.densities)) < tol * scale
+
+
+def test_system_sparse_and_dense_hamiltonians_agree(kpm):
+    """kwant/tests/test_kpm.py:393-408: the same Hamiltonian given as a
+    system, a sparse matrix and a dense array gives the same moments."""
+    from kwant_gb300 import lattices
+    syst = lattices.square(12, t=1.0, seed=4)
+    ham = syst.hamiltonian_submatrix(sparse=True).tocsr()
+    kw = dict(num_moments=80, num_vectors=4, rng=9)
+    a = kpm.SpectralDensity(syst, **kw)
+    b = kpm.SpectralDensity(ham, **kw)
+    c = kpm.SpectralDensity(ham.toarray(), **kw)
+    for other in (b, c):
+        assert np.allclose(other._a, a._a, rtol=0, atol=1e-12 * a._a)
+        assert np.max(np.abs(np.array(other._moments_list) -
+                             np.array(a._moments_list))) < 1e-10
