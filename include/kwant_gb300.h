@@ -387,6 +387,16 @@ KPM_API int kpm_fermi_sums(int64_t n, const double* energies,
                            const double* values, int64_t P, const double* mu,
                            const double* temperature, double* out);
 
+/* Learned-surrogate ensemble on the device (no reference counterpart): the
+ * DOS of each of E members (E <= 8) at K energies is members[e][p] . At[:,k]
+ * (members E x P x M, At M x K, both FP64 row-major); spread[p] = the
+ * largest over k of the members' standard deviation (ddof 1); with ref
+ * (P x M moments), err[p] = the largest |member mean - ref[p] . At[:,k]|.
+ * err may be NULL; it needs ref. */
+KPM_API int kpm_ensemble_dos(int64_t E, int64_t P, int64_t M, int64_t K,
+                             const double* members, const double* At,
+                             const double* ref, double* spread, double* err);
+
 /* Integral factor of Correlator._build_integral_factor (kwant/kpm.py:
  * 720-760) on the device: mu (M x M complex128), kernel weights g (M, with
  * g[0] already halved), nodes x_k (2M) -> factor (2M complex128). */

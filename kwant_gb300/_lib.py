@@ -121,6 +121,7 @@ def _load():
         'kpm_correlator_moments': [P, D, D, P, P, P, I64, I64, I, I, P],
         'kpm_integral_factor': [I64, P, P, P, P],
         'kpm_fermi_sums': [I64, P, P, I64, P, I64, P, P, P],
+        'kpm_ensemble_dos': [I64, I64, I64, I64, P, P, P, P, P],
         'kpm_last_kernel_ms': [P, P],
         'kpm_dos_moments_noalloc': [P, D, D, I, P, I64, I64, P, P, P],
         'kpm_last_gemm': [P, P, P],
@@ -551,6 +552,29 @@ def dos(csr, a, b, precision, vecs, M, kernel=KERNEL_JACKSON):
     check(lib.kpm_dos(csr.ref(), float(a), float(b), precision, ptr(vecs), R,
                       M, kernel, ptr(mom), ptr(gam), ptr(rho)))
     return mom, gam, rho
+
+
+def ensemble_dos(members, At, ref=None):
+    """Surrogate ensemble DOS on the device (kpm_ensemble_dos): members
+    (E, P, M) moments, At (M, K) projection to K energies.  Returns the
+    spread (P) and, with ref (P, M), the error of the member mean (P)."""
+    mem = np.ascontiguousarray(members, dtype=np.float64)
+    At = np.ascontiguousarray(At, dtype=np.float64)
+    E, P, M = mem.shape
+    if At.shape[0] != M:
+        raise ValueError('At must be (num_moments, energies)')
+    K = At.shape[1]
+    spread = np.empty(P)
+    err = None
+    rp = None
+    if ref is not None:
+        rp = np.ascontiguousarray(ref, dtype=np.float64)
+        if rp.shape != (P, M):
+            raise ValueError('ref must be (points, num_moments)')
+        err = np.empty(P)
+    check(lib.kpm_ensemble_dos(E, P, M, K, ptr(mem), ptr(At), ptr(rp),
+                               ptr(spread), ptr(err)))
+    return spread, err
 
 
 class Batch:

@@ -318,6 +318,69 @@ __global__ void fermi_sums_kernel(int64_t n, const double* __restrict__ e,
   if (threadIdx.x == 0) out[blockIdx.x] = make_double2(rr[0], ri[0]);
 }
 
+namespace kpm {
+
+// Surrogate ensemble DOS, one block per point p: the DOS of member e at
+// energy k is d_e(k) = sum_n mem[e][p][n] At[n][k]; out the largest (over
+// k) standard deviation over the members (ddof 1) and, with reference
+// moments, the largest |mean_e d_e(k) - sum_n ref[p][n] At[n][k]|.  FP64,
+// the point's moments staged in shared memory, At read along k
+// (coalesced).
+constexpr int ENS_MAX = 8;
+__global__ void ensemble_dos_kernel(int64_t E, int64_t P, int64_t M,
+                                    int64_t K, const double* __restrict__ mem,
+                                    const double* __restrict__ At,
+                                    const double* __restrict__ ref,
+                                    double* __restrict__ spread,
+                                    double* __restrict__ err) {
+  extern __shared__ double sm[];              // (E + 1) x M
+  const int64_t p = blockIdx.x;
+  for (int64_t i = threadIdx.x; i < E * M; i += blockDim.x) {
+    const int64_t e = i / M, n = i % M;
+    sm[i] = mem[(e * P + p) * M + n];
+  }
+  if (ref)
+    for (int64_t n = threadIdx.x; n < M; n += blockDim.x)
+      sm[E * M + n] = ref[p * M + n];
+  __syncthreads();
+  double smax = 0.0, emax = 0.0;
+  for (int64_t k = threadIdx.x; k < K; k += blockDim.x) {
+    double d[ENS_MAX], dr = 0.0;
+    for (int e = 0; e < ENS_MAX; ++e) d[e] = 0.0;
+    for (int64_t n = 0; n < M; ++n) {
+      const double a = At[n * K + k];
+#pragma unroll
+      for (int e = 0; e < ENS_MAX; ++e)
+        if (e < E) d[e] = fma(sm[e * M + n], a, d[e]);
+      if (ref) dr = fma(sm[E * M + n], a, dr);
+    }
+    double mean = 0.0;
+    for (int e = 0; e < E; ++e) mean += d[e];
+    mean /= (double)E;
+    double var = 0.0;
+    for (int e = 0; e < E; ++e) var += (d[e] - mean) * (d[e] - mean);
+    if (E > 1) smax = fmax(smax, sqrt(var / (double)(E - 1)));
+    if (ref) emax = fmax(emax, fabs(mean - dr));
+  }
+  __shared__ double rs[256], re[256];
+  rs[threadIdx.x] = smax;
+  re[threadIdx.x] = emax;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) {
+      rs[threadIdx.x] = fmax(rs[threadIdx.x], rs[threadIdx.x + s]);
+      re[threadIdx.x] = fmax(re[threadIdx.x], re[threadIdx.x + s]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    spread[p] = rs[0];
+    if (err) err[p] = re[0];
+  }
+}
+
+}  // namespace kpm
+
 extern "C" {
 
 int kpm_chebval(int64_t M, int64_t W, const double* coefs, int64_t E,
@@ -466,6 +529,68 @@ int kpm_fermi_sums(int64_t n, const double* energies, const double* weights,
   dev_free(dout, s);
   if (st != KPM_OK) return st;
   KPM_CUDA(e);
+  return KPM_OK;
+}
+
+
+int kpm_ensemble_dos(int64_t E, int64_t P, int64_t M, int64_t K,
+                     const double* members, const double* At,
+                     const double* ref, double* spread, double* err) {
+  NvtxRange nvtx("kpm_ensemble_dos");
+  KPM_REQUIRE(E > 0 && E <= kpm::ENS_MAX && P > 0 && M > 0 && K > 0 &&
+                  members && At && spread && (err == nullptr || ref),
+              "kpm_ensemble_dos: invalid argument");
+  KPM_REQUIRE(P < (int64_t)1 << 31 && (E + 1) * M * 8 <= 160 * 1024,
+              "kpm_ensemble_dos: sizes too large");
+  int dev, sms;
+  KPM_TRY(init_device(&dev, &sms));
+  cudaStream_t s = 0;
+  double *dm = nullptr, *da = nullptr, *dr = nullptr, *ds = nullptr,
+         *de = nullptr;
+  int st = dev_alloc((void**)&dm, (size_t)E * P * M * 8, s);
+  if (st == KPM_OK) st = dev_alloc((void**)&da, (size_t)M * K * 8, s);
+  if (st == KPM_OK && ref) st = dev_alloc((void**)&dr, (size_t)P * M * 8, s);
+  if (st == KPM_OK) st = dev_alloc((void**)&ds, (size_t)P * 8, s);
+  if (st == KPM_OK && err) st = dev_alloc((void**)&de, (size_t)P * 8, s);
+  cudaError_t e = cudaSuccess;
+  if (st == KPM_OK) {
+    e = cudaMemcpyAsync(dm, members, (size_t)E * P * M * 8,
+                        cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(da, At, (size_t)M * K * 8, cudaMemcpyHostToDevice,
+                          s);
+    if (e == cudaSuccess && ref)
+      e = cudaMemcpyAsync(dr, ref, (size_t)P * M * 8, cudaMemcpyHostToDevice,
+                          s);
+    const size_t smem = (size_t)(E + 1) * M * 8;
+    if (e == cudaSuccess && smem > 48 * 1024)
+      e = cudaFuncSetAttribute(ensemble_dos_kernel,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem);
+    if (e == cudaSuccess) {
+      ensemble_dos_kernel<<<(unsigned)P, 256, smem, s>>>(E, P, M, K, dm, da,
+                                                        dr, ds, de);
+      count_launch(1);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(spread, ds, (size_t)P * 8, cudaMemcpyDeviceToHost,
+                          s);
+    if (e == cudaSuccess && err)
+      e = cudaMemcpyAsync(err, de, (size_t)P * 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  }
+  dev_free(dm, s);
+  dev_free(da, s);
+  dev_free(dr, s);
+  dev_free(ds, s);
+  dev_free(de, s);
+  if (st != KPM_OK) return st;
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_error("kpm_ensemble_dos: %s", cudaGetErrorString(e));
+    return KPM_ECUDA;
+  }
   return KPM_OK;
 }
 

@@ -228,20 +228,19 @@ class MomentSurrogate:
         mem = self.predict_members(points)
         if len(self.nets) < 2:                        # no spread: no estimate
             return mem[0], np.full(mem.shape[1], np.inf)
-        dos = mem @ dos_op.T                          # E x P x K
-        spread = dos.std(axis=0, ddof=1).max(axis=1)
+        # the members' DOS and its spread on the device
+        spread, _ = _lib.ensemble_dos(mem, np.ascontiguousarray(dos_op.T))
         return mem.mean(axis=0), self.scale * spread
 
     def calibrate(self, points, moments, dos_op, quantile=0.95):
         """Set ``scale`` so that the estimate covers the actual DOS error
         (against the given KPM moments) on ``quantile`` of the points."""
         mem = self.predict_members(points)
-        dos = mem @ dos_op.T
-        err = np.abs(dos.mean(axis=0) - moments @ dos_op.T).max(axis=1)
+        spread, err = _lib.ensemble_dos(mem, np.ascontiguousarray(dos_op.T),
+                                        ref=moments)
         if len(self.nets) < 2:
             self.scale = np.inf
             return err, np.full(err.shape, np.inf)
-        spread = dos.std(axis=0, ddof=1).max(axis=1)
         self.scale = float(np.quantile(err / np.maximum(spread, 1e-300),
                                        quantile))
         return err, spread

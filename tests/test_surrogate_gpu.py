@@ -252,3 +252,22 @@ def test_surrogate_sweep_fallback_is_plain_kpm(lib):
     assert np.mean(err[accept] <= tol) >= 0.8
     sur.close()
     sw.close()
+
+
+def test_ensemble_dos_on_device_matches_numpy():
+    """kpm_ensemble_dos (the surrogate's DOS spread and calibration error
+    on the device) against the same projections in numpy, FP64."""
+    from kwant_gb300 import _lib, surrogate as S
+    rng = np.random.RandomState(4)
+    E, P, M = 4, 37, 96
+    A, _ = S.dos_operator(M, 2.5, 0.1)
+    mem = rng.randn(E, P, M) * np.exp(-np.arange(M) / 30.0)
+    ref = rng.randn(P, M) * np.exp(-np.arange(M) / 30.0)
+    spread, err = _lib.ensemble_dos(mem, np.ascontiguousarray(A.T), ref=ref)
+    dos = mem @ A.T
+    want_s = dos.std(axis=0, ddof=1).max(axis=1)
+    want_e = np.abs(dos.mean(axis=0) - ref @ A.T).max(axis=1)
+    assert np.allclose(spread, want_s, rtol=1e-12, atol=1e-14)
+    assert np.allclose(err, want_e, rtol=1e-12, atol=1e-14)
+    s2, e2 = _lib.ensemble_dos(mem[:1], np.ascontiguousarray(A.T))
+    assert np.all(s2 == 0.0) and e2 is None
