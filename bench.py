@@ -363,9 +363,6 @@ def run_ours(args):
             traffic = B * (774.5 / 794.0)
 
     # ---- e2e through the C ABI one-shot call (host buffers) ----------------
-    # (right after the device-resident timed region: measured after the
-    # FP64 accuracy pass instead, the same call took up to 1.16 s against
-    # 1.04 s, although in a separate process an FP64 pass left it at 1.03 s)
     e2e = None
     if args.e2e and rank == 0 and args.precision != 'single':
         pin_vec = torch.empty((R, n, 2), dtype=torch.float64,
@@ -981,8 +978,12 @@ def run_surrogate(args):
     M, R = args.sur_moments, args.sur_vectors
     t0 = time.perf_counter()
     fam = lattices.honeycomb_family(args.sur_cells, seed=0)
+    # plain complex64 recursion: the DOS is judged at |x| <= 0.95, where it
+    # is within ~3e-7 of the FP64 path, far below the R = 32 stochastic
+    # error (~6e-4) that bounds every tolerance here; the compensated step
+    # would cost 1.6x the time per point for no visible difference
     sweep = S.MomentSweep(fam, box, num_moments=M, num_vectors=R,
-                          precision='mixed', rng=1)
+                          precision='single', rng=1)
     A, _ = S.dos_operator(M, sweep.a, sweep.b)
     setup_s = time.perf_counter() - t0
     Xtr = S.random_points(box, args.sur_train, 11)
