@@ -978,7 +978,7 @@ def run_surrogate(args):
     M, R = args.sur_moments, args.sur_vectors
     t0 = time.perf_counter()
     fam = lattices.honeycomb_family(args.sur_cells, seed=0)
-    # plain complex64 recursion: the DOS is judged at |x| <= 0.95, where it
+    # plain complex64 recursion: the DOS is compared at |x| <= 0.95, where it
     # is within ~3e-7 of the FP64 path, far below the R = 32 stochastic
     # error (~6e-4) that bounds every tolerance here; the compensated step
     # would cost 1.6x the time per point for no visible difference
@@ -1000,7 +1000,7 @@ def run_surrogate(args):
                      batch=256, lr=1e-3)
     train_s = time.perf_counter() - t0
     cal_err, cal_spread = sur.calibrate(Xtr[-ncal:], Ytr[-ncal:], A)
-    # plain sweep of the held-out points (also the judge of the errors)
+    # plain sweep of the held-out points (also the reference of the errors)
     t0 = time.perf_counter()
     Yte = sweep.moments(Xte)
     plain_s = time.perf_counter() - t0
@@ -1040,8 +1040,7 @@ def run_surrogate(args):
             args.sur_tol < float(np.median(noise)),
         'note': 'the plain sweep (R vectors) is itself uncertain by its '
                 'stochastic DOS error; a tolerance below it cannot be '
-                'certified by the R-vector KPM check that judges the '
-                'surrogate'}
+                'certified by the R-vector KPM check of the surrogate'}
     line = {
         'metric': 'held-out sweep points/s at DOS Linf error <= tol '
                   '(surrogate + KPM fallback)',

@@ -1,6 +1,6 @@
 // Learned moment surrogate: a small MLP trained and evaluated on the GPU
 // with hand-written kernels (no reference counterpart; the plain KPM is its
-// judge and fallback).
+// error check and fallback).
 //
 //   x (model parameters) -> [Linear -> GELU] x (L-1) -> Linear -> moments
 //

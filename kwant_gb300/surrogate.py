@@ -19,7 +19,7 @@ module puts a learned map in front of it:
     is its error estimate.
 ``SurrogateSweep``
     predictions where the estimated DOS error is at most ``tol`` and the
-    plain KPM (the fallback and the judge) everywhere else.
+    plain KPM (the fallback and the error check) everywhere else.
 
 DOS conventions: per site and per unit energy, Jackson kernel, at the
 Chebyshev nodes x_k of 2M points with |x_k| <= ``x_max`` (energies
