@@ -150,11 +150,21 @@ class BatchedDOS:
         t0 = time.perf_counter()
         launches0 = _lib.launch_count()
         if not self._sys:
-            for s, H in enumerate(self._mats):
-                a, b = self.scales[s]
-                h = _lib.Handle(H, a, b, _lib.PREC_MIXED)
-                self._sys.append((h, _lib.Block(h, None,
-                                                num_vectors=self.num_vectors)))
+            made = []
+            try:
+                for s, H in enumerate(self._mats):
+                    a, b = self.scales[s]
+                    h = _lib.Handle(H, a, b, _lib.PREC_MIXED)
+                    made.append((h, None))
+                    made[-1] = (h, _lib.Block(h, None,
+                                              num_vectors=self.num_vectors))
+            except BaseException:
+                for h, blk in made:      # nothing half-built stays resident
+                    if blk is not None:
+                        blk.close()
+                    h.close()
+                raise
+            self._sys = made
         out = np.empty((len(self._sys), self.num_moments), complex)
         for s, (h, blk) in enumerate(self._sys):
             # the device generator of 'single' with this system's key: the
