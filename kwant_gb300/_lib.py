@@ -561,6 +561,8 @@ def ensemble_dos(members, At, ref=None):
     mem = np.ascontiguousarray(members, dtype=np.float64)
     At = np.ascontiguousarray(At, dtype=np.float64)
     E, P, M = mem.shape
+    if not 0 < E <= 8:
+        raise ValueError('the device ensemble takes 1 to 8 members')
     if At.shape[0] != M:
         raise ValueError('At must be (num_moments, energies)')
     K = At.shape[1]
