@@ -43,19 +43,6 @@ class LoweredOperator:
     real0: bool
     scalar: bool           # output is a scalar (sum=True or matrix op)
 
-    def evaluate_host(self, bra, ket):
-        """Numpy evaluation of the term form (test helper)."""
-        bra = np.asarray(bra, complex)
-        ket = np.asarray(ket, complex)
-        seg = np.repeat(np.arange(self.num_terms), np.diff(self.bra_ptr))
-        coef = np.zeros(self.num_terms, complex)
-        np.add.at(coef, seg, np.conj(self.bra_val) * bra[self.bra_col])
-        contrib = np.conj(coef) * ket[self.term_row]
-        out = np.zeros(self.num_outputs, complex)
-        tchunk = np.repeat(np.arange(self.num_chunks), np.diff(self.chunk_ptr))
-        np.add.at(out, self.chunk_out[tchunk], contrib)
-        return out
-
 
 def _finish(term_row, term_out, bra_ptr, bra_col, bra_val, num_outputs,
             sum_, real0, scalar):

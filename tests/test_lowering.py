@@ -11,6 +11,22 @@ from kwant_gb300 import operator as kop
 from kwant_gb300.system import LatticeSystem
 
 
+def evaluate_host(low, bra, ket):
+    """Numpy evaluation of a lowered operator's term form: per term the
+    bra coefficient sum_j conj(b_j) bra[col_j], then conj(coef) ket[row]
+    accumulated into the term's output slot."""
+    bra = np.asarray(bra, complex)
+    ket = np.asarray(ket, complex)
+    seg = np.repeat(np.arange(low.num_terms), np.diff(low.bra_ptr))
+    coef = np.zeros(low.num_terms, complex)
+    np.add.at(coef, seg, np.conj(low.bra_val) * bra[low.bra_col])
+    contrib = np.conj(coef) * ket[low.term_row]
+    out = np.zeros(low.num_outputs, complex)
+    tchunk = np.repeat(np.arange(low.num_chunks), np.diff(low.chunk_ptr))
+    np.add.at(out, low.chunk_out[tchunk], contrib)
+    return out
+
+
 def _rashba_system(g):
     ham = csr(g)
     n = ham.shape[0]
@@ -23,7 +39,7 @@ def test_density_local_matrix_onsite():
     sz = np.diag([1.0, -1.0])
     d = kop.Density(syst, onsite=sz, where=list(g['where_sites']))
     low = kop.lower(d)
-    got = low.evaluate_host(g['bra'], g['ket'])
+    got = evaluate_host(low, g['bra'], g['ket'])
     np.testing.assert_allclose(got, g['dens_loc_call'], rtol=0, atol=1e-12)
 
 
@@ -33,7 +49,7 @@ def test_density_summed():
     d = kop.Density(syst, onsite=np.diag([1.0, -1.0]), sum=True)
     low = kop.lower(d)
     assert low.num_outputs == 1 and low.scalar
-    got = low.evaluate_host(g['bra'], g['ket'])[0]
+    got = evaluate_host(low, g['bra'], g['ket'])[0]
     assert abs(got - g['dens_sz_call']) < 1e-10
 
 
@@ -43,7 +59,7 @@ def test_current_lowering():
     hw = [tuple(x) for x in g['hop_where']]
     c = kop.Current(syst, onsite=np.diag([1.0, -1.0]), where=hw)
     low = kop.lower(c)
-    got = low.evaluate_host(g['bra'], g['ket'])
+    got = evaluate_host(low, g['bra'], g['ket'])
     np.testing.assert_allclose(got, g['cur_call'], rtol=0, atol=1e-12)
 
 
@@ -75,7 +91,7 @@ def test_chain_current_scalar_sites():
     blocks = [ham[a:a + 1, b:b + 1].toarray() for a, b in where]
     ref = ko.current_matels(bra, ket, [(0, 1, 0), (n, 0, n)], where, blocks,
                             np.eye(1))
-    np.testing.assert_allclose(kop.lower(c).evaluate_host(bra, ket), ref,
+    np.testing.assert_allclose(evaluate_host(kop.lower(c), bra, ket), ref,
                                atol=1e-12)
 
 
@@ -87,7 +103,7 @@ def test_matrix_operator_lowering():
     ket = rs.randn(12) + 1j * rs.randn(12)
     low = kop.lower_matrix(O)
     assert low.scalar
-    got = low.evaluate_host(bra, ket)[0]
+    got = evaluate_host(low, bra, ket)[0]
     assert abs(got - np.vdot(bra, O @ ket)) < 1e-12
 
 
@@ -98,7 +114,7 @@ def test_sum_chunking_large():
     assert low.num_chunks == (n + kop.SUM_CHUNK - 1) // kop.SUM_CHUNK
     rs = np.random.RandomState(1)
     v = rs.randn(n) + 1j * rs.randn(n)
-    assert abs(low.evaluate_host(v, v)[0] - np.vdot(v, v)) < 1e-10
+    assert abs(evaluate_host(low, v, v)[0] - np.vdot(v, v)) < 1e-10
 
 
 def test_where_validation():
