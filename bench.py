@@ -731,10 +731,10 @@ def kubo_record(args, steps, warmup, cpu=True, accuracy=True):
         'roofline': {'bound': 'tensor', 'achieved': achieved, 'peak': tpeak,
                      'unit': 'TFLOP/s', 'frac': achieved / tpeak,
                      # ncu dram bytes of one launch on the 60 x 60 x 2,
-                     # R = 16 case: 472.4 + 4.1 MB against 472.0 MB of
+                     # R = 16 case: 477.9 + 9.7 MB against 472.0 MB of
                      # operands (4 BF16 planes x M x K_pad x 2 operands),
                      # scaled
-                     'traffic': (476.5 / 472.0) * 16.0 * M * g_fl /
+                     'traffic': (487.6 / 472.0) * 16.0 * M * g_fl /
                                 (24.0 * M * M) if g_fl else None,
                      'kernel': 'bf16x3_tc_kernel',
                      'mma_flops_per_launch': g_fl, 'avg_launch_ms': g_ms,
@@ -756,6 +756,22 @@ def kubo_record(args, steps, warmup, cpu=True, accuracy=True):
             'sigma_grid': '%d chemical potentials in b +- 0.8 a, T in %s'
                           % (len(mus), temps.tolist()),
             'reference': 'FP64 GPU path, all %d vectors' % R}
+        # the same conductivity with FP16 hi/lo parts (gemm 'fp16x3': same
+        # layout, MMAs and recursions), timed and checked alike
+        step(gemm=4)
+        torch.cuda.synchronize()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        mu16 = step(gemm=4)
+        f1.record(stream)
+        torch.cuda.synchronize()
+        rec['accuracy']['fp16x3'] = {
+            'ms_per_step': f0.elapsed_time(f1),
+            'contraction_ms': h.last_gemm()[0],
+            'mu_rel_linf_vs_fp64': _rel_linf(mu16, mu64),
+            'sigma_xy_rel_linf_vs_fp64': _rel_linf(
+                _sigma_grid(mu16, a, b, M, mus, temps), s_64)}
     if cpu:
         procs = min(args.cpu_procs or os.cpu_count() or 1, R)
         tmp = tempfile.NamedTemporaryFile(suffix='.npz', delete=False)

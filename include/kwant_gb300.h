@@ -365,7 +365,12 @@ KPM_API int kpm_handle_matvec(kpm_handle* h, const double* x, double* y);
  * _velocity, kwant/kpm.py:1042-1085).  gemm selects the contraction:
  *   0 = FP64 CUDA-core GEMM, 1 = tensor-core split-BF16 (hi+lo) GEMM with
  *   FP32 accumulation (tcgen05), 2 = automatic (1 for MIXED, 0 for FP64),
- *   3 = the same BF16 hi/lo products on CUDA cores (checks gemm 1).
+ *   3 = the same BF16 hi/lo products on CUDA cores (checks gemm 1),
+ *   4 = tensor-core split-FP16 (hi+lo) GEMM: gemm 1's layout, MMAs and
+ *   time with 11 instead of 8 significant bits per part, 5 = gemm 4's
+ *   products on CUDA cores (checks gemm 4).  With gemm 4 / 5 a vector entry
+ *   above the FP16 range (65504) makes mu non-finite: KPM_EDIVERGED, with
+ *   mu_out written.
  * mu_out is the mean over vectors (or R x M x M when per_vector). */
 KPM_API int kpm_correlator_moments(kpm_handle* h, double a2, double b2,
                                    const kpm_csr_desc* v_alpha,

@@ -16,9 +16,12 @@
 //   BF16x3: each real component x stored as hi = bf16(x), lo = bf16(x - hi)
 //           in four planes (re_hi, re_lo, im_hi, im_lo); the tensor-core GEMM
 //           (kpm_gemm_tc.cu) forms hi*hi + hi*lo + lo*hi with FP32
-//           accumulation.
+//           accumulation.  FP16x3: the same with IEEE half parts (11
+//           significant bits each instead of 8).
 
 #include <cuda_bf16.h>
+
+#include <cmath>
 
 #include "kpm_common.cuh"
 #include "kpm_internal.cuh"
@@ -282,7 +285,10 @@ int kpm_correlator_moments(kpm_handle* h, double a2, double b2,
               "kpm_correlator_moments: operator shape mismatch");
   KPM_REQUIRE(a2 > 0, "kpm_correlator_moments: a2 must be positive");
   if (gemm == 2) gemm = h->precision == KPM_PREC_MIXED ? 1 : 0;
-  KPM_REQUIRE(gemm >= 0 && gemm <= 3, "kpm_correlator_moments: bad gemm");
+  KPM_REQUIRE(gemm >= 0 && gemm <= 5 && gemm != 2,
+              "kpm_correlator_moments: bad gemm");
+  const bool simt = gemm == 3 || gemm == 5;   // CUDA-core split products
+  const int f16 = gemm >= 4;                  // FP16 planes
   if (gemm != 0 && per_vector) {
     set_error("kpm_correlator_moments: per-vector moments need gemm=0");
     return KPM_EUNSUPPORTED;
@@ -307,6 +313,7 @@ int kpm_correlator_moments(kpm_handle* h, double a2, double b2,
   if (st == KPM_OK && want_fuse) st = ell_aligned(h, &Vb, &fused);
   if (st == KPM_OK) st = store_alloc(&psi, kind, M, K, s);
   if (st == KPM_OK) st = store_alloc(&omega, kind, M, K, s);
+  psi.f16 = omega.f16 = f16;
   if (st == KPM_OK) st = kpm_block_create(h, vecs, R, 1, &bR);
   if (st == KPM_OK) st = timed_begin(h);
   // Omega's starting vectors v_alpha|r>
@@ -382,12 +389,23 @@ int kpm_correlator_moments(kpm_handle* h, double a2, double b2,
   if (st == KPM_OK) {
     if (gemm == 0)
       st = gemm_fp64(h, &omega, &psi, M, K, R, per_vector, mu_out);
-    else if (gemm == 3)
+    else if (simt)
       st = gemm_bf16x3_simt(h, &omega, &psi, M, K, R, mu_out);
     else
       st = gemm_bf16x3(h, &omega, &psi, M, K, R, mu_out);
   }
   if (st == KPM_OK) st = timed_end(h);
+  if (st == KPM_OK && f16) {
+    // an FP16 part above 65504 becomes infinite: report it, with mu written
+    for (int64_t i = 0; i < 2 * M * M; ++i)
+      if (!std::isfinite(mu_out[i])) {
+        set_error("kpm_correlator_moments: non-finite moments with FP16 "
+                  "planes (a vector entry above the FP16 range); use the "
+                  "bfloat16 or FP64 contraction");
+        st = KPM_EDIVERGED;
+        break;
+      }
+  }
   if (bR) kpm_block_destroy(bR);
   store_free(&psi, s);
   store_free(&omega, s);

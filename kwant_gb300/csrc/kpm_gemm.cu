@@ -86,12 +86,21 @@ gemm_c128_kernel(const double2* __restrict__ A, const double2* __restrict__ B,
     }
 }
 
-// Same contraction on BF16x3 planes with FP32 products/accumulation per
-// split (hi*hi + hi*lo + lo*hi for every real product).
+// 16-bit plane element as float: bfloat16, or FP16 when f16
+__device__ __forceinline__ float plane_value(const __nv_bfloat16* p,
+                                             int64_t i, int f16) {
+  return f16 ? __half2float(reinterpret_cast<const __half*>(p)[i])
+             : __bfloat162float(p[i]);
+}
+
+// Same contraction on BF16x3 planes (bfloat16, or FP16 when f16) with FP32
+// products/accumulation per split (hi*hi + hi*lo + lo*hi for every real
+// product).
 __global__ void __launch_bounds__(256)
 gemm_bf16x3_simt_kernel(const __nv_bfloat16* __restrict__ A,
                         const __nv_bfloat16* __restrict__ B, int64_t M,
-                        int64_t Kp, int64_t K, double2* __restrict__ part) {
+                        int64_t Kp, int64_t K, int f16,
+                        double2* __restrict__ part) {
   const int64_t tm = blockIdx.x, tn = blockIdx.y, sp = blockIdx.z;
   const int64_t splits = gridDim.z;
   const int64_t chunk = ceil_div(K, splits);
@@ -107,10 +116,10 @@ gemm_bf16x3_simt_kernel(const __nv_bfloat16* __restrict__ A,
       const int64_t ma = tm * GT + r, nb = tn * GT + r;
       for (int q = 0; q < 4; ++q) {
         As[q][r][c] = (kk < ke && ma < M)
-                          ? __bfloat162float(A[store_index(M, q, ma, kk)])
+                          ? plane_value(A, store_index(M, q, ma, kk), f16)
                           : 0.f;
         Bs[q][r][c] = (kk < ke && nb < M)
-                          ? __bfloat162float(B[store_index(M, q, nb, kk)])
+                          ? plane_value(B, store_index(M, q, nb, kk), f16)
                           : 0.f;
       }
     }
@@ -223,8 +232,9 @@ int gemm_bf16x3_simt(kpm_handle* h, const Store* omega, const Store* psi,
   KPM_TRY(dev_alloc((void**)&part, (size_t)splits * M * M * sizeof(double2),
                     h->stream));
   dim3 grid((unsigned)tiles1, (unsigned)tiles1, (unsigned)splits);
+  KPM_REQUIRE(omega->f16 == psi->f16, "gemm_bf16x3_simt: plane types differ");
   gemm_bf16x3_simt_kernel<<<grid, 256, 0, h->stream>>>(
-      omega->planes, psi->planes, M, omega->Kp, K, part);
+      omega->planes, psi->planes, M, omega->Kp, K, omega->f16, part);
   count_launch(1);
   int st = KPM_OK;
   if (cudaGetLastError() != cudaSuccess) {

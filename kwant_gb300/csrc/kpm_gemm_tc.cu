@@ -4,7 +4,10 @@
 //
 // (Correlator._calculate_moments_matrix, kwant/kpm.py:685-695) on BF16x3
 // stores: every real component x is held as hi = bf16(x), lo = bf16(x - hi),
-// in four K-major planes (re_hi, re_lo, im_hi, im_lo).  With A = Omega,
+// in four K-major planes (re_hi, re_lo, im_hi, im_lo); FP16 stores hold
+// hi = half(x), lo = half(x - hi) in the same layout and run the same MMAs
+// with both operand formats set to FP16 (~2^-22 instead of ~2^-16 relative
+// per product, for the same time).  With A = Omega,
 // B = Psi:
 //   Re mu = Ar Br^T + Ai Bi^T,   Im mu = Ar Bi^T - Ai Br^T,
 // and every real product X Y^T is formed as Xh Yh^T + Xh Yl^T + Xl Yh^T
@@ -45,15 +48,50 @@ struct TcArgs {
   int splits;
   int nt;           // output columns per CTA (multiple of 16, <= 256)
   int ntiles_n;
-  int tmem_cols;    // power of two >= 2 * nt
+  int tmem_cols;    // power of two >= 2 * nt (4 * nt when promoting)
   float2* part;     // [split][M][M] (re, im) partials
   int* err;
   uint64_t wait_ns; // bound of every mbarrier wait
   int stall;        // test only: the producer issues no loads
+  int f16;          // FP16 planes (else bfloat16); A and B alike
+  int64_t promote;  // K chunks per FP32 accumulation run (0: the split)
 };
 
+// warps: 0 allocates tensor memory and runs the TMA producer (one lane),
+// 1 issues the MMAs (one lane), 2-5 drain the accumulators; warp w reaches
+// the tensor-memory lanes 32 (w % 4) .. 32 (w % 4) + 31, so warps 2-5 cover
+// all 128 rows of the tile.
+constexpr int GEMM_THREADS = 192;
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t addr, uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]),
+        "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]),
+        "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+        "=r"(v[15])
+      : "r"(addr));
+}
+
+__device__ __forceinline__ void tmem_st16(uint32_t addr,
+                                          const uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+      "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(addr),
+      "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]),
+      "r"(v[6]), "r"(v[7]), "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]),
+      "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15])
+      : "memory");
+}
+
 template <int KC, int STAGES>
-__global__ void __launch_bounds__(THREADS, 1)
+__global__ void __launch_bounds__(GEMM_THREADS, 1)
 bf16x3_tc_kernel(const __grid_constant__ CUtensorMap map_a,
                  const __grid_constant__ CUtensorMap map_b, TcArgs args) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -67,8 +105,10 @@ bf16x3_tc_kernel(const __grid_constant__ CUtensorMap map_a,
   uint8_t* sb = smem + STAGES * a_bytes;       // STAGES x b_bytes
   uint64_t* full = reinterpret_cast<uint64_t*>(sb + STAGES * b_bytes);
   uint64_t* empty = full + STAGES;
-  uint64_t* done = empty + STAGES;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  uint64_t* done = empty + STAGES;   // every MMA of the CTA completed
+  uint64_t* promo = done + 1;        // a run's MMAs completed
+  uint64_t* resume = promo + 1;      // its accumulators were drained
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(resume + 1);
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   // tile / split of this CTA
@@ -80,6 +120,10 @@ bf16x3_tc_kernel(const __grid_constant__ CUtensorMap map_a,
   const int64_t kc0 = split * c_per;
   const int64_t kc1 = kc0 + c_per < args.kchunks ? kc0 + c_per : args.kchunks;
   const int64_t nk = kc1 > kc0 ? kc1 - kc0 : 0;
+  // FP32 accumulation runs of `run` K chunks; each run's sums are added
+  // into a master copy in tensor memory (FP32, round to nearest)
+  const int64_t run = args.promote > 0 ? args.promote : (nk > 0 ? nk : 1);
+  const int64_t runs = ceil_div(nk, run);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -87,6 +131,8 @@ bf16x3_tc_kernel(const __grid_constant__ CUtensorMap map_a,
       mbar_init(&empty[s], 1);
     }
     mbar_init(done, 1);
+    mbar_init(promo, 1);
+    mbar_init(resume, 4);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -119,12 +165,22 @@ bf16x3_tc_kernel(const __grid_constant__ CUtensorMap map_a,
     drain_loads(full, STAGES, issued, args.err, args.wait_ns);
   } else if (warp == 1 && lane == 0) {
     // ---- MMA issuer
-    const uint32_t id_pos = instr_desc(nt, false);
-    const uint32_t id_neg = instr_desc(nt, true);
+    const uint32_t id_pos = instr_desc(nt, false, args.f16 != 0);
+    const uint32_t id_neg = instr_desc(nt, true, args.f16 != 0);
     const uint32_t d_re = tmem, d_im = tmem + (uint32_t)nt;
     const uint32_t plane_a = TM * KC * 2, plane_b = (uint32_t)nt * KC * 2;
     bool ok = true;
     for (int64_t i = 0; i < nk && ok; ++i) {
+      const int64_t in_run = i % run;
+      if (in_run == 0 && i > 0) {
+        // the previous run's accumulators must be drained first
+        if (!mbar_wait(resume, (uint32_t)((i / run - 1) & 1), args.err, 5,
+                       args.wait_ns)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+      }
       const int s = (int)(i % STAGES);
       const uint32_t ph = (uint32_t)((i / STAGES) & 1);
       if (!mbar_wait(&full[s], ph, args.err, 2, args.wait_ns)) {
@@ -146,7 +202,8 @@ bf16x3_tc_kernel(const __grid_constant__ CUtensorMap map_a,
         const uint64_t Brl = smem_desc<KC>(b0 + 1 * plane_b + ko);
         const uint64_t Bih = smem_desc<KC>(b0 + 2 * plane_b + ko);
         const uint64_t Bil = smem_desc<KC>(b0 + 3 * plane_b + ko);
-        const uint32_t acc0 = (i > 0 || ks > 0) ? 1u : 0u;
+        // the first MMA of a run overwrites the accumulators
+        const uint32_t acc0 = (in_run > 0 || ks > 0) ? 1u : 0u;
         // Re += Ar Br + Ai Bi
         mma_bf16(d_re, Arh, Brh, id_pos, acc0);
         mma_bf16(d_re, Arh, Brl, id_pos, 1u);
@@ -163,59 +220,71 @@ bf16x3_tc_kernel(const __grid_constant__ CUtensorMap map_a,
         mma_bf16(d_im, Ail, Brh, id_neg, 1u);
       }
       mma_commit(&empty[s]);  // frees the stage when these MMAs complete
+      if (in_run == run - 1 || i == nk - 1) mma_commit(promo);  // run done
     }
     mma_commit(done);  // all MMAs of this thread
-  }
-
-  // ---- epilogue: all four warps (the MMA thread always commits `done`);
-  // one thread decides for the CTA, so that every warp takes the same
-  // branch around the warp-collective tensor-memory loads
-  __shared__ int go;
-  asm volatile("tcgen05.fence::before_thread_sync;");
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const bool ok = mbar_wait_all(done, 0, args.wait_ns);
-    if (!ok) atomicCAS(args.err, 0, 3);
-    go = ok && nk > 0 && *(volatile int*)args.err == 0;
-  }
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;");
-  if (go) {
-    const int row = tm * TM + warp * 32 + lane;
-    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+  } else if (warp >= 2) {
+    // ---- drain: after every run, add its accumulators into the master
+    // copy (tensor-memory columns 2 nt .. 4 nt); after the last, write the
+    // sums to this split's partials.  Each warp decides from one lane, so
+    // that its warp-collective tensor-memory accesses are never divergent.
+    const int q = warp % 4;
+    const int row = tm * TM + q * 32 + lane;
+    const uint32_t lane_base = (uint32_t)(q * 32) << 16;
+    const uint32_t acc = tmem + lane_base, mst = acc + 2 * (uint32_t)nt;
     float2* dst = args.part + ((int64_t)split * args.M + row) * args.M;
-    for (int c = 0; c < nt; c += 16) {
-      uint32_t re[16], im[16];
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-          "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-          : "=r"(re[0]), "=r"(re[1]), "=r"(re[2]), "=r"(re[3]), "=r"(re[4]),
-            "=r"(re[5]), "=r"(re[6]), "=r"(re[7]), "=r"(re[8]), "=r"(re[9]),
-            "=r"(re[10]), "=r"(re[11]), "=r"(re[12]), "=r"(re[13]),
-            "=r"(re[14]), "=r"(re[15])
-          : "r"(tmem + lane_base + (uint32_t)c));
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-          "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-          : "=r"(im[0]), "=r"(im[1]), "=r"(im[2]), "=r"(im[3]), "=r"(im[4]),
-            "=r"(im[5]), "=r"(im[6]), "=r"(im[7]), "=r"(im[8]), "=r"(im[9]),
-            "=r"(im[10]), "=r"(im[11]), "=r"(im[12]), "=r"(im[13]),
-            "=r"(im[14]), "=r"(im[15])
-          : "r"(tmem + lane_base + (uint32_t)(nt + c)));
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (row < args.M) {
+    for (int64_t g = 0; g < runs; ++g) {
+      int ok = 1;
+      if (lane == 0)
+        ok = mbar_wait(promo, (uint32_t)(g & 1), args.err, 3, args.wait_ns);
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const bool last = g == runs - 1;
+      for (int c = 0; c < 2 * nt; c += 16) {
+        // columns c .. c + 15 of [re (nt) | im (nt)]
+        uint32_t v[16], m[16];
+        tmem_ld16(acc + (uint32_t)c, v);
+        if (g > 0) tmem_ld16(mst + (uint32_t)c, m);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (g > 0) {
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int64_t col = (int64_t)tn * nt + c + j;
-          if (col < args.M)
-            dst[col] = make_float2(__uint_as_float(re[j]),
-                                   __uint_as_float(im[j]));
+          for (int j = 0; j < 16; ++j)
+            v[j] = __float_as_uint(__uint_as_float(v[j]) +
+                                   __uint_as_float(m[j]));
         }
+        if (!last) {
+          tmem_st16(mst + (uint32_t)c, v);
+        } else if (row < args.M) {
+          const bool im = c >= nt;
+          const int64_t col0 = (int64_t)tn * nt + (im ? c - nt : c);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int64_t col = col0 + j;
+            if (col < args.M) {
+              if (im) dst[col].y = __uint_as_float(v[j]);
+              else dst[col].x = __uint_as_float(v[j]);
+            }
+          }
+        }
+      }
+      if (!last) {
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(resume);
       }
     }
   }
+
+  // ---- release: no MMA may still be running when the tensor memory is
+  // freed (the MMA thread always commits `done`)
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
+  if (threadIdx.x == 0 && !mbar_wait_all(done, 0, args.wait_ns))
+    atomicCAS(args.err, 0, 3);
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
   if (warp == 0) {
     asm volatile(
         "tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
@@ -256,7 +325,10 @@ static int make_map(CUtensorMap* map, const Store* s, int box_rows) {
                            (cuuint64_t)4 * s->M * STORE_KB * 2};
   cuuint32_t box[4] = {(cuuint32_t)KC, (cuuint32_t)box_rows, 4, 1};
   cuuint32_t estr[4] = {1, 1, 1, 1};
-  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, s->planes, dims,
+  CUresult r = fn(map,
+                  s->f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                         : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
+                  4, s->planes, dims,
                   strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                   KC == 32 ? CU_TENSOR_MAP_SWIZZLE_64B
                            : CU_TENSOR_MAP_SWIZZLE_32B,
@@ -274,16 +346,22 @@ static int make_map(CUtensorMap* map, const Store* s, int box_rows) {
 template <int KC, int STAGES>
 static int gemm_bf16x3_tc_kc(kpm_handle* h, const Store* omega,
                              const Store* psi, int64_t M, int64_t R, int nt,
-                             double* mu_host) {
+                             int64_t run_k, double* mu_host) {
   using namespace tc;
   KPM_REQUIRE(omega->kind == STORE_BF16X3 && psi->kind == STORE_BF16X3,
               "tensor-core contraction needs BF16x3 stores");
+  // one MMA kind::f16 takes A and B of the same type
+  KPM_REQUIRE(omega->f16 == psi->f16,
+              "tensor-core contraction: plane types differ");
   KPM_REQUIRE(omega->Kp % KC == 0 && omega->Kp == psi->Kp,
               "store K padding mismatch");
   KPM_REQUIRE(M < (1 << 20), "too many moments");
   const int ntiles_n = (int)ceil_div(M, nt);
+  // runs of run_k K elements need a master copy of the accumulators in
+  // tensor memory: 4 nt <= 512 columns
+  const int64_t promote = run_k > 0 && 4 * nt <= 512 ? ceil_div(run_k, KC) : 0;
   int tmem_cols = 32;
-  while (tmem_cols < 2 * nt) tmem_cols *= 2;
+  while (tmem_cols < (promote ? 4 : 2) * nt) tmem_cols *= 2;
   const int64_t kchunks = omega->Kp / KC;
   const int tiles = (int)(ceil_div(M, TM) * ntiles_n);
   // one CTA per SM in total, split K among the tiles
@@ -300,7 +378,7 @@ static int gemm_bf16x3_tc_kc(kpm_handle* h, const Store* omega,
 
   const size_t a_bytes = 4 * TM * KC * 2, b_bytes = (size_t)4 * nt * KC * 2;
   const size_t smem = 1024 + STAGES * (a_bytes + b_bytes) +
-                      (2 * STAGES + 1) * 8 + 16;
+                      (2 * STAGES + 3) * 8 + 16;
   KPM_CUDA(cudaFuncSetAttribute(bf16x3_tc_kernel<KC, STAGES>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem));
@@ -318,9 +396,11 @@ static int gemm_bf16x3_tc_kc(kpm_handle* h, const Store* omega,
   if (st == KPM_OK && e == cudaSuccess) {
     const WaitCfg wc = wait_cfg();
     TcArgs args{M,    kchunks, splits, nt,      ntiles_n,
-                tmem_cols, part, err,  wc.ns,   wc.stall};
+                tmem_cols, part, err,  wc.ns,   wc.stall, omega->f16,
+                promote};
     cudaEventRecord(h->ev_gemm0, h->stream);
-    bf16x3_tc_kernel<KC, STAGES><<<(unsigned)(tiles * splits), THREADS, smem,
+    bf16x3_tc_kernel<KC, STAGES><<<(unsigned)(tiles * splits), GEMM_THREADS,
+                                   smem,
                            h->stream>>>(map_a, map_b, args);
     count_launch(1);
     e = cudaGetLastError();
@@ -365,32 +445,45 @@ static int gemm_bf16x3_tc_kc(kpm_handle* h, const Store* omega,
   return KPM_OK;
 }
 
-// Output tile width nt (MMA N, <= 256; KPM_TC_NT=128 narrows it) and as
-// many pipeline stages as the shared memory holds (at most 4): a 128 x 256
-// tile has 96 KB stages (2), a 128 x 128 tile 64 KB (3).  Measured on the
-// Kubo workload (M = 256, K = 1.28e6, K-blocked stores): 1.11 ms either
-// way (0.95 of the measured BF16 peak); the 256-wide tiles split K over
-// twice as many CTAs, so each FP32 accumulator sums half as many products
-// (moments-matrix error 1.0e-4 against 2.0e-4 relative).  Before the
-// stores were K-blocked the same kernel took 3.09 ms (row-major planes: a
-// stage gathered 512 pieces of 64 bytes, each a 2.5 MB row stride apart).
+// Output tile width nt (MMA N) and as many pipeline stages as the shared
+// memory holds (at most 4): a 128 x 128 tile has 64 KB stages (3), a
+// 128 x 256 tile 96 KB (2).  Measured on the Kubo workload (M = 256,
+// K = 1.28e6, K-blocked stores) both take 1.11 ms (0.95 of the measured
+// BF16 peak); before the stores were K-blocked the same kernel took 3.09 ms
+// (row-major planes: a stage gathered 512 pieces of 64 bytes, each a 2.5 MB
+// row stride apart).
+//
+// The tensor cores' FP32 accumulation error grows with the number of
+// products summed into one accumulator: with one accumulation run per
+// split (K / 76 = 16,800 products per CTA on that workload) the moments
+// matrix was 1.0e-4 off the FP64 contraction, with 4,096 / 1,024 / 256
+// K elements per run 2.5e-5 / 5.8e-6 / 1.5e-6.  So 128-wide tiles (the
+// default) add every run of RUN_K = 1024 K elements into a master copy
+// in tensor memory (FP32, round to nearest) and restart the MMA
+// accumulation.  KPM_TC_NT=256 selects 256-wide tiles (no room for the
+// master copy: one run per split); KPM_TC_RUN sets the run length in K
+// elements (0: one run per split).
+constexpr int64_t RUN_K = 1024;
+
 int gemm_bf16x3(kpm_handle* h, const Store* omega, const Store* psi,
                 int64_t M, int64_t K, int64_t R, double* mu_host) {
   (void)K;
-  int nt_max = 256;
+  int nt_max = 128;
   if (const char* e = getenv("KPM_TC_NT")) nt_max = atoi(e) >= 256 ? 256 : 128;
+  int64_t run_k = RUN_K;
+  if (const char* e = getenv("KPM_TC_RUN")) run_k = atoll(e);
   const int nt = (int)round_up(M < nt_max ? M : nt_max, 16);
   if (h->tc_kc != 32)
     return gemm_bf16x3_tc_kc<16, tc::Stage<16>::STAGES>(h, omega, psi, M, R,
-                                                        nt, mu_host);
+                                                        nt, run_k, mu_host);
   const size_t stage = (size_t)4 * (tc::TM + nt) * 32 * 2;
   const size_t budget = 227 * 1024 - 2048;
   const size_t stages = budget / stage;
   if (stages >= 4)
-    return gemm_bf16x3_tc_kc<32, 4>(h, omega, psi, M, R, nt, mu_host);
+    return gemm_bf16x3_tc_kc<32, 4>(h, omega, psi, M, R, nt, run_k, mu_host);
   if (stages == 3)
-    return gemm_bf16x3_tc_kc<32, 3>(h, omega, psi, M, R, nt, mu_host);
-  return gemm_bf16x3_tc_kc<32, 2>(h, omega, psi, M, R, nt, mu_host);
+    return gemm_bf16x3_tc_kc<32, 3>(h, omega, psi, M, R, nt, run_k, mu_host);
+  return gemm_bf16x3_tc_kc<32, 2>(h, omega, psi, M, R, nt, run_k, mu_host);
 }
 
 }  // namespace kpm

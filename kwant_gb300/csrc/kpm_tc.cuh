@@ -145,12 +145,13 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
   return d;
 }
 
-// Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major,
-// M = 128, N = n; optional negation of A.
-__host__ __device__ constexpr uint32_t instr_desc(int n, bool neg_a) {
+// Instruction descriptor, kind::f16: D = F32, A = B = BF16 (or both FP16
+// when f16), both K-major, M = 128, N = n; optional negation of A.
+__host__ __device__ constexpr uint32_t instr_desc(int n, bool neg_a,
+                                                  bool f16 = false) {
   return (1u << 4)                    // D format F32
-         | (1u << 7)                  // A format BF16
-         | (1u << 10)                 // B format BF16
+         | ((f16 ? 0u : 1u) << 7)     // A format: 0 FP16, 1 BF16
+         | ((f16 ? 0u : 1u) << 10)    // B format (the same as A)
          | ((neg_a ? 1u : 0u) << 13)  // negate A
          | ((uint32_t)(n >> 3) << 17) // N / 8
          | ((uint32_t)(TM >> 4) << 24);  // M / 16

@@ -512,6 +512,30 @@ def test_conductivity_mixed_bf16x3(kpm):
     assert np.all(err <= tol), np.max(err / tol)
 
 
+def test_conductivity_mixed_fp16x3(kpm):
+    """gemm='fp16x3': the same tensor-core products on FP16 hi/lo parts.
+    Against the reference's conductivity fixture the moments matrix is held
+    to 2e-6 relative (the FP16 split alone, emulated in numpy on these
+    vectors: 7.2e-8; the BF16 split: 3.9e-6), and sigma to the error that
+    this moments-matrix error implies, as for 'bf16x3'."""
+    g = load('conductivity')
+    ham = csr(g)
+    pos = g['orb_positions']
+    kw = dict(rng=0, num_moments=48, num_vectors=4,
+              bounds=(g['lmin'], g['lmax']))
+    cond = kpm.conductivity(ham, alpha='x', beta='y', positions=pos,
+                            precision='mixed', gemm='fp16x3', **kw)
+    assert _rel(cond.moments_matrix, g['mu_xy']) < 2e-6
+    vals = np.array([[cond(mu=m, temperature=T) for m in g['mus']]
+                     for T in g['temps']])
+    ref = g['values_xy']
+    bound = _sigma_error_bound(cond.moments_matrix - g['mu_xy'], cond._a,
+                               cond._b, 48, g['mus'], g['temps'])
+    err = np.abs(vals - ref)
+    tol = bound * (1 + 1e-6) + 1e-9 * np.max(np.abs(ref))
+    assert np.all(err <= tol), np.max(err / tol)
+
+
 def test_tensor_core_contraction_matches_cuda_cores(kpm):
     """The tcgen05 split-BF16 GEMM equals the CUDA-core evaluation of the
     same hi*hi + hi*lo + lo*hi products (FP32 sums in another order), and
@@ -541,6 +565,74 @@ def test_tensor_core_contraction_matches_cuda_cores(kpm):
         mu_64 = _lib.correlator_moments(h64, a2, b2, vx, vy, vecs, M, gemm=0)
         assert _rel(mu_tc, mu_cc) < 1e-5, M
         assert _rel(mu_tc, mu_64) < 1e-4, M
+        # FP16 hi/lo parts: the same products with 11-bit parts; a numpy
+        # emulation of the split on this case gives 7.5e-8 (BF16: 4.3e-6)
+        mu_t16 = _lib.correlator_moments(hm, a2, b2, vx, vy, vecs, M, gemm=4)
+        mu_c16 = _lib.correlator_moments(hm, a2, b2, vx, vy, vecs, M, gemm=5)
+        assert _rel(mu_t16, mu_c16) < 2e-6, M
+        assert _rel(mu_t16, mu_64) < 2e-6, M
+
+
+def test_tensor_core_accumulation_runs(kpm, monkeypatch):
+    """At a large K (Rashba 120 x 120 x 2, R = 16: K = 460,800, ~12,000 per
+    CTA) the tensor cores' FP32 accumulation error dominates the moments
+    matrix.  Restarting the accumulation every 1024 K elements (default;
+    the run's sums go into a master copy in tensor memory) must be several
+    times closer to the FP64 contraction than one run per split
+    (KPM_TC_RUN=0), in both part formats; the FP64 path and both formats
+    see the same vectors."""
+    from kwant_gb300 import _lib, lattices
+    syst = lattices.rashba_square(120, seed=0)
+    ham = syst.hamiltonian_submatrix(sparse=True).tocsr()
+    pos = syst.orbital_positions()
+    vx = ko.velocity(ham, pos, 0)
+    vy = ko.velocity(ham, pos, 1)
+    n = ham.shape[0]
+    vecs = np.exp(2j * np.pi * np.random.RandomState(1)
+                  .random_sample((16, n)))
+    g = float(np.max(np.asarray(abs(ham).sum(axis=1))))
+    a, b = ko.rescale_ab(-g, g, 0.05)
+    _a = a * (1 - 0.05 / 2)
+    a2, b2 = ko.rescale_ab(b - _a, b + _a, 0.05)
+    hm = _lib.Handle(ham, a, b, _lib.PREC_MIXED)
+    h64 = _lib.Handle(ham, a, b, _lib.PREC_FP64)
+    M = 256
+    mu_64 = _lib.correlator_moments(h64, a2, b2, vx, vy, vecs, M, gemm=0)
+    for gemm in (1, 4):
+        monkeypatch.delenv('KPM_TC_RUN', raising=False)
+        err_runs = _rel(_lib.correlator_moments(hm, a2, b2, vx, vy, vecs, M,
+                                                gemm=gemm), mu_64)
+        monkeypatch.setenv('KPM_TC_RUN', '0')
+        err_one = _rel(_lib.correlator_moments(hm, a2, b2, vx, vy, vecs, M,
+                                               gemm=gemm), mu_64)
+        assert err_runs < 2e-5 and err_runs * 4 < err_one, \
+            (gemm, err_runs, err_one)
+
+
+def test_fp16_contraction_out_of_range_is_reported(kpm):
+    """Vector entries above the FP16 range (65504) make the FP16 split
+    contraction non-finite: the call reports KPMDiverged (moments written);
+    the BF16 split of the same vectors stays finite and accurate."""
+    from kwant_gb300 import _lib, lattices
+    syst = lattices.rashba_square(8, seed=1)
+    ham = syst.hamiltonian_submatrix(sparse=True).tocsr()
+    pos = syst.orbital_positions()
+    vx = ko.velocity(ham, pos, 0)
+    vy = ko.velocity(ham, pos, 1)
+    n = ham.shape[0]
+    vecs = 1e5 * np.exp(2j * np.pi * np.random.RandomState(2)
+                        .random_sample((2, n)))
+    g = float(np.max(np.asarray(abs(ham).sum(axis=1))))
+    a, b = ko.rescale_ab(-g, g, 0.05)
+    _a = a * (1 - 0.05 / 2)
+    a2, b2 = ko.rescale_ab(b - _a, b + _a, 0.05)
+    hm = _lib.Handle(ham, a, b, _lib.PREC_MIXED)
+    with pytest.raises(_lib.KPMDiverged, match='FP16'):
+        _lib.correlator_moments(hm, a2, b2, vx, vy, vecs, 32, gemm=4)
+    h64 = _lib.Handle(ham, a, b, _lib.PREC_FP64)
+    mu_bf = _lib.correlator_moments(hm, a2, b2, vx, vy, vecs, 32, gemm=1)
+    mu_64 = _lib.correlator_moments(h64, a2, b2, vx, vy, vecs, 32, gemm=0)
+    assert np.all(np.isfinite(mu_bf)) and _rel(mu_bf, mu_64) < 1e-4
 
 
 # --------------------------------------------------------------- reordering
