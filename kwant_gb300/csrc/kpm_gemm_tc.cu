@@ -15,20 +15,32 @@
 // FP32 accumulation in tensor memory, the minus sign through the MMA's
 // negate-A bit.
 //
-// One CTA computes a 128 x NT output tile of both Re and Im (2*NT <= 512
-// TMEM columns) over one K range (split-K); 4 warps: warp 0 allocates TMEM
-// and issues the TMA loads (one 4D box per operand = its four planes of one
-// K block of the K-blocked store), warp 1 issues the MMAs from one thread,
-// all four warps drain TMEM in the epilogue.  Pipeline stages of 32
-// K-elements (64-byte swizzle), as many as the shared memory holds.  The
-// split partials (FP32) are summed in FP64 in a fixed order.
+// One CTA computes a 128 x NT output tile of both Re and Im over one K range
+// (split-K); 6 warps: warp 0 allocates TMEM and issues the TMA loads (one 4D
+// box per operand = its four planes of one K block of the K-blocked store),
+// warp 1 issues the MMAs from one thread, warps 2-5 (one per quarter of the
+// TMEM lanes) drain the accumulators.  Pipeline stages of 32 K-elements
+// (64-byte swizzle), as many as the shared memory holds.
+//
+// Accumulation runs: the MMAs accumulate `promote` K chunks (1024 K
+// elements by default) into TMEM columns [0, 2 NT), then the MMA thread
+// commits to `promo` and waits on `resume`; the drain warps add the run's
+// sums into a master copy in columns [2 NT, 4 NT) (FP32, round to nearest;
+// the first run is copied) and arrive on `resume`, and the next run's first
+// MMA overwrites the accumulators.  After the last run the drain warps write
+// accumulators + master to this split's FP32 partials, which are summed in
+// FP64 in a fixed order.  The tensor cores' FP32 accumulation error grows
+// with the products summed into one accumulator; the runs bound that count.
+// 256-wide tiles (2 NT = 512 columns) leave no room for the master copy and
+// run one accumulation per split.
 //
 // Every wait on an mbarrier is bounded (2 s of GPU time by default,
 // KPM_DEBUG_WAIT_NS); on expiry the kernel records an error code and stops
-// issuing work; the producer waits for the loads it already issued, one
-// thread decides for the whole CTA whether the epilogue reads tensor memory
-// (all warps take the same branch), the CTA releases its tensor memory and
-// returns, and the host reports KPM_ETIMEOUT.
+// issuing work: the producer waits for the loads it already issued, each
+// drain warp decides from one lane whether it reads tensor memory (its
+// warp-collective accesses never diverge), the MMA thread always commits
+// `done`, which thread 0 awaits before the CTA releases its tensor memory,
+// and the host reports KPM_ETIMEOUT.
 
 #include <cuda.h>
 #include <cudaTypedefs.h>

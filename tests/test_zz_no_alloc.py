@@ -93,11 +93,13 @@ def test_noalloc_matches_allocating_entry_point(precision):
         got = got[:, :R].T
         err = np.max(np.abs(got - expected)) / np.max(np.abs(expected))
         assert err < TOL[precision], (call, err)
-        if not mixed:
-            ref = g['moments_list']
-            err = np.max(np.abs(got[:, :ref.shape[1]] - ref)) / \
-                np.max(np.abs(ref))
-            assert err < TOL[precision], (call, err)
+        # against the reference's own moments (golden fixture): FP64 to
+        # rounding; the complex64 recursion within 1e-5 of the largest
+        # moment (a numpy complex64 recursion of these vectors: 1e-7)
+        ref = g['moments_list']
+        err = np.max(np.abs(got[:, :ref.shape[1]] - ref)) / \
+            np.max(np.abs(ref))
+        assert err < (1e-5 if mixed else TOL[precision]), (call, err)
 
 
 def test_noalloc_rejects_oversized_requests():
