@@ -571,6 +571,12 @@ def test_tensor_core_contraction_matches_cuda_cores(kpm):
         mu_c16 = _lib.correlator_moments(hm, a2, b2, vx, vy, vecs, M, gemm=5)
         assert _rel(mu_t16, mu_c16) < 2e-6, M
         assert _rel(mu_t16, mu_64) < 2e-6, M
+    # an odd vector count: the store rows are written one value at a time
+    v5 = vecs[:5]
+    mu_64 = _lib.correlator_moments(h64, a2, b2, vx, vy, v5, 48, gemm=0)
+    for gemm, tol in ((1, 1e-4), (4, 2e-6)):
+        mu = _lib.correlator_moments(hm, a2, b2, vx, vy, v5, 48, gemm=gemm)
+        assert _rel(mu, mu_64) < tol, gemm
 
 
 def test_tensor_core_accumulation_runs(kpm, monkeypatch):
