@@ -146,6 +146,13 @@ def _cpu_task(args):
     return time.perf_counter() - t0
 
 
+def _oracle_task(args):
+    """The oracle's FP64 moments of one vector (the checker, untimed)."""
+    from oracle import kpm_oracle as ko
+    vec, M = args
+    return np.array(ko.moments_dos(_W['ham'], _W['a'], _W['b'], vec, M)[0])
+
+
 class CpuBaseline:
     """The oracle port of the reference (one vector at a time, scipy CSR
     matvec + vdot), one spawned process per core over disjoint vectors."""
@@ -166,6 +173,10 @@ class CpuBaseline:
         self.pool.map(_cpu_task, jobs)
         dt = time.perf_counter() - t0
         return self.nnz * self.procs * M / dt, dt
+
+    def oracle_moments(self, vecs, M):
+        """(k, M) oracle moments of the given vectors, one process each."""
+        return np.array(self.pool.map(_oracle_task, [(v, M) for v in vecs]))
 
     def close(self):
         self.pool.close()
@@ -416,9 +427,16 @@ def run_ours(args):
 
     # ---- accuracy vs the FP64 path (untimed) -------------------------------
     accuracy = None
+    nodes = kpm._chebyshev_nodes(2 * M)
+
+    def dos_k(mm):
+        """Densities (mean over the given vectors' moments, Jackson kernel,
+        device reconstruction) at the 2M nodes."""
+        return _lib.reconstruct(mm[:, :, None], True, False, a,
+                                _lib.KERNEL_JACKSON, 4.0, nodes)[1][:, 0]
+
+    mom64 = None
     if args.accuracy and rank == 0:
-        nodes = kpm._chebyshev_nodes(2 * M)
-        mom64 = None
         if prec != _lib.PREC_FP64:
             h64 = _lib.Handle(csr, a, b, _lib.PREC_FP64)
             b64 = _lib.Block(h64, vecs, keep_a0=True)
@@ -433,11 +451,7 @@ def run_ours(args):
             b64.close()
             h64.close()
 
-            def dens(mm):
-                return _lib.reconstruct(mm[:, :, None], True, False, a,
-                                        _lib.KERNEL_JACKSON, 4.0,
-                                        nodes)[1][:, 0]
-            d32, d64 = dens(mom), dens(mom64)
+            d32, d64 = dos_k(mom), dos_k(mom64)
             diff = np.abs(d32 - d64) / n
             # nodes inside the spectral bounds (the eps margin excluded):
             # there the DOS is nonzero; outside it the 1/sqrt(1 - x^2)
@@ -461,11 +475,36 @@ def run_ours(args):
     if args.cpu and rank == 0 and world == 1:
         procs = args.cpu_procs or os.cpu_count() or 1
         base = CpuBaseline(ham, a, b, vecs, procs)
+        om = None
         try:
             base.run(8)  # spawn + load
             v, dt = base.run(args.ref_moments)
+            k = min(args.oracle_vectors, R)
+            if accuracy is not None and k > 0:
+                # the oracle (complex128 scipy recursion of kwant.kpm's
+                # algorithm) on the first k vectors at the full M, after the
+                # timed CPU sample
+                t0 = time.perf_counter()
+                om = base.oracle_moments(vecs[:k], M)
+                o_dt = time.perf_counter() - t0
         finally:
             base.close()
+        if om is not None:
+            from oracle import kpm_oracle as ko
+            rho_o = ko.calc_fft_moments(ko.reduce_moments(om, a))[0]
+            accuracy['oracle'] = {
+                'vectors': int(k), 'moments': int(M),
+                'dos_linf_per_orbital_vs_oracle': float(
+                    np.max(np.abs(dos_k(mom[:k]) - rho_o)) / n),
+                'fp64_gpu_dos_linf_per_orbital_vs_oracle': float(
+                    np.max(np.abs(dos_k(mom64[:k]) - rho_o)) / n),
+                'fp64_gpu_moments_rel_linf_vs_oracle': float(
+                    np.max(np.abs(mom64[:k] - om)) / np.max(np.abs(om))),
+                'oracle_s': o_dt,
+                'reference': 'oracle port of kwant.kpm (complex128 scipy '
+                             'recursion and its own reconstruction) on the '
+                             'same Hamiltonian, vectors and (a, b), the '
+                             'first %d vectors, all 2M nodes' % k}
         cpu = {'value': v, 'unit': UNIT, 'cores': procs, 'kind': 'port',
                'sample': '%d vectors x %d moments of the same workload, one '
                          'spawned process per vector (%.1f s; scipy\'s CSR '
@@ -1134,6 +1173,9 @@ def main():
     p.add_argument('--vectors', type=int, default=64)
     p.add_argument('--moments', type=int, default=2000)
     p.add_argument('--ref-moments', type=int, default=100)
+    p.add_argument('--oracle-vectors', type=int, default=16,
+                   help='vectors of the headline DOS run checked against '
+                        'the oracle at the full M (0: none)')
     p.add_argument('--cpu-procs', type=int, default=0)
     p.add_argument('--no-e2e', dest='e2e', action='store_false')
     p.add_argument('--no-cpu', dest='cpu', action='store_false')
