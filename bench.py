@@ -984,8 +984,64 @@ def run_batch(args):
             rec['accuracy'] = batch_accuracy(bm, mom, Ls, Ws, R, M)
         bm.close()
         line['mixed'] = rec
+    if args.cpu:
+        line['cpu_baseline'] = batch_cpu(args, Ls, Ws, R, M,
+                                         line.get('accuracy'))
     print(json.dumps(line))
     return 0
+
+
+def batch_cpu(args, Ls, Ws, R, M, accuracy):
+    """CPU baseline of the batched workload: the oracle port on the largest
+    system of the batch (its Hamiltonian assembled on the host, exact zeros
+    dropped as in Kwant's CSR), one spawned process per vector over 16
+    vectors x 128 moments.  With accuracy, the oracle's FP64 moments of the
+    smallest system's first 16 device-generated vectors at the full M pin
+    the FP64 GPU path that the batch's own accuracy figures are measured
+    against."""
+    from kwant_gb300 import _lib, batch
+    procs = args.cpu_procs or os.cpu_count() or 1
+    big = int(np.argmax(Ls))
+    H = batch.wilson_dirac_matrix(int(Ls[big]), 1.5, float(Ws[big]), 100 + big)
+    H.eliminate_zeros()
+    n = H.shape[0]
+    g = float(np.max(np.asarray(abs(H).sum(axis=1))))
+    a, b = g / (1 - 0.05 / 2), 0.0
+    vecs = batch.random_phase_vectors(1, big, procs, n).astype(complex)
+    base = CpuBaseline(H, a, b, vecs, procs)
+    try:
+        base.run(8)  # spawn + load
+        v, dt = base.run(args.batch_cpu_moments)
+    finally:
+        base.close()
+    out = {'value': v, 'unit': UNIT, 'cores': procs, 'kind': 'port',
+           'sample': '%d vectors x %d moments of the largest system (L = '
+                     '%d, %d orbitals), one spawned process per vector '
+                     '(%.1f s)' % (procs, args.batch_cpu_moments,
+                                   int(Ls[big]), n, dt),
+           'cpu': _cpu_model()}
+    if accuracy is not None and args.oracle_vectors > 0:
+        s = int(np.argmin(Ls))
+        Hs = batch.wilson_dirac_matrix(int(Ls[s]), 1.5, float(Ws[s]), 100 + s)
+        Hs.eliminate_zeros()
+        k = min(args.oracle_vectors, R, procs)
+        vs = batch.random_phase_vectors(1, s, k, Hs.shape[0]).astype(complex)
+        gs = float(np.max(np.asarray(abs(Hs).sum(axis=1))))
+        a_s, b_s = gs / (1 - 0.05 / 2), 0.0
+        ob = CpuBaseline(Hs, a_s, b_s, vs, k)
+        try:
+            om = ob.oracle_moments(vs, M)
+        finally:
+            ob.close()
+        m64 = _lib.dos(Hs, a_s, b_s, _lib.PREC_FP64, vs, M)[0]
+        accuracy['oracle'] = {
+            'system': 'smallest (L = %d)' % int(Ls[s]), 'vectors': int(k),
+            'moments': int(M),
+            'fp64_gpu_moments_rel_linf_vs_oracle': float(
+                np.max(np.abs(m64 - om)) / np.max(np.abs(om))),
+            'reference': 'oracle port of kwant.kpm (complex128 scipy '
+                         'recursion) on the same Hamiltonian and vectors'}
+    return out
 
 
 def mat_ell_mixed(Ls):
@@ -1173,6 +1229,7 @@ def main():
     p.add_argument('--vectors', type=int, default=64)
     p.add_argument('--moments', type=int, default=2000)
     p.add_argument('--ref-moments', type=int, default=100)
+    p.add_argument('--batch-cpu-moments', type=int, default=128)
     p.add_argument('--oracle-vectors', type=int, default=16,
                    help='vectors of the headline DOS run checked against '
                         'the oracle at the full M (0: none)')
