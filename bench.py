@@ -130,19 +130,32 @@ class ClockSampler:
 _W = {}
 
 
-def _cpu_init(path, a, b):
+def _cpu_init(path, a, b, where=None):
     import scipy.sparse as sp
     d = np.load(path)
     _W['ham'] = sp.csr_matrix((d['data'], d['indices'], d['indptr']),
                               shape=tuple(d['shape']))
     _W['a'], _W['b'] = a, b
+    _W['where'] = where
 
 
 def _cpu_task(args):
     from oracle import kpm_oracle as ko
     vec, M = args
     t0 = time.perf_counter()
-    ko.moments_dos(_W['ham'], _W['a'], _W['b'], vec, M)
+    if _W['where'] is None:
+        ko.moments_dos(_W['ham'], _W['a'], _W['b'], vec, M)
+    else:
+        # Density (identity onsite) on one-orbital sites, the operator path
+        # (kwant/kpm.py:478-484); density_matels' products for norbs = 1,
+        # vectorised over the sites
+        n = _W['ham'].shape[0]
+        start, _ = ko.site_orbitals([(0, 1, 0), (n, 0, n)], _W['where'])
+        start = np.asarray(start)
+
+        def op(bra, ket):
+            return np.conj(bra[start]) * ket[start]
+        ko.moments_operator(_W['ham'], _W['a'], _W['b'], vec, M, op)
     return time.perf_counter() - t0
 
 
@@ -157,7 +170,7 @@ class CpuBaseline:
     """The oracle port of the reference (one vector at a time, scipy CSR
     matvec + vdot), one spawned process per core over disjoint vectors."""
 
-    def __init__(self, ham, a, b, vecs, procs):
+    def __init__(self, ham, a, b, vecs, procs, where=None):
         self.tmp = tempfile.NamedTemporaryFile(suffix='.npz', delete=False)
         self.tmp.close()
         np.savez(self.tmp.name, data=ham.data, indices=ham.indices,
@@ -165,7 +178,8 @@ class CpuBaseline:
         self.nnz = ham.nnz
         self.procs = procs
         self.vecs = vecs
-        self.pool = _spawn_pool(procs, _cpu_init, (self.tmp.name, a, b))
+        self.pool = _spawn_pool(procs, _cpu_init, (self.tmp.name, a, b,
+                                                   where))
 
     def run(self, M):
         t0 = time.perf_counter()
@@ -652,6 +666,20 @@ def run_ldos(args):
                      'launches_timed': n_step},
         'accuracy': accuracy,
     }
+    if args.cpu:
+        procs = args.cpu_procs or os.cpu_count() or 1
+        base = CpuBaseline(ham, a, b, vecs, procs, where=list(where))
+        try:
+            base.run(4)  # spawn + load
+            v, dt = base.run(args.ref_moments)
+        finally:
+            base.close()
+        line['cpu_baseline'] = {
+            'value': v, 'unit': UNIT, 'cores': procs, 'kind': 'port',
+            'sample': '%d vectors x %d moments of the same workload (operator '
+                      'path, Density on the 1000 sites), one spawned process '
+                      'per vector (%.1f s)' % (procs, args.ref_moments, dt),
+            'cpu': _cpu_model()}
     print(json.dumps(line))
     block.close()
     op.close()
@@ -1189,6 +1217,29 @@ def run_surrogate(args):
         'costs_s': {'setup': setup_s, 'dataset': gen_s, 'train': train_s,
                     'train_loss': [float(x) for x in losses]},
     }
+    if args.cpu:
+        # the reference has no surrogate: its sweep is the plain KPM at every
+        # point; the oracle port on the first held-out point's Hamiltonian
+        # (host assembly of the family), one spawned process per vector
+        procs = min(args.cpu_procs or os.cpu_count() or 1, R)
+        H = fam.hamiltonian(*Xte[0])
+        vecs = np.exp(2j * np.pi * np.random.RandomState(3)
+                      .random_sample((procs, H.shape[0])))
+        base = CpuBaseline(H, sweep.a, sweep.b, vecs, procs)
+        try:
+            base.run(8)  # spawn + load
+            _, dt = base.run(M)
+        finally:
+            base.close()
+        pt_s = dt * R / procs
+        line['cpu_baseline'] = {
+            'value': 1.0 / pt_s, 'unit': 'points/s', 'cores': procs,
+            'kind': 'port',
+            'sample': '%d of the %d vectors x %d moments of one held-out '
+                      'point (%.1f s), scaled to the point\'s %d vectors; '
+                      'plain KPM at every point (no surrogate)'
+                      % (procs, R, M, dt, R),
+            'cpu': _cpu_model()}
     print(json.dumps(line))
     return 0
 
