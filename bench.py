@@ -932,6 +932,7 @@ def run_batch(args):
     ms = float(np.median(times))
     _, nodes, vpl = bd.stats()
     fmt, ell_k = bd.step_format()
+    order = bd.work_order()
     # Kwant CSR nnz (exact zeros dropped): 4 per site onsite, 8 per
     # directed hopping block (Gamma_0 diagonal + tau_x (x) sigma_j)
     nnz = int(sum(4 * L ** 3 + 8 * 6 * L * L * (L - 1) for L in Ls))
@@ -965,6 +966,7 @@ def run_batch(args):
                                           R, M),
                    'L': [int(x) for x in Ls], 'orbitals': orbs, 'nnz': nnz,
                    'graph_nodes': nodes, 'vectors_per_lane': vpl,
+                   'work_order': order,
                    'step_format': ['BSR 4x4', 'orbital-row ELL, width %d'
                                    % ell_k,
                                    'sparse blocks (staged in shared memory)'
@@ -972,10 +974,14 @@ def run_batch(args):
                    'prepare_s': prep_s},
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm,
                      'unit': 'GB/s', 'frac': achieved / hbm,
-                     # ncu dram bytes of one BSR launch on the 2-system
-                     # (L = 37, 32) case: 2.443 GB against 2.138 GB
-                     # algorithmic, scaled by algorithmic bytes
-                     'traffic': B * (2.443 / 2.138) if fmt == 0 else None,
+                     # ncu dram bytes of BSR launches on the 2-system
+                     # (L = 37, 32) case against 2.138 GB algorithmic:
+                     # 2.697 + 0.668 GB partition-major, 2.281 + 0.664 GB
+                     # group-major; scaled by the algorithmic bytes
+                     'traffic': B * ((2.697 + 0.668) / 2.138
+                                     if order == 'partition' else
+                                     (2.281 + 0.664) / 2.138)
+                     if fmt == 0 else None,
                      'kernel': ['bsr_step_kernel', 'ell_batch_step_kernel',
                                 'sb_step_kernel'][fmt] +
                                ' (+ finalize, per graph step)',

@@ -316,6 +316,13 @@ KPM_API int kpm_batch_stats(kpm_batch* bt, double* ms, int64_t* nodes,
  * rows' vector rows staged in shared memory, products over the non-zero
  * entries only); the autotuner times all of them and keeps the fastest. */
 KPM_API int kpm_batch_format(kpm_batch* bt, int* format, int* ell_width);
+/* Work order chosen at the first kpm_batch_run (formats 0 and 1): 0 when
+ * the vector groups of a row partition run side by side (they share its
+ * matrix rows in L2), 1 when all partitions of one vector group do (the
+ * resident blocks then cover a band of rows wide enough that the gathered
+ * rows of distant neighbours, e.g. L^2 block rows away on an L^3 lattice,
+ * are still in L2).  Results do not depend on it. */
+KPM_API int kpm_batch_order(kpm_batch* bt, int* group_major);
 KPM_API int kpm_batch_destroy(kpm_batch* bt);
 
 /* ---- reconstruction (device) -------------------------------------------------

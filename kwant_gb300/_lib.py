@@ -131,6 +131,7 @@ def _load():
         'kpm_batch_run': [P, P],
         'kpm_batch_stats': [P, P, P, P],
         'kpm_batch_format': [P, P, P],
+        'kpm_batch_order': [P, P],
         'kpm_batch_destroy': [P],
         'kpm_profile': [P, I],
         'kpm_profile_read': [P, P, P],
@@ -627,6 +628,13 @@ class Batch:
         f, k = C.c_int(), C.c_int()
         check(lib.kpm_batch_format(self._b, C.byref(f), C.byref(k)))
         return f.value, k.value
+
+    def work_order(self):
+        """'partition' (the vector groups of a row partition side by side)
+        or 'group' (all partitions of one vector group side by side)."""
+        g = C.c_int()
+        check(lib.kpm_batch_order(self._b, C.byref(g)))
+        return 'group' if g.value else 'partition'
 
     def close(self):
         if getattr(self, '_b', None):

@@ -209,6 +209,13 @@ class BatchedDOS:
             return 3, 0
         return self._b.step_format()
 
+    def work_order(self):
+        """'single': the autotuner's work order ('partition' or 'group',
+        see kpm_batch_order); 'mixed': None (systems run one by one)."""
+        if self.precision == 'mixed':
+            return None
+        return self._b.work_order()
+
     def close(self):
         """Free the device state of a 'mixed' batch."""
         if self.precision == 'mixed':

@@ -125,7 +125,7 @@ template <int VPL, int PHASE, int OCC>
 __global__ void __launch_bounds__(STEP_THREADS, OCC)
 bsr_step_kernel(const SysDev* __restrict__ sys,
                 const int64_t* __restrict__ prefix, int nsys, int64_t total,
-                int64_t Rpad) {
+                int64_t Rpad, int gmajor) {
   using PT = typename Pay<VPL>::T;
   constexpr int G = 16 * VPL;
   constexpr int FLUSH = 8;       // block rows (32 orbital rows)
@@ -147,8 +147,19 @@ bsr_step_kernel(const SysDev* __restrict__ sys,
     }
     const SysDev& S = sys[lo];
     const int64_t local = w - prefix[lo];
-    const int xi = (int)(local / groups);
-    const int g = (int)(local - (int64_t)xi * groups);
+    // work order within a system: partition-major (the vector groups of a
+    // row partition side by side, sharing its block rows in L2) or
+    // group-major (all partitions of one vector group side by side, so the
+    // resident blocks cover a wider band of rows and the gathered rows of
+    // distant neighbours are still in L2); the results do not depend on it
+    int xi, g;
+    if (gmajor) {
+      g = (int)(local / S.xitems);
+      xi = (int)(local - (int64_t)g * S.xitems);
+    } else {
+      xi = (int)(local / groups);
+      g = (int)(local - (int64_t)xi * groups);
+    }
     const int64_t col = (int64_t)g * 16 + lane;
     const PT* __restrict__ X;
     const PT* P = nullptr;
@@ -394,7 +405,7 @@ template <int VPL, int PHASE>
 __global__ void __launch_bounds__(STEP_THREADS, VPL == 1 ? 6 : 4)
 ell_batch_step_kernel(const SysDev* __restrict__ sys,
                       const int64_t* __restrict__ prefix, int nsys,
-                      int64_t total, int64_t Rpad) {
+                      int64_t total, int64_t Rpad, int gmajor) {
   using PT = typename Pay<VPL>::T;
   constexpr int G = 16 * VPL;
   constexpr int FLUSH = 32;      // orbital rows
@@ -417,8 +428,14 @@ ell_batch_step_kernel(const SysDev* __restrict__ sys,
     const int KQ = K / 4;
     const int64_t rows = S.nb * BS;
     const int64_t local = w - prefix[lo];
-    const int xi = (int)(local / groups);
-    const int g = (int)(local - (int64_t)xi * groups);
+    int xi, g;                 // work order as in bsr_step_kernel
+    if (gmajor) {
+      g = (int)(local / S.xitems);
+      xi = (int)(local - (int64_t)g * S.xitems);
+    } else {
+      xi = (int)(local / groups);
+      g = (int)(local - (int64_t)xi * groups);
+    }
     const int64_t col = (int64_t)g * 16 + lane;
     const PT* __restrict__ X;
     const PT* P = nullptr;
@@ -947,6 +964,7 @@ struct kpm_batch {
   int ell = 0;               // step format: 0 BSR, 1 orbital-row ELL,
                              // 2 sparse-block (staged BSR, zeros skipped)
   int occ2 = 0;              // 1: BSR VPL-2 kernel budgeted for 2 blocks/SM
+  int gmajor = 0;            // 1: BSR work items in vector-group-major order
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int64_t nodes = 0;
@@ -1036,7 +1054,7 @@ int launch_bsr(kpm_batch* bt) {
   if (grid > total) grid = total;
   kern<<<(unsigned)grid, STEP_THREADS, 0, bt->stream>>>(
       bt->d_sys[bt->ell], bt->d_prefix[bt->ell][VPL - 1],
-      (int)bt->sys.size(), total, bt->Rpad);
+      (int)bt->sys.size(), total, bt->Rpad, bt->gmajor);
   count_launch(1);
   KPM_CHECK_LAUNCH();
   return KPM_OK;
@@ -1189,19 +1207,27 @@ int prepare(kpm_batch* bt) {
   KPM_CUDA(cudaEventCreate(&bt->e1));
   KPM_CUDA(cudaStreamSynchronize(s));
 
-  // autotuner: time three steps of each (format, VPL) variant; within a
-  // format the arithmetic is identical across VPL, and the two formats
-  // differ only in the order of the dot-product partial sums
+  // autotuner: time three steps of each (format, register budget, work
+  // order, VPL) variant; within a format the arithmetic is identical across
+  // VPL, budgets and work orders, and the two formats differ only in the
+  // order of the dot-product partial sums
   float best = 1e30f;
-  int best_fmt = 0, best_occ2 = 0;
+  int best_fmt = 0, best_occ2 = 0, best_gm = 0;
   const char* force = getenv("KPM_BATCH_FORMAT");
   int f_lo = 0, f_hi = have_ell ? 2 : 0;
   if (have_ell && force && strcmp(force, "ell") == 0) f_lo = f_hi = 1;
   if (have_ell && force && strcmp(force, "sparse") == 0) f_lo = f_hi = 2;
+  // work orders: both (BSR, ELL), or the one KPM_BATCH_ORDER names
+  const char* ord = getenv("KPM_BATCH_ORDER");
+  const int gm_only = ord && strcmp(ord, "partition") == 0 ? 0
+                      : ord && strcmp(ord, "group") == 0 ? 1 : -1;
   for (int f = f_lo; f <= f_hi; ++f)
-  for (int o2 = 0; o2 < (f ? 1 : 2); ++o2) {
+  for (int o2 = 0; o2 < (f ? 1 : 2); ++o2)
+  for (int gm = 0; gm < (f == 2 ? 1 : 2); ++gm) {
+    if (f != 2 && gm_only >= 0 && gm != gm_only) continue;
     bt->ell = f;
     bt->occ2 = o2;
+    bt->gmajor = gm;
     for (int vpl = 1; vpl <= 2; ++vpl) {
       if (bt->Rpad % (16 * vpl)) continue;
       if (o2 && vpl == 1) continue;
@@ -1221,11 +1247,13 @@ int prepare(kpm_batch* bt) {
         bt->vpl = vpl;
         best_fmt = f;
         best_occ2 = o2;
+        best_gm = gm;
       }
     }
   }
   bt->ell = best_fmt;
   bt->occ2 = best_occ2;
+  bt->gmajor = best_gm;
   // keep only the chosen format's matrices (the sparse-block kernel reads
   // the BSR block columns and its own entries)
   for (auto& y : bt->sys) {
@@ -1459,6 +1487,12 @@ int kpm_batch_format(kpm_batch* bt, int* format, int* ell_width) {
   *ell_width = 0;
   if (bt->ell == 1)
     for (auto& y : bt->sys) *ell_width = std::max(*ell_width, y.ell_k);
+  return KPM_OK;
+}
+
+int kpm_batch_order(kpm_batch* bt, int* group_major) {
+  KPM_REQUIRE(bt && group_major, "kpm_batch_order: null argument");
+  *group_major = bt->gmajor;
   return KPM_OK;
 }
 

@@ -148,6 +148,29 @@ def test_sparse_blocks_run_as_orbital_ell(monkeypatch):
         assert np.max(np.abs(m_sb[s] - ref)) / np.max(np.abs(ref)) < 1e-5
 
 
+def test_work_orders_give_identical_moments(monkeypatch):
+    """The two work orders of the BSR and ELL step kernels (a partition's
+    vector groups side by side, or all partitions of a vector group side by
+    side) change only which block computes what when: the moments are
+    bit-identical, and the batch reports the order it ran."""
+    from kwant_gb300 import batch
+    R, M, seed = 64, 24, 4
+    mats = [_host_wilson_dirac(6, 1.5, 1.5, 2), _host_wilson_dirac(4, 1.5, 0.3, 3)]
+
+    def run(fmt, order):
+        monkeypatch.setenv('KPM_BATCH_FORMAT', fmt)
+        monkeypatch.setenv('KPM_BATCH_ORDER', order)
+        bd = batch.BatchedDOS(R, M, seed=seed)
+        for H in mats:
+            bd.add_matrix(H, _gershgorin(H))
+        mom = bd.moments()
+        assert bd.work_order() == order
+        return mom
+
+    for fmt in ('bsr', 'ell'):
+        assert np.array_equal(run(fmt, 'partition'), run(fmt, 'group')), fmt
+
+
 def test_dense_blocks_stay_bsr():
     from kwant_gb300 import batch
     rng = np.random.RandomState(0)
