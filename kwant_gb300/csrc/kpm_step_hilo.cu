@@ -262,17 +262,28 @@ cheb_step_hilo_kernel(StepArgs p, HiloArgs q,
     }
   };
 
-  // partition-major work order: the sub-groups of a row partition run
-  // side by side (they share the partition's ELL rows in L2).  Measured on
-  // the 2e6-orbital graphene workload, R = 64: 1.08 ms per step against
-  // 1.12 ms sub-group-major; blocks of 192 or 160 threads (3 or 4 per SM)
-  // were slower still (1.15-1.22 ms), and so were blocks of 128 threads at
-  // 4 or 5 per SM (1.03 and 1.33 ms against 1.01 ms).  The gathered hi
-  // slices are copied through L2 only (cp.async.cg): 1.026 -> 1.010 ms
-  // against copies that also allocate in L1 (15 % L1 hit rate)
+  // work order: pairs of sub-groups, partition by partition (the two
+  // sub-groups of a partition run side by side and share its ELL rows in
+  // L2), the next pair after all partitions.  Against all sub-groups of a
+  // partition side by side, the resident blocks then cover twice as many
+  // consecutive rows, so more of the gathered neighbours are still in L2,
+  // for one more read of the ELL rows per pair.  Measured on the 2e6-orbital
+  // graphene workload: R = 64 0.973 ms per step against 0.987 (0.713 /
+  // 0.703 of HBM), R = 128 1.961 against 2.135 ms; one sub-group at a time
+  // took 1.029 ms (R = 64).  The Wilson-Dirac systems (R = 256, width 16):
+  // 7.05 s against 7.14 s per run of four.  Results are identical in every
+  // order.  Blocks of 192 or 160 threads (3 or 4 per SM) were slower
+  // (1.15-1.22 ms at the time), and so were blocks of 128 threads at 4 or 5
+  // per SM (1.03 and 1.33 ms against 1.01 ms).  The gathered hi slices are
+  // copied through L2 only (cp.async.cg): 1.026 -> 1.010 ms against copies
+  // that also allocate in L1 (15 % L1 hit rate)
+  const int pair = p.groups < 2 ? p.groups : 2;
   for (int w = blockIdx.x; w < work; w += gridDim.x) {
-    const int xi = w / p.groups;
-    const int g = w - xi * p.groups;
+    const int g0 = (w / (p.xitems * pair)) * pair;   // first of this pair
+    const int npair = p.groups - g0 < pair ? p.groups - g0 : pair;
+    const int rem = w - g0 * p.xitems;               // < xitems * npair
+    const int xi = rem / npair;
+    const int g = g0 + (rem - xi * npair);
     const int col = g * SW + lane;
     double* my = red + slot * (G * 3) + lane * 6;   // vectors 2 lane, +1
 #pragma unroll
