@@ -374,16 +374,16 @@ def run_ours(args):
     B = step_bytes(nnz, n, R, args.precision)
     avg_step_ms = step_ms / max(n_step, 1)
     achieved = B / (avg_step_ms / 1e3) / 1e9
-    # DRAM bytes per step launch: ncu dram__bytes_read + dram__bytes_write
-    # of one step launch on the 500 x 500-cell, R = 64 case (the workload
-    # here is too large for a multi-pass capture), scaled to this launch by
-    # its algorithmic bytes: cheb_step_hilo_kernel 913.2 + 353.1 MB against
-    # 1178.0 MB ('mixed'), cheb_step_ell_kernel 774.5 MB against 794.0 MB
-    # ('single')
+    # DRAM bytes per step launch, ncu dram__bytes_read + dram__bytes_write:
+    # 'mixed', a one-pass capture of two step launches of this default
+    # workload (1000 x 1000 cells, R = 64): 3.813 + 1.501 GB against 4.712
+    # GB algorithmic; 'single', one launch on the 500 x 500-cell case,
+    # 774.5 MB against 794.0 MB, scaled by the algorithmic bytes
     traffic = None
     if args.reorder and R == 64:
         if args.precision == 'mixed':
-            traffic = B * ((913.2 + 353.1) / 1178.0)
+            traffic = B * ((3.813 + 1.501) / 4.712) if args.cells == 1000 \
+                else None
         elif args.precision == 'single':
             traffic = B * (774.5 / 794.0)
 
