@@ -71,7 +71,11 @@ void count_launch(int n);
 // compensated step runs two 256-thread blocks per SM, and 2 partitions per
 // SM give each block half as many pipeline starts and block reductions as 4
 // (graphene, 2e6 orbitals, R = 64: 1.000 -> 0.985 ms per step); the other
-// steps keep 4.
+// steps keep 4.  One partition per SM is faster still when the blocks hold
+// two or more 16-vector sub-groups (0.971 -> 0.921 ms at R = 64, 0.479 ->
+// 0.457 at R = 32) but leaves half of the resident blocks idle at R <= 16
+// (0.232 -> 0.336 ms at R = 16); since the count must not depend on R, it
+// stays at 2.
 int dos_xitems(const kpm_handle* h, int64_t rows);
 // event pair around the next launch when profiling (*e1: closing event)
 int prof_begin(kpm_handle* h, cudaEvent_t* e1);
